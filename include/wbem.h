@@ -1,0 +1,146 @@
+/*
+ * wbem.h - C ABI of the GB300 (sm_103a) collocation BEM library.
+ *
+ * This is the drop-in boundary under WaveBEM's BEMProblem<3>
+ * (include/bem_problem.h:87-180 of the reference). Every entry point takes
+ * plain host pointers and sizes, returns an int status (WBEM_OK = 0) and keeps
+ * its device memory inside an opaque handle. One handle serves one thread at a
+ * time; handles share no state. Nothing here falls back to the CPU: without a
+ * usable CUDA device wbem_create fails with WBEM_ERR_CUDA.
+ *
+ * Conventions (identical to the reference's):
+ *   - X[3*i+d]: support point of dof i (reference position plus Eulerian
+ *     displacement, i.e. what DoFTools::map_dofs_to_support_points returns with
+ *     the MappingQEulerian).
+ *   - cells[4*c+k]: dof of local vertex k of cell c in deal.II lexicographic
+ *     order (0:(0,0) 1:(1,0) 2:(0,1) 3:(1,1)); the cell normal is
+ *     d x/d xi  x  d x/d eta normalised. A cell whose direction_flag() is false
+ *     is passed with vertices (0,2,1,3).
+ *   - double nodes: CSR (dn_ptr[N+1], dn_idx) with row i = double_nodes_set[i]
+ *     in ascending order (source/computational_domain.cc:258-307).
+ *   - dirichlet_mask[i] = comp_dom.surface_nodes(i) (1 on Dirichlet nodes);
+ *     other_nodes = 1 - surface_nodes.
+ *   - tmp_rhs: phi on Dirichlet nodes, dphi/dn on Neumann nodes.
+ *   - Matrices exported row-major N x N in the caller's dof order.
+ */
+#ifndef WBEM_H
+#define WBEM_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define WBEM_OK 0
+#define WBEM_ERR_ARG 1        /* invalid argument (sizes, indices, NULL pointers) */
+#define WBEM_ERR_STATE 2      /* call out of order (e.g. solve before assemble) */
+#define WBEM_ERR_CUDA 3       /* CUDA runtime error / no device */
+#define WBEM_ERR_NOMEM 4      /* device allocation failed */
+#define WBEM_ERR_SINGULAR 5   /* zero or non-finite pivot */
+#define WBEM_ERR_NOCONV 6     /* iterative solver hit max_steps (SolverControl::NoConvergence) */
+#define WBEM_ERR_NONFINITE 7  /* non-finite input or result */
+#define WBEM_ERR_TIMEOUT 8    /* a bounded device wait gave up */
+
+/* precision forms */
+#define WBEM_PREC_FP64 0  /* plain: FP64 everywhere */
+#define WBEM_PREC_MIXED 1 /* FP32 far field (double-float panel base + FP32 quadrature deltas),
+                             FP64 singular/near field and alpha, FP32 LU with BF16x3
+                             tensor-core updates, FP64 GMRES iterative refinement */
+
+/* linear solvers */
+#define WBEM_SOLVER_AUTO 0  /* FP64 -> GMRES; MIXED -> LU + GMRES-IR */
+#define WBEM_SOLVER_GMRES 1 /* FP64 GMRES(restart), block-Jacobi preconditioner */
+#define WBEM_SOLVER_LU 2    /* dense LU (FP64 or mixed) refined by FP64 GMRES */
+
+typedef struct wbem_context* wbem_handle;
+
+typedef struct {
+  int precision;                 /* WBEM_PREC_* */
+  int solver;                    /* WBEM_SOLVER_* */
+  int quadrature_order;          /* "Quadrature order" (Gauss points per direction), 4 */
+  int singular_quadrature_order; /* "Singular quadrature order", 5 */
+  int gmres_restart;             /* SolverGMRES AdditionalData(100) */
+  int max_steps;                 /* SolverControl "Max steps" */
+  double tolerance;              /* SolverControl "Tolerance" (absolute, on the residual) */
+  double near_field_ratio;       /* MIXED: a panel is near when |x_i - centre| < ratio * diameter */
+  int keep_matrices;             /* keep FP64 N (dG/dn) and D (G) for wbem_get_matrices */
+  int reserved[7];
+} wbem_options;
+
+typedef struct {
+  double t_geometry_ms, t_assemble_ms, t_singular_ms, t_alpha_ms, t_system_ms;
+  double t_factor_ms, t_solve_ms, t_adjoint_ms;
+  int iterations;           /* GMRES iterations of the last solve */
+  double residual;          /* final residual norm of the last solve */
+  int kernel_launches;      /* kernels launched by the last assemble+solve */
+  int n_dofs, n_cells;
+  int reserved[8];
+} wbem_stats;
+
+/* Defaults of prm-files/default.prm:217-230 plus library choices. */
+int wbem_default_options(wbem_options* opt);
+
+/* Create / destroy a handle on CUDA device `device`. */
+int wbem_create(wbem_handle* h, int device);
+int wbem_destroy(wbem_handle h);
+/* Text of the last error of this handle (never NULL). */
+const char* wbem_last_error(wbem_handle h);
+
+/*
+ * Mesh and double nodes. Replaces the implicit inputs BEMProblem reads from
+ * ComputationalDomain: dh/fe/mapping support points, cell dof indices and
+ * double_nodes_set (source/bem_problem.cc:168-169, :223-230). dn_ptr/dn_idx
+ * may be NULL, in which case the library finds the double nodes itself with
+ * the reference's rule (boundary dofs, coincidence below 1e-8).
+ */
+int wbem_set_geometry(wbem_handle h, const double* X, int n_dofs, const int* cells, int n_cells,
+                      const int* dn_ptr, const int* dn_idx);
+/* New support points for the same topology (the Eulerian map_points update). */
+int wbem_update_nodes(wbem_handle h, const double* X);
+/* surface_nodes (1 = Dirichlet). Mutable between solves, like the reference's. */
+int wbem_set_bc(wbem_handle h, const unsigned char* dirichlet_mask);
+
+/* BEMProblem::assemble_system + compute_alpha (source/bem_problem.cc:106-618),
+ * plus, for the LU solvers, the factorisation of the system. */
+int wbem_assemble(wbem_handle h, const wbem_options* opt);
+
+/* BEMProblem::solve_system (source/bem_problem.cc:821-895): unknown entries of
+ * phi (Neumann nodes) and dphi_dn (Dirichlet nodes) are written, the others are
+ * left untouched. Reuses the current assembly (and its factors). */
+int wbem_solve_system(wbem_handle h, const double* tmp_rhs, double* phi, double* dphi_dn);
+
+/* BEMProblem::solve (source/bem_problem.cc:969-987): assemble + solve_system. */
+int wbem_solve(wbem_handle h, const wbem_options* opt, const double* tmp_rhs, double* phi,
+               double* dphi_dn);
+
+/* alpha (source/bem_problem.cc:594-618), N values. */
+int wbem_get_alpha(wbem_handle h, double* alpha);
+/* neumann_matrix / dirichlet_matrix (include/bem_problem.h:153-154), row-major
+ * N x N, caller order. Needs keep_matrices = 1 (or the FP64 form). Either
+ * pointer may be NULL. */
+int wbem_get_matrices(wbem_handle h, double* neumann, double* dirichlet);
+/* BEMProblem::vmult (source/bem_problem.cc:620-670) and compute_rhs (:673-811). */
+int wbem_vmult(wbem_handle h, const double* src, double* dst);
+int wbem_compute_rhs(wbem_handle h, const double* src, double* dst);
+
+/* Hull force F = sum over cells hull_cells[k] of  int p n_dir dS,
+ * p = -(U . grad phi + |grad phi|^2 / 2) (steady, rho = 1, g = 0 form of
+ * source/free_surface.cc:6936-6942); dir = 0,1,2 selects the force component. */
+int wbem_hull_force(wbem_handle h, const int* hull_cells, int n_hull, const double* U, int dir,
+                    const double* phi, const double* dphi_dn, double* force);
+
+/* Adjoint of assemble + solve_system + hull force, at the current solution of
+ * the last wbem_solve / wbem_solve_system with tmp_rhs: returns dF/dX (N x 3,
+ * with tmp_rhs held fixed) and dF/dtmp_rhs (N). Reuses the factors for the
+ * transposed solve and recomputes matrix tiles (no dG/dX storage). */
+int wbem_force_adjoint(wbem_handle h, const int* hull_cells, int n_hull, const double* U, int dir,
+                       const double* tmp_rhs, double* dF_dX, double* dF_drhs);
+
+int wbem_get_stats(wbem_handle h, wbem_stats* st);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WBEM_H */

@@ -1,0 +1,99 @@
+// Library handle: host-side topology, device buffers and solver state.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+#include "../../include/wbem.h"
+#include "kernels.h"
+
+struct wbem_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  wbem_stats stats{};
+  wbem_options opt{};
+
+  // ---- host topology (caller order)
+  int N = 0, C = 0;
+  std::vector<double> X;
+  std::vector<int> cells;
+  std::vector<int> dn_ptr, dn_idx;
+  std::vector<unsigned char> mask;
+  bool have_mask = false;
+  // internal order: perm[internal] = caller dof, iperm[caller] = internal dof
+  std::vector<int> perm, iperm;
+  int n_tiles = 0;
+
+  // ---- device topology / geometry (internal order)
+  double* d_X = nullptr;        // N x 3
+  int4* d_cell_dofs = nullptr;  // C
+  int* d_dnset = nullptr;       // N x kMaxSet
+  int* d_tile_ptr = nullptr;    // n_tiles + 1
+  int2* d_tile_ent = nullptr;
+  int* d_sptr = nullptr;        // singular panels per row (CSR)
+  int* d_scell = nullptr;
+  int* d_perm = nullptr;        // internal -> caller
+  int* d_iperm = nullptr;       // caller -> internal
+  int* d_ncptr = nullptr;       // node -> (cell, local vertex) CSR, internal nodes
+  int* d_ncent = nullptr;
+  uint8_t* d_mask = nullptr;
+  double* d_rec = nullptr;      // FP64 panel records
+  float* d_rec32 = nullptr;     // mixed panel records
+  double* d_cellc = nullptr;    // mixed: panel centre / normal / moments (double-float source)
+  float* d_cellgeo = nullptr;   // mixed: centre (float), radius^2 for the near test
+  size_t rec_cells = 0;
+
+  // ---- matrices (internal order)
+  double* d_N = nullptr;
+  double* d_D = nullptr;
+  float2* d_N2 = nullptr;
+  float2* d_D2 = nullptr;
+  double* d_alpha = nullptr;
+  double* d_alpha_part = nullptr;
+  double* d_alpha_near = nullptr;
+  double* d_alpha_sing = nullptr;
+  int* d_near_cnt = nullptr;
+  int* d_near_cells = nullptr;
+  int near_cap = 0;
+  size_t mat_elems = 0;       // allocated N*N (fp64 or float2)
+  int assembled_prec = -1;    // precision of the current assembly, -1 = none
+  bool factors_valid = false;
+
+  // ---- constraints (internal order)
+  int n_crows = 0;
+  int* d_crow = nullptr;
+  int* d_cptr = nullptr;
+  int* d_ccol = nullptr;
+  double* d_cval = nullptr;
+  double* d_cinh = nullptr;
+  uint8_t* d_cflag = nullptr;
+  int* d_cptr_full = nullptr;
+  int* d_ccol_full = nullptr;
+  double* d_cval_full = nullptr;
+  int* d_tptr = nullptr;   // transposed constraint entries (by column)
+  int* d_tsrc = nullptr;
+  double* d_tval = nullptr;
+  size_t cons_cap_rows = 0, cons_cap_ent = 0;
+
+  // ---- solver workspaces
+  double* d_binv = nullptr;
+  double* d_V = nullptr;   // (restart + 1) x N Krylov basis
+  int V_cap = 0;
+  double* d_vec[8] = {};   // N-vectors
+  double* d_part = nullptr;
+  double* d_small = nullptr;
+  float* d_lu = nullptr;   // mixed LU factors
+  uint16_t* d_split = nullptr;
+  float* d_lutmp = nullptr;
+  int* d_info = nullptr;
+  size_t lu_elems = 0;
+  // last solution (internal order), kept for the adjoint
+  double* d_sol = nullptr;
+  double* d_rhs = nullptr;
+  double* d_b = nullptr;   // known data (internal order)
+  bool have_solution = false;
+
+  wbem::DevErr* d_err = nullptr;
+  int launches = 0;
+};

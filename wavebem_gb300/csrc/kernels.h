@@ -1,0 +1,157 @@
+// Launch wrappers shared between the CUDA translation units and the host
+// orchestration (wbem_api.cu). All pointers are device pointers in the
+// library's internal dof order unless stated otherwise.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "common.cuh"
+
+namespace wbem {
+
+constexpr int kRowsPerTile = 128;  // collocation rows per assembly CTA (one per thread)
+constexpr int kColsPerTile = 64;   // matrix columns (dofs) per assembly CTA
+constexpr int kMaxSet = 8;         // max size of a double-node set
+constexpr int kMaxQ1 = 8;          // max regular quadrature order per direction
+constexpr int kMaxSingular = 2 * 8 * 8;  // max points of a vertex-singular rule
+constexpr int kBJ = 128;           // block-Jacobi block size
+
+// quadrature tables (constant memory, per translation unit that uses them)
+struct QuadTables {
+  int q1;                            // regular order per direction
+  int nsp;                           // points of each vertex-singular rule
+  double gp[kMaxQ1 * kMaxQ1][3];     // regular rule: xi, eta, w
+  double phi[kMaxQ1 * kMaxQ1][4];    // shape values at the regular points
+  double sp[4][kMaxSingular][3];     // singular rules per vertex: xi, eta, w
+};
+
+cudaError_t upload_quadrature(const QuadTables& t);
+
+// ---- assembly (FP64 plain form)
+cudaError_t launch_cell_records_fp64(int C, const double* X, const int4* cell_dofs, double* rec,
+                                     int q1, cudaStream_t s);
+cudaError_t launch_tile_fp64(int N, int q1, const double* X, const int* dnset, int n_tiles,
+                             const int* tile_ptr, const int2* tile_ent, const int4* cell_dofs,
+                             const double* rec, double* Nm, double* Dm, DevErr* err,
+                             cudaStream_t s);
+cudaError_t launch_singular_fp64(int N, const double* X, const int* dnset, const int* sptr,
+                                 const int* scell, const int4* cell_dofs, double* Nm, double* Dm,
+                                 DevErr* err, cudaStream_t s);
+cudaError_t launch_alpha_rowsum(int N, const double* Nm, double* alpha, cudaStream_t s);
+
+// ---- assembly (mixed form): N2/D2 hold (hi, lo) float pairs
+cudaError_t launch_cell_records_mixed(int C, const double* X, const int4* cell_dofs, float* rec32,
+                                      double* cellc, float* cellgeo, int q1, cudaStream_t s);
+cudaError_t launch_tile_mixed(int N, int q1, const double* X, const int* dnset, int n_tiles,
+                              const int* tile_ptr, const int2* tile_ent, const int4* cell_dofs,
+                              const float* rec32, const double* cellc, const float* cellgeo,
+                              float ratio, float2* N2, float2* D2, double* alpha_part,
+                              DevErr* err, cudaStream_t s);
+cudaError_t launch_near_mixed(int N, const double* X, const int* dnset, int C,
+                              const int4* cell_dofs, const float* cellgeo, float ratio,
+                              const double* rec64, int near_cap, int* near_cnt, int* near_cells,
+                              float2* N2, float2* D2, double* alpha_near, DevErr* err,
+                              cudaStream_t s);
+cudaError_t launch_singular_mixed(int N, const double* X, const int* dnset, const int* sptr,
+                                  const int* scell, const int4* cell_dofs, float2* N2, float2* D2,
+                                  double* alpha_sing, DevErr* err, cudaStream_t s);
+cudaError_t launch_alpha_mixed(int N, int n_tiles, const double* alpha_part,
+                               const double* alpha_near, const double* alpha_sing, double* alpha,
+                               cudaStream_t s);
+
+// ---- operators and solver pieces
+// y = sum_j sel(i,j) x_j (+ diagonal term), sel per mode:
+//   mode 0 (system, vmult):   mask_j ? -D_ij : N_ij ; y_i += (1-mask_i) alpha_i x_i
+//   mode 1 (rhs):             mask_j ? -N_ij : D_ij ; y_i -= mask_i alpha_i x_i
+cudaError_t launch_matvec_fp64(int N, int mode, const double* Nm, const double* Dm,
+                               const uint8_t* mask, const double* alpha, const double* x,
+                               double* y, cudaStream_t s);
+cudaError_t launch_matvec_mixed(int N, int mode, const float2* N2, const float2* D2,
+                                const uint8_t* mask, const double* alpha, const double* x,
+                                double* y, cudaStream_t s);
+// transposed system operator: y_j = sum_i sel(i,j) x_i (+ diagonal)
+cudaError_t launch_matvec_t_fp64(int N, const double* Nm, const double* Dm, const uint8_t* mask,
+                                 const double* alpha, const double* x, double* y, double* part,
+                                 cudaStream_t s);
+cudaError_t launch_matvec_t_mixed(int N, const float2* N2, const float2* D2, const uint8_t* mask,
+                                  const double* alpha, const double* x, double* y, double* part,
+                                  cudaStream_t s);
+// constrained rows: y_i = x_i - sum c_ij x_j
+cudaError_t launch_constraint_rows(int nrows, const int* crow, const int* cptr, const int* ccol,
+                                   const double* cval, const double* x, double* y,
+                                   cudaStream_t s);
+// constrained rows of the transposed operator (scatter form, deterministic)
+cudaError_t launch_constraint_rows_t(int N, int nrows, const int* crow, const int* cptr,
+                                     const int* ccol, const double* cval, const int* tptr,
+                                     const int* tsrc, const double* tval,
+                                     const uint8_t* cflag, const double* x, double* y,
+                                     cudaStream_t s);
+cudaError_t launch_set_rows(int nrows, const int* crow, const double* val, double* y,
+                            cudaStream_t s);
+
+// block-Jacobi (FP64)
+cudaError_t launch_bj_build(int N, const double* Nm, const double* Dm, const float2* N2,
+                            const float2* D2, const uint8_t* mask, const double* alpha,
+                            const uint8_t* cflag, const int* cptr_full, const int* ccol_full,
+                            const double* cval_full, double* binv, DevErr* err, cudaStream_t s);
+cudaError_t launch_bj_apply(int N, const double* binv, const double* x, double* y, int transpose,
+                            cudaStream_t s);
+
+// Krylov helpers (FP64)
+cudaError_t launch_multidot(int N, int k, const double* V, const double* w, double* part,
+                            double* out, cudaStream_t s);
+cudaError_t launch_axpy_basis(int N, int k, const double* V, const double* h, double* w,
+                              double sign, cudaStream_t s);
+cudaError_t launch_scale(int N, const double* x, double a, double* y, cudaStream_t s);
+cudaError_t launch_axpby(int N, double a, const double* x, double b, double* y, cudaStream_t s);
+cudaError_t launch_nrm2(int N, const double* x, double* part, double* out, cudaStream_t s);
+cudaError_t launch_gather(int N, const int* idx, const double* x, double* y, cudaStream_t s);
+cudaError_t launch_scatter(int N, const int* idx, const double* x, double* y, cudaStream_t s);
+// out[r][q] = A[ip[r0 + r]][ip[q]] for r < nr (caller-order rows of an
+// internal-order matrix; A2 = (hi, lo) pairs when A is NULL)
+cudaError_t launch_gather_rows(int N, int r0, int nr, const int* ip, const double* A,
+                               const float2* A2, double* out, cudaStream_t s);
+
+// LU (mixed): FP32 no-pivot blocked LU with BF16x3 tensor-core trailing updates
+struct LuWork {
+  float* A;          // N x N row-major, in place
+  uint16_t* Lhi;     // panel splits (bf16 bits)
+  uint16_t* Llo;
+  uint16_t* Uhi;
+  uint16_t* Ulo;
+  int* info;
+};
+cudaError_t launch_form_lu_input(int N, const float2* N2, const float2* D2, const double* Nm,
+                                 const double* Dm, const uint8_t* mask, const double* alpha,
+                                 const uint8_t* cflag, const int* cptr_full, const int* ccol_full,
+                                 const double* cval_full, float* A, cudaStream_t s);
+int lu_factor_mixed(int N, LuWork& w, DevErr* err, cudaStream_t s, int* launches);
+cudaError_t launch_lu_solve(int N, const float* LU, const double* b, double* x, float* tmp,
+                            int transpose, cudaStream_t s);
+// tensor-core GEMM C -= A*B (BF16x3 split), exposed for tests
+cudaError_t launch_gemm_bf16x3(int M, int Ncols, int K, const uint16_t* Ahi, const uint16_t* Alo,
+                               int lda, const uint16_t* Bhi, const uint16_t* Blo, int ldb,
+                               float* Cm, int ldc, DevErr* err, cudaStream_t s);
+
+// hull force and adjoint
+cudaError_t launch_hull_force(int nh, const int4* hull_dofs, const double* X, const double* U,
+                              int dir, const double* phi, const double* dphi, double* part,
+                              cudaStream_t s);
+cudaError_t launch_hull_force_grad(int nh, const int4* hull_dofs, const double* X,
+                                   const double* U, int dir, const double* phi, const double* dphi,
+                                   double* gX_cell, double* gphi_cell, double* gdphi_cell,
+                                   cudaStream_t s);
+cudaError_t launch_adjoint_tiles(int N, int q1, const double* X, const int* dnset, int C,
+                                 const int4* cell_dofs, const double* lambda, const double* phi,
+                                 const double* dphi, const uint8_t* rowmask, double* gX_row,
+                                 double* gX_cell_part, int row_blocks, DevErr* err,
+                                 cudaStream_t s);
+cudaError_t launch_adjoint_singular(int N, const double* X, const int* dnset, const int* sptr,
+                                    const int* scell, const int4* cell_dofs,
+                                    const double* lambda, const double* phi, const double* dphi,
+                                    const uint8_t* rowmask, double* gX_row, double* gX_sing,
+                                    DevErr* err, cudaStream_t s);
+cudaError_t launch_reduce_cell_grad(int N, int C, int row_blocks, const double* gX_cell_part,
+                                    const double* gX_sing, const int* ncptr, const int* ncent,
+                                    const double* gX_row, double* gX, cudaStream_t s);
+
+}  // namespace wbem

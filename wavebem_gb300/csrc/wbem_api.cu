@@ -1,0 +1,1273 @@
+// C ABI of the library (include/wbem.h): host orchestration of the device
+// kernels. Host work here is limited to mesh topology bookkeeping (dof
+// renumbering, panel lists, double-node sets, constraint lines), argument
+// validation and the small least-squares updates of GMRES; every O(N^2) or
+// O(N C) operation runs on the GPU.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <set>
+#include <unordered_map>
+#include <vector>
+#include "context.h"
+
+using namespace wbem;
+
+namespace wbem {
+cudaError_t upload_quadrature_fp64(const QuadTables& t);
+cudaError_t upload_quadrature_mixed(const QuadTables& t);
+cudaError_t upload_quadrature_adjoint(const QuadTables& t);
+int solve_mixed(wbem_context* h, const double* d_rhs, double* d_x, int transpose);
+int assemble_mixed(wbem_context* h);
+int factor_mixed(wbem_context* h);
+void free_mixed(wbem_context* h);
+int adjoint_force(wbem_context* h, const int* hull_cells, int n_hull, const double* U, int dir,
+                  const double* tmp_rhs, double* dF_dX, double* dF_drhs);
+int hull_force_dev(wbem_context* h, const int* hull_cells, int n_hull, const double* U, int dir,
+                   const double* d_phi, const double* d_dphi, double* force);
+}  // namespace wbem
+
+// ------------------------------------------------------------------ errors
+static int fail(wbem_context* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+#define CU(call)                                                                            \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess)                                                                  \
+      return fail(h, e_ == cudaErrorMemoryAllocation ? WBEM_ERR_NOMEM : WBEM_ERR_CUDA,      \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));                      \
+  } while (0)
+
+#define CHK(expr)               \
+  do {                          \
+    int s_ = (expr);            \
+    if (s_ != WBEM_OK) return s_; \
+  } while (0)
+
+namespace wbem {
+
+int check_device_error(wbem_context* h, const char* what) {
+  cudaError_t e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess)
+    return fail(h, WBEM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  DevErr de;
+  e = cudaMemcpy(&de, h->d_err, sizeof(DevErr), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess)
+    return fail(h, WBEM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  if (de.code != 0) {
+    char buf[256];
+    snprintf(buf, sizeof buf, "%s: device error %d at site %d (%d, %d)", what, de.code, de.where,
+             de.a, de.b);
+    DevErr z{};
+    cudaMemcpy(h->d_err, &z, sizeof z, cudaMemcpyHostToDevice);
+    return fail(h, de.code, buf);
+  }
+  return WBEM_OK;
+}
+
+template <typename T>
+int dev_alloc(wbem_context* h, T** p, size_t n) {
+  if (*p) {
+    cudaFree(*p);
+    *p = nullptr;
+  }
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return fail(h, WBEM_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
+  return WBEM_OK;
+}
+
+template <typename T>
+int upload(wbem_context* h, T** p, const std::vector<T>& v) {
+  CHK(dev_alloc(h, p, v.size()));
+  if (!v.empty()) CU(cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return WBEM_OK;
+}
+
+}  // namespace wbem
+
+// ------------------------------------------------------------ quadrature
+// Gauss-Legendre points and weights on [0,1] (Newton on the Legendre
+// recurrence), ascending.
+static void gauss_legendre01(int n, std::vector<double>& x, std::vector<double>& w) {
+  x.resize(n);
+  w.resize(n);
+  const long double pi = 3.141592653589793238462643383279502884L;
+  for (int i = 0; i < n; ++i) {
+    long double z = cosl(pi * (i + 0.75L) / (n + 0.5L)), dp = 1;
+    for (int it = 0; it < 100; ++it) {
+      long double p0 = 1, p1 = z;
+      if (n == 1) p1 = z, p0 = 1;
+      long double pn = (n == 0) ? 1 : z, pm = 1;
+      for (int k = 2; k <= n; ++k) {
+        long double pk = ((2 * k - 1) * z * pn - (k - 1) * pm) / k;
+        pm = pn;
+        pn = pk;
+      }
+      (void)p0;
+      (void)p1;
+      dp = n * (z * pn - pm) / (z * z - 1);
+      long double dz = pn / dp;
+      z -= dz;
+      if (fabsl(dz) < 1e-20L) break;
+    }
+    x[i] = (double)((1 - z) / 2);
+    w[i] = (double)(1 / ((1 - z * z) * dp * dp));
+  }
+}
+
+static int build_quadrature(wbem_context* h, int q1, int sorder) {
+  if (q1 < 1 || q1 > kMaxQ1) return fail(h, WBEM_ERR_ARG, "quadrature_order must be in [1,8]");
+  if (sorder < 1 || 2 * sorder * sorder > kMaxSingular)
+    return fail(h, WBEM_ERR_ARG, "singular_quadrature_order must be in [1,8]");
+  QuadTables t{};
+  t.q1 = q1;
+  std::vector<double> x, w;
+  gauss_legendre01(q1, x, w);
+  for (int b = 0; b < q1; ++b)
+    for (int a = 0; a < q1; ++a) {
+      const int q = a + q1 * b;
+      const double s = x[a], u = x[b];
+      t.gp[q][0] = s;
+      t.gp[q][1] = u;
+      t.gp[q][2] = w[a] * w[b];
+      t.phi[q][0] = (1 - s) * (1 - u);
+      t.phi[q][1] = s * (1 - u);
+      t.phi[q][2] = (1 - s) * u;
+      t.phi[q][3] = s * u;
+    }
+  // vertex-singular rules (polar map of the two triangles at the vertex, with
+  // the 1/R weight folded into the weights), see the oracle for the derivation
+  std::vector<double> sx, sw;
+  gauss_legendre01(sorder, sx, sw);
+  const int m = sorder * sorder;
+  t.nsp = 2 * m;
+  const double pi4 = 0.78539816339744830962;
+  for (int v = 0; v < 4; ++v) {
+    for (int b = 0; b < sorder; ++b)
+      for (int a = 0; a < sorder; ++a) {
+        const int q = a + sorder * b;
+        const double u = sx[a], th = pi4 * sx[b];
+        const double px = u, py = u * std::tan(th);
+        double wq = sw[a] * sw[b] * pi4 / std::cos(th) * std::sqrt(px * px + py * py);
+        double pts[2][2] = {{px, py}, {py, px}};
+        for (int half = 0; half < 2; ++half) {
+          double X0 = pts[half][0], Y0 = pts[half][1], Xr = X0, Yr = Y0;
+          if (v == 1) { Xr = 1 - Y0; Yr = X0; }
+          if (v == 2) { Xr = Y0; Yr = 1 - X0; }
+          if (v == 3) { Xr = 1 - X0; Yr = 1 - Y0; }
+          t.sp[v][half * m + q][0] = Xr;
+          t.sp[v][half * m + q][1] = Yr;
+          t.sp[v][half * m + q][2] = wq;
+        }
+      }
+  }
+  CU(upload_quadrature_fp64(t));
+  CU(upload_quadrature_mixed(t));
+  CU(upload_quadrature_adjoint(t));
+  return WBEM_OK;
+}
+
+// ------------------------------------------------------------- topology
+static void find_double_nodes(int N, const double* X, int C, const int* cells,
+                              std::vector<int>& ptr, std::vector<int>& idx) {
+  // boundary dofs: nodes on an edge used by exactly one cell
+  std::map<std::pair<int, int>, int> ecount;
+  const int E[4][2] = {{0, 1}, {1, 3}, {3, 2}, {2, 0}};
+  for (int c = 0; c < C; ++c)
+    for (int e = 0; e < 4; ++e) {
+      int a = cells[4 * c + E[e][0]], b = cells[4 * c + E[e][1]];
+      if (a > b) std::swap(a, b);
+      ecount[{a, b}]++;
+    }
+  std::vector<char> bnd(N, 0);
+  for (auto& kv : ecount)
+    if (kv.second == 1) bnd[kv.first.first] = bnd[kv.first.second] = 1;
+  const double tol = 1e-8, cell = 1e-6;
+  struct Key {
+    long long x, y, z;
+    bool operator==(const Key& o) const { return x == o.x && y == o.y && z == o.z; }
+  };
+  struct KH {
+    size_t operator()(const Key& k) const {
+      return (size_t)(k.x * 73856093LL) ^ (size_t)(k.y * 19349663LL) ^ (size_t)(k.z * 83492791LL);
+    }
+  };
+  std::unordered_map<Key, std::vector<int>, KH> grid;
+  auto key = [&](int i) {
+    return Key{(long long)std::floor(X[3 * i] / cell), (long long)std::floor(X[3 * i + 1] / cell),
+               (long long)std::floor(X[3 * i + 2] / cell)};
+  };
+  for (int i = 0; i < N; ++i) grid[key(i)].push_back(i);
+  ptr.assign(N + 1, 0);
+  idx.clear();
+  for (int i = 0; i < N; ++i) {
+    std::vector<int> s{i};
+    if (bnd[i]) {
+      Key k = key(i);
+      for (long long dx = -1; dx <= 1; ++dx)
+        for (long long dy = -1; dy <= 1; ++dy)
+          for (long long dz = -1; dz <= 1; ++dz) {
+            auto it = grid.find(Key{k.x + dx, k.y + dy, k.z + dz});
+            if (it == grid.end()) continue;
+            for (int j : it->second) {
+              if (j == i) continue;
+              double d0 = X[3 * i] - X[3 * j], d1 = X[3 * i + 1] - X[3 * j + 1],
+                     d2 = X[3 * i + 2] - X[3 * j + 2];
+              if (std::sqrt(d0 * d0 + d1 * d1 + d2 * d2) < tol) s.push_back(j);
+            }
+          }
+    }
+    std::sort(s.begin(), s.end());
+    idx.insert(idx.end(), s.begin(), s.end());
+    ptr[i + 1] = (int)idx.size();
+  }
+}
+
+static uint64_t spread21(uint64_t v) {
+  v &= 0x1fffffULL;
+  v = (v | (v << 32)) & 0x1f00000000ffffULL;
+  v = (v | (v << 16)) & 0x1f0000ff0000ffULL;
+  v = (v | (v << 8)) & 0x100f00f00f00f00fULL;
+  v = (v | (v << 4)) & 0x10c30c30c30c30c3ULL;
+  v = (v | (v << 2)) & 0x1249249249249249ULL;
+  return v;
+}
+
+// Internal dof order: Morton (Z-order) of the support points, so that a tile
+// of consecutive dofs is a compact patch of the surface.
+static void morton_order(int N, const double* X, std::vector<int>& perm, std::vector<int>& iperm) {
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (int i = 0; i < N; ++i)
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = std::min(lo[d], X[3 * i + d]);
+      hi[d] = std::max(hi[d], X[3 * i + d]);
+    }
+  double ext = std::max(hi[0] - lo[0], std::max(hi[1] - lo[1], hi[2] - lo[2]));
+  if (!(ext > 0)) ext = 1;
+  std::vector<std::pair<uint64_t, int>> k(N);
+  for (int i = 0; i < N; ++i) {
+    uint64_t q[3];
+    for (int d = 0; d < 3; ++d) {
+      double t = (X[3 * i + d] - lo[d]) / ext;
+      t = std::min(std::max(t, 0.0), 1.0);
+      q[d] = (uint64_t)(t * 2097151.0);
+    }
+    k[i] = {spread21(q[0]) | (spread21(q[1]) << 1) | (spread21(q[2]) << 2), i};
+  }
+  std::sort(k.begin(), k.end());
+  perm.resize(N);
+  iperm.resize(N);
+  for (int i = 0; i < N; ++i) {
+    perm[i] = k[i].second;
+    iperm[k[i].second] = i;
+  }
+}
+
+static int build_topology(wbem_context* h) {
+  const int N = h->N, C = h->C;
+  morton_order(N, h->X.data(), h->perm, h->iperm);
+  const auto& ip = h->iperm;
+  // cell dofs (internal)
+  std::vector<int4> cd(C);
+  for (int c = 0; c < C; ++c)
+    cd[c] = make_int4(ip[h->cells[4 * c]], ip[h->cells[4 * c + 1]], ip[h->cells[4 * c + 2]],
+                      ip[h->cells[4 * c + 3]]);
+  // column tiles
+  const int CT = kColsPerTile;
+  h->n_tiles = (N + CT - 1) / CT;
+  std::vector<std::vector<int2>> tl(h->n_tiles);
+  for (int c = 0; c < C; ++c) {
+    const int d[4] = {cd[c].x, cd[c].y, cd[c].z, cd[c].w};
+    int tiles[4];
+    int nt = 0;
+    for (int k = 0; k < 4; ++k) {
+      int t = d[k] / CT;
+      bool seen = false;
+      for (int u = 0; u < nt; ++u) seen |= tiles[u] == t;
+      if (!seen) tiles[nt++] = t;
+    }
+    const int owner = d[0] / CT;
+    for (int u = 0; u < nt; ++u) {
+      uint32_t slots = 0;
+      for (int k = 0; k < 4; ++k) {
+        uint32_t sl = (d[k] / CT == tiles[u]) ? (uint32_t)(d[k] % CT) : 255u;
+        slots |= sl << (8 * k);
+      }
+      int2 e;
+      e.x = c | (tiles[u] == owner ? (int)0x80000000u : 0);
+      e.y = (int)slots;
+      tl[tiles[u]].push_back(e);
+    }
+  }
+  std::vector<int> tptr(h->n_tiles + 1, 0);
+  std::vector<int2> tent;
+  for (int t = 0; t < h->n_tiles; ++t) {
+    tent.insert(tent.end(), tl[t].begin(), tl[t].end());
+    tptr[t + 1] = (int)tent.size();
+  }
+  // double-node sets (internal)
+  std::vector<int> dnset((size_t)N * kMaxSet, -1);
+  for (int p = 0; p < N; ++p) {
+    const int i = ip[p];
+    int k = 0;
+    for (int e = h->dn_ptr[p]; e < h->dn_ptr[p + 1]; ++e) dnset[(size_t)i * kMaxSet + k++] = ip[h->dn_idx[e]];
+  }
+  // node -> (cell, vertex) adjacency (internal nodes)
+  std::vector<int> ncptr(N + 1, 0), ncent;
+  for (int c = 0; c < C; ++c) {
+    const int d[4] = {cd[c].x, cd[c].y, cd[c].z, cd[c].w};
+    for (int k = 0; k < 4; ++k) ncptr[d[k] + 1]++;
+  }
+  for (int i = 0; i < N; ++i) ncptr[i + 1] += ncptr[i];
+  ncent.resize(ncptr[N]);
+  {
+    std::vector<int> fill(ncptr.begin(), ncptr.end() - 1);
+    for (int c = 0; c < C; ++c) {
+      const int d[4] = {cd[c].x, cd[c].y, cd[c].z, cd[c].w};
+      for (int k = 0; k < 4; ++k) ncent[fill[d[k]]++] = c * 4 + k;
+    }
+  }
+  // singular panels per row: cells adjacent to a node of the row's set
+  std::vector<int> sptr(N + 1, 0), scell;
+  for (int i = 0; i < N; ++i) {
+    std::vector<int> s;
+    for (int k = 0; k < kMaxSet; ++k) {
+      const int j = dnset[(size_t)i * kMaxSet + k];
+      if (j < 0) continue;
+      for (int e = ncptr[j]; e < ncptr[j + 1]; ++e) s.push_back(ncent[e] / 4);
+    }
+    std::sort(s.begin(), s.end());
+    s.erase(std::unique(s.begin(), s.end()), s.end());
+    scell.insert(scell.end(), s.begin(), s.end());
+    sptr[i + 1] = (int)scell.size();
+  }
+  std::vector<double> Xi((size_t)N * 3);
+  for (int i = 0; i < N; ++i)
+    for (int d = 0; d < 3; ++d) Xi[3 * (size_t)i + d] = h->X[3 * (size_t)h->perm[i] + d];
+  CHK(upload(h, &h->d_X, Xi));
+  CHK(upload(h, &h->d_cell_dofs, cd));
+  CHK(upload(h, &h->d_dnset, dnset));
+  CHK(upload(h, &h->d_tile_ptr, tptr));
+  CHK(upload(h, &h->d_tile_ent, tent));
+  CHK(upload(h, &h->d_sptr, sptr));
+  CHK(upload(h, &h->d_scell, scell));
+  CHK(upload(h, &h->d_perm, h->perm));
+  CHK(upload(h, &h->d_iperm, h->iperm));
+  CHK(upload(h, &h->d_ncptr, ncptr));
+  CHK(upload(h, &h->d_ncent, ncent));
+  return WBEM_OK;
+}
+
+// ------------------------------------------------------------ constraints
+// BEMProblem<3>::compute_constraints (source/bem_problem.cc:990-1105) with
+// deal.II ConstraintMatrix semantics (add_line is idempotent, close() resolves
+// entries that point at constrained dofs). Caller order in, internal order
+// uploaded. Normals and surface gradients (L2 projections) are only needed
+// for Dirichlet-Dirichlet double nodes.
+namespace {
+struct Lines {
+  std::map<int, std::vector<std::pair<int, double>>> l;
+  std::map<int, double> inh;
+  void add_line(int i) {
+    if (!l.count(i)) {
+      l[i] = {};
+      inh[i] = 0;
+    }
+  }
+  void add_entry(int i, int j, double v) {
+    for (auto& e : l[i])
+      if (e.first == j) return;
+    l[i].push_back({j, v});
+  }
+  void close() {
+    for (int pass = 0; pass < 64; ++pass) {
+      bool changed = false;
+      for (auto& kv : l) {
+        std::vector<std::pair<int, double>> out;
+        double v = inh[kv.first];
+        for (auto& e : kv.second) {
+          auto it = l.find(e.first);
+          if (it != l.end() && e.first != kv.first) {
+            changed = true;
+            v += e.second * inh[e.first];
+            for (auto& e2 : it->second) out.push_back({e2.first, e.second * e2.second});
+          } else {
+            out.push_back(e);
+          }
+        }
+        std::map<int, double> m;
+        for (auto& e : out) m[e.first] += e.second;
+        kv.second.assign(m.begin(), m.end());
+        inh[kv.first] = v;
+      }
+      if (!changed) break;
+    }
+  }
+};
+
+// L2 projection onto Q1 with the consistent mass matrix (CG to round-off).
+void l2_project(int N, const double* X, int C, const int* cells, int q1,
+                const std::vector<std::vector<double>>& cellval /*C x q x 3*/,
+                std::vector<double>& out /*N x 3*/) {
+  std::vector<double> x, w;
+  gauss_legendre01(q1, x, w);
+  std::vector<std::map<int, double>> M(N);
+  std::vector<double> rhs(3 * (size_t)N, 0.0);
+  for (int c = 0; c < C; ++c) {
+    const int* cc = cells + 4 * c;
+    for (int b = 0; b < q1; ++b)
+      for (int a = 0; a < q1; ++a) {
+        const int q = a + q1 * b;
+        double s = x[a], u = x[b];
+        double ph[4] = {(1 - s) * (1 - u), s * (1 - u), (1 - s) * u, s * u};
+        double jx[3], je[3];
+        for (int d = 0; d < 3; ++d) {
+          jx[d] = (1 - u) * (X[3 * cc[1] + d] - X[3 * cc[0] + d]) + u * (X[3 * cc[3] + d] - X[3 * cc[2] + d]);
+          je[d] = (1 - s) * (X[3 * cc[2] + d] - X[3 * cc[0] + d]) + s * (X[3 * cc[3] + d] - X[3 * cc[1] + d]);
+        }
+        double cr[3] = {jx[1] * je[2] - jx[2] * je[1], jx[2] * je[0] - jx[0] * je[2],
+                        jx[0] * je[1] - jx[1] * je[0]};
+        double jxw = std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]) * w[a] * w[b];
+        for (int i = 0; i < 4; ++i) {
+          for (int j = 0; j < 4; ++j) M[cc[i]][cc[j]] += ph[i] * ph[j] * jxw;
+          for (int d = 0; d < 3; ++d) rhs[(size_t)d * N + cc[i]] += ph[i] * cellval[c][3 * q + d] * jxw;
+        }
+      }
+  }
+  out.assign(3 * (size_t)N, 0.0);
+  for (int d = 0; d < 3; ++d) {
+    std::vector<double> xs(N, 0.0), r(rhs.begin() + (size_t)d * N, rhs.begin() + (size_t)(d + 1) * N), z(N), p(N), Ap(N), dinv(N);
+    double bn = 0;
+    for (int i = 0; i < N; ++i) {
+      dinv[i] = 1.0 / M[i][i];
+      bn += r[i] * r[i];
+    }
+    bn = std::sqrt(bn);
+    if (bn > 0) {
+      for (int i = 0; i < N; ++i) z[i] = dinv[i] * r[i];
+      p = z;
+      double rz = 0;
+      for (int i = 0; i < N; ++i) rz += r[i] * z[i];
+      for (int it = 0; it < 10 * N + 100; ++it) {
+        for (int i = 0; i < N; ++i) {
+          double s = 0;
+          for (auto& kv : M[i]) s += kv.second * p[kv.first];
+          Ap[i] = s;
+        }
+        double pAp = 0;
+        for (int i = 0; i < N; ++i) pAp += p[i] * Ap[i];
+        double al = rz / pAp, rn = 0;
+        for (int i = 0; i < N; ++i) {
+          xs[i] += al * p[i];
+          r[i] -= al * Ap[i];
+          rn += r[i] * r[i];
+        }
+        if (std::sqrt(rn) < 1e-15 * bn) break;
+        double rz2 = 0;
+        for (int i = 0; i < N; ++i) {
+          z[i] = dinv[i] * r[i];
+          rz2 += r[i] * z[i];
+        }
+        for (int i = 0; i < N; ++i) p[i] = z[i] + rz2 / rz * p[i];
+        rz = rz2;
+      }
+    }
+    for (int i = 0; i < N; ++i) out[3 * (size_t)i + d] = xs[i];
+  }
+}
+}  // namespace
+
+static int build_constraints(wbem_context* h, const double* tmp_rhs) {
+  const int N = h->N;
+  const auto& m = h->mask;
+  const auto& P = h->dn_ptr;
+  const auto& I = h->dn_idx;
+  bool need_geo = false;
+  for (int i = 0; i < N && !need_geo; ++i)
+    if (m[i])
+      for (int k = P[i]; k < P[i + 1]; ++k)
+        if (I[k] != i && m[I[k]]) need_geo = true;
+  std::vector<double> nn, gg;
+  if (need_geo) {
+    const int q1 = h->opt.quadrature_order;
+    std::vector<double> x, w;
+    gauss_legendre01(q1, x, w);
+    std::vector<std::vector<double>> cn(h->C), cg(h->C);
+    for (int c = 0; c < h->C; ++c) {
+      const int* cc = &h->cells[4 * c];
+      cn[c].resize(3 * q1 * q1);
+      cg[c].resize(3 * q1 * q1);
+      double f[4];
+      for (int k = 0; k < 4; ++k) f[k] = m[cc[k]] ? tmp_rhs[cc[k]] : 0.0;
+      for (int b = 0; b < q1; ++b)
+        for (int a = 0; a < q1; ++a) {
+          const int q = a + q1 * b;
+          double s = x[a], u = x[b];
+          double jx[3], je[3];
+          const double* X = h->X.data();
+          for (int d = 0; d < 3; ++d) {
+            jx[d] = (1 - u) * (X[3 * cc[1] + d] - X[3 * cc[0] + d]) + u * (X[3 * cc[3] + d] - X[3 * cc[2] + d]);
+            je[d] = (1 - s) * (X[3 * cc[2] + d] - X[3 * cc[0] + d]) + s * (X[3 * cc[3] + d] - X[3 * cc[1] + d]);
+          }
+          double cr[3] = {jx[1] * je[2] - jx[2] * je[1], jx[2] * je[0] - jx[0] * je[2],
+                          jx[0] * je[1] - jx[1] * je[0]};
+          double l = std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+          double gx = -(1 - u) * f[0] + (1 - u) * f[1] - u * f[2] + u * f[3];
+          double ge = -(1 - s) * f[0] - s * f[1] + (1 - s) * f[2] + s * f[3];
+          double g11 = 0, g12 = 0, g22 = 0;
+          for (int d = 0; d < 3; ++d) {
+            g11 += jx[d] * jx[d];
+            g12 += jx[d] * je[d];
+            g22 += je[d] * je[d];
+          }
+          double det = g11 * g22 - g12 * g12;
+          double c1 = (g22 * gx - g12 * ge) / det, c2 = (-g12 * gx + g11 * ge) / det;
+          for (int d = 0; d < 3; ++d) {
+            cn[c][3 * q + d] = cr[d] / l;
+            cg[c][3 * q + d] = c1 * jx[d] + c2 * je[d];
+          }
+        }
+    }
+    l2_project(N, h->X.data(), h->C, h->cells.data(), q1, cn, nn);
+    l2_project(N, h->X.data(), h->C, h->cells.data(), q1, cg, gg);
+    for (int i = 0; i < N; ++i) {
+      double l = std::sqrt(nn[3 * i] * nn[3 * i] + nn[3 * i + 1] * nn[3 * i + 1] + nn[3 * i + 2] * nn[3 * i + 2]);
+      for (int d = 0; d < 3; ++d) nn[3 * i + d] /= l;
+    }
+  }
+  auto dot3 = [](const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
+  Lines c;
+  for (int i = 0; i < N; ++i) {
+    int first = I[P[i]];
+    for (int k = P[i]; k < P[i + 1]; ++k)
+      if (m[I[k]] == 1) {
+        first = I[k];
+        break;
+      }
+    if (i != first) continue;
+    for (int k = P[i]; k < P[i + 1]; ++k) {
+      const int o = I[k];
+      if (o == i) continue;
+      if (m[i] == 1) {
+        if (m[o] == 1) {
+          const double* ni = &nn[3 * i];
+          const double* no = &nn[3 * o];
+          double dd = std::sqrt((ni[0] - no[0]) * (ni[0] - no[0]) + (ni[1] - no[1]) * (ni[1] - no[1]) +
+                                (ni[2] - no[2]) * (ni[2] - no[2]));
+          if (dd < 1e-4) {
+            c.add_line(o);
+            c.add_entry(o, i, 1.0);
+          } else {
+            c.add_line(o);
+            const double* gi = &gg[3 * i];
+            const double* go = &gg[3 * o];
+            double cij = dot3(ni, no);
+            double this_g = (1.0 / (1.0 - cij * cij)) * (dot3(go, ni) + dot3(gi, no) * cij);
+            double other_g = (1.0 / (1.0 - cij * cij)) * (dot3(gi, no) + dot3(go, ni) * cij);
+            c.add_line(i);
+            c.inh[i] = this_g;
+            c.add_line(o);
+            c.inh[o] = other_g;
+          }
+        } else {
+          c.add_line(o);
+          c.inh[o] = tmp_rhs[i];
+        }
+      } else {
+        c.add_line(o);
+        c.add_entry(o, i, 1.0);
+      }
+    }
+  }
+  c.close();
+  // internal order, rows sorted
+  const auto& ip = h->iperm;
+  std::vector<std::pair<int, int>> rows;  // (internal row, caller row)
+  for (auto& kv : c.l) rows.push_back({ip[kv.first], kv.first});
+  std::sort(rows.begin(), rows.end());
+  std::vector<int> crow, cptr{0}, ccol;
+  std::vector<double> cval, cinh;
+  std::vector<uint8_t> cflag(N, 0);
+  std::vector<int> cptr_full(N + 1, 0), ccol_full;
+  std::vector<double> cval_full;
+  std::vector<std::vector<std::pair<int, double>>> byrow(N);
+  for (auto& r : rows) {
+    crow.push_back(r.first);
+    cflag[r.first] = 1;
+    cinh.push_back(c.inh[r.second]);
+    for (auto& e : c.l[r.second]) {
+      ccol.push_back(ip[e.first]);
+      cval.push_back(e.second);
+      byrow[r.first].push_back({ip[e.first], e.second});
+    }
+    cptr.push_back((int)ccol.size());
+  }
+  for (int i = 0; i < N; ++i) {
+    for (auto& e : byrow[i]) {
+      ccol_full.push_back(e.first);
+      cval_full.push_back(e.second);
+    }
+    cptr_full[i + 1] = (int)ccol_full.size();
+  }
+  // transposed entries: for column j, the constrained rows i with entry c_ij
+  std::vector<int> tptr(N + 1, 0), tsrc;
+  std::vector<double> tval;
+  std::vector<std::vector<std::pair<int, double>>> bycol(N);
+  for (int i = 0; i < N; ++i)
+    for (auto& e : byrow[i]) bycol[e.first].push_back({i, e.second});
+  for (int j = 0; j < N; ++j) {
+    for (auto& e : bycol[j]) {
+      tsrc.push_back(e.first);
+      tval.push_back(e.second);
+    }
+    tptr[j + 1] = (int)tsrc.size();
+  }
+  h->n_crows = (int)crow.size();
+  CHK(upload(h, &h->d_crow, crow));
+  CHK(upload(h, &h->d_cptr, cptr));
+  CHK(upload(h, &h->d_ccol, ccol));
+  CHK(upload(h, &h->d_cval, cval));
+  CHK(upload(h, &h->d_cinh, cinh));
+  CHK(upload(h, &h->d_cflag, cflag));
+  CHK(upload(h, &h->d_cptr_full, cptr_full));
+  CHK(upload(h, &h->d_ccol_full, ccol_full));
+  CHK(upload(h, &h->d_cval_full, cval_full));
+  CHK(upload(h, &h->d_tptr, tptr));
+  CHK(upload(h, &h->d_tsrc, tsrc));
+  CHK(upload(h, &h->d_tval, tval));
+  return WBEM_OK;
+}
+
+// ------------------------------------------------------------- workspaces
+namespace wbem {
+int ensure_vectors(wbem_context* h, int restart) {
+  const int N = h->N;
+  for (int k = 0; k < 8; ++k)
+    if (!h->d_vec[k]) CHK(dev_alloc(h, &h->d_vec[k], (size_t)N));
+  if (!h->d_part) CHK(dev_alloc(h, &h->d_part, (size_t)256 * 128 + (size_t)32 * N));
+  if (!h->d_small) CHK(dev_alloc(h, &h->d_small, (size_t)512));
+  if (!h->d_sol) CHK(dev_alloc(h, &h->d_sol, (size_t)N));
+  if (!h->d_rhs) CHK(dev_alloc(h, &h->d_rhs, (size_t)N));
+  if (!h->d_b) CHK(dev_alloc(h, &h->d_b, (size_t)N));
+  if (h->V_cap < restart + 1) {
+    CHK(dev_alloc(h, &h->d_V, (size_t)(restart + 1) * N));
+    h->V_cap = restart + 1;
+  }
+  return WBEM_OK;
+}
+
+// y = A x (constrained system operator), FP64 or mixed storage.
+int apply_system(wbem_context* h, const double* x, double* y) {
+  if (h->assembled_prec == WBEM_PREC_FP64)
+    CU(launch_matvec_fp64(h->N, 0, h->d_N, h->d_D, h->d_mask, h->d_alpha, x, y, h->stream));
+  else
+    CU(launch_matvec_mixed(h->N, 0, h->d_N2, h->d_D2, h->d_mask, h->d_alpha, x, y, h->stream));
+  CU(launch_constraint_rows(h->n_crows, h->d_crow, h->d_cptr, h->d_ccol, h->d_cval, x, y, h->stream));
+  h->launches += 2;
+  return WBEM_OK;
+}
+
+// y = A^T x for the constrained operator.
+int apply_system_t(wbem_context* h, const double* x, double* y) {
+  // x with its constrained entries zeroed feeds the unconstrained rows
+  double* xz = h->d_vec[7];
+  CU(cudaMemcpyAsync(xz, x, sizeof(double) * h->N, cudaMemcpyDeviceToDevice, h->stream));
+  if (h->n_crows) {
+    double* zeros = h->d_part;
+    CU(cudaMemsetAsync(zeros, 0, sizeof(double) * h->n_crows, h->stream));
+    CU(launch_set_rows(h->n_crows, h->d_crow, zeros, xz, h->stream));
+  }
+  double* part = h->d_part + 256 * 128;
+  if (h->assembled_prec == WBEM_PREC_FP64)
+    CU(launch_matvec_t_fp64(h->N, h->d_N, h->d_D, h->d_mask, h->d_alpha, xz, y, part, h->stream));
+  else
+    CU(launch_matvec_t_mixed(h->N, h->d_N2, h->d_D2, h->d_mask, h->d_alpha, xz, y, part, h->stream));
+  if (h->n_crows)
+    CU(launch_constraint_rows_t(h->N, h->n_crows, h->d_crow, h->d_cptr, h->d_ccol, h->d_cval,
+                                h->d_tptr, h->d_tsrc, h->d_tval, h->d_cflag, x, y, h->stream));
+  h->launches += 5;
+  return WBEM_OK;
+}
+
+static int read_scalar(wbem_context* h, const double* d, double* v) {
+  CU(cudaMemcpyAsync(v, d, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CU(cudaStreamSynchronize(h->stream));
+  return WBEM_OK;
+}
+
+// Right-preconditioned GMRES(m) with classical Gram-Schmidt and one
+// re-orthogonalisation, Givens rotations on the host. prec(z <- M^{-1} v).
+// Stops when the residual norm is <= max(tol, 1e-14 ||rhs||) (absolute
+// tolerance as deal.II's SolverControl, floored at round-off level).
+template <typename Op, typename Prec>
+int gmres(wbem_context* h, const double* rhs, double* x, int restart, int max_steps, double tol,
+          Op op, Prec prec, int* iters, double* resid) {
+  const int N = h->N;
+  double* r = h->d_vec[0];
+  double* w = h->d_vec[1];
+  double* z = h->d_vec[2];
+  double* hbuf = h->d_small;  // [0..restart+1] h, [256..] h2
+  double* part = h->d_part;
+  double bnorm;
+  CU(launch_nrm2(N, rhs, part, hbuf, h->stream));
+  CHK(read_scalar(h, hbuf, &bnorm));
+  const double target = std::max(tol, 1e-14 * bnorm);
+  CU(cudaMemsetAsync(x, 0, sizeof(double) * N, h->stream));
+  int it = 0;
+  double res = bnorm;
+  std::vector<double> H((size_t)(restart + 1) * restart), cs(restart), sn(restart), g(restart + 1),
+      hv(restart + 2), hv2(restart + 2), y(restart);
+  bool first = true;
+  while (true) {
+    // r = rhs - A x
+    if (first) {
+      CU(cudaMemcpyAsync(r, rhs, sizeof(double) * N, cudaMemcpyDeviceToDevice, h->stream));
+      first = false;
+    } else {
+      CHK(op(x, r));
+      CU(launch_axpby(N, 1.0, rhs, -1.0, r, h->stream));
+    }
+    CU(launch_nrm2(N, r, part, hbuf, h->stream));
+    double beta;
+    CHK(read_scalar(h, hbuf, &beta));
+    res = beta;
+    if (!std::isfinite(beta)) return fail(h, WBEM_ERR_NONFINITE, "GMRES: non-finite residual");
+    if (beta <= target) break;
+    if (it >= max_steps) {
+      if (iters) *iters = it;
+      if (resid) *resid = res;
+      return fail(h, WBEM_ERR_NOCONV, "GMRES: no convergence within max_steps");
+    }
+    CU(launch_scale(N, r, 1.0 / beta, h->d_V, h->stream));
+    std::fill(g.begin(), g.end(), 0.0);
+    g[0] = beta;
+    int k = 0;
+    for (; k < restart && it < max_steps; ++k) {
+      double* vk = h->d_V + (size_t)k * N;
+      double* vk1 = h->d_V + (size_t)(k + 1) * N;
+      CHK(prec(vk, z));
+      CHK(op(z, w));
+      CU(launch_multidot(N, k + 1, h->d_V, w, part, hbuf, h->stream));
+      CU(launch_axpy_basis(N, k + 1, h->d_V, hbuf, w, -1.0, h->stream));
+      CU(launch_multidot(N, k + 1, h->d_V, w, part, hbuf + 256, h->stream));
+      CU(launch_axpy_basis(N, k + 1, h->d_V, hbuf + 256, w, -1.0, h->stream));
+      CU(launch_nrm2(N, w, part, hbuf + 255, h->stream));
+      CU(cudaMemcpyAsync(hv.data(), hbuf, sizeof(double) * (k + 1), cudaMemcpyDeviceToHost, h->stream));
+      CU(cudaMemcpyAsync(hv2.data(), hbuf + 256, sizeof(double) * (k + 1), cudaMemcpyDeviceToHost, h->stream));
+      double hn;
+      CU(cudaMemcpyAsync(&hn, hbuf + 255, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+      CU(cudaStreamSynchronize(h->stream));
+      h->launches += 9;
+      ++it;
+      for (int j = 0; j <= k; ++j) H[(size_t)j * restart + k] = hv[j] + hv2[j];
+      H[(size_t)(k + 1) * restart + k] = hn;
+      if (hn > 0) CU(launch_scale(N, w, 1.0 / hn, vk1, h->stream));
+      for (int j = 0; j < k; ++j) {
+        double a = H[(size_t)j * restart + k], b = H[(size_t)(j + 1) * restart + k];
+        H[(size_t)j * restart + k] = cs[j] * a + sn[j] * b;
+        H[(size_t)(j + 1) * restart + k] = -sn[j] * a + cs[j] * b;
+      }
+      double a = H[(size_t)k * restart + k], b = H[(size_t)(k + 1) * restart + k];
+      double d = std::hypot(a, b);
+      if (d == 0) return fail(h, WBEM_ERR_SINGULAR, "GMRES: breakdown");
+      cs[k] = a / d;
+      sn[k] = b / d;
+      H[(size_t)k * restart + k] = d;
+      H[(size_t)(k + 1) * restart + k] = 0;
+      g[k + 1] = -sn[k] * g[k];
+      g[k] = cs[k] * g[k];
+      res = std::fabs(g[k + 1]);
+      if (res <= target || hn == 0) {
+        ++k;
+        break;
+      }
+    }
+    for (int j = k - 1; j >= 0; --j) {
+      double s = g[j];
+      for (int l = j + 1; l < k; ++l) s -= H[(size_t)j * restart + l] * y[l];
+      y[j] = s / H[(size_t)j * restart + j];
+    }
+    CU(cudaMemcpyAsync(hbuf, y.data(), sizeof(double) * k, cudaMemcpyHostToDevice, h->stream));
+    CU(cudaMemsetAsync(w, 0, sizeof(double) * N, h->stream));
+    CU(launch_axpy_basis(N, k, h->d_V, hbuf, w, 1.0, h->stream));
+    CHK(prec(w, z));
+    CU(launch_axpby(N, 1.0, z, 1.0, x, h->stream));
+    // the host vector y must stay alive until the copy above completes
+    CU(cudaStreamSynchronize(h->stream));
+  }
+  if (iters) *iters = it;
+  if (resid) *resid = res;
+  return WBEM_OK;
+}
+
+int gmres_fp64(wbem_context* h, const double* rhs, double* x, int transpose) {
+  auto op = [&](const double* a, double* b) {
+    return transpose ? apply_system_t(h, a, b) : apply_system(h, a, b);
+  };
+  auto prec = [&](const double* a, double* b) -> int {
+    CU(launch_bj_apply(h->N, h->d_binv, a, b, transpose, h->stream));
+    return WBEM_OK;
+  };
+  int it = 0;
+  double res = 0;
+  int st = gmres(h, rhs, x, h->opt.gmres_restart, h->opt.max_steps, h->opt.tolerance, op, prec,
+                 &it, &res);
+  h->stats.iterations = it;
+  h->stats.residual = res;
+  return st;
+}
+
+int build_block_jacobi(wbem_context* h) {
+  const int nb = (h->N + kBJ - 1) / kBJ;
+  CHK(dev_alloc(h, &h->d_binv, (size_t)nb * kBJ * kBJ));
+  CU(launch_bj_build(h->N, h->d_N, h->d_D, h->d_N2, h->d_D2, h->d_mask, h->d_alpha, h->d_cflag,
+                     h->d_cptr_full, h->d_ccol_full, h->d_cval_full, h->d_binv, h->d_err,
+                     h->stream));
+  h->launches++;
+  return check_device_error(h, "block-Jacobi");
+}
+
+}  // namespace wbem
+
+// ---------------------------------------------------------------- timing
+namespace {
+struct Timer {
+  cudaEvent_t a, b;
+  cudaStream_t s;
+  explicit Timer(cudaStream_t st) : s(st) {
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, s);
+  }
+  double ms() {
+    cudaEventRecord(b, s);
+    cudaEventSynchronize(b);
+    float t = 0;
+    cudaEventElapsedTime(&t, a, b);
+    cudaEventRecord(a, s);
+    return t;
+  }
+  ~Timer() {
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+  }
+};
+}  // namespace
+
+// ================================================================ C ABI
+extern "C" {
+
+int wbem_default_options(wbem_options* o) {
+  if (!o) return WBEM_ERR_ARG;
+  std::memset(o, 0, sizeof *o);
+  o->precision = WBEM_PREC_FP64;
+  o->solver = WBEM_SOLVER_AUTO;
+  o->quadrature_order = 4;
+  o->singular_quadrature_order = 5;
+  o->gmres_restart = 100;
+  o->max_steps = 1000;
+  o->tolerance = 1e-12;
+  o->near_field_ratio = 2.0;
+  o->keep_matrices = 1;
+  return WBEM_OK;
+}
+
+int wbem_create(wbem_handle* out, int device) {
+  if (!out) return WBEM_ERR_ARG;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return WBEM_ERR_CUDA;
+  if (device < 0 || device >= n) return WBEM_ERR_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return WBEM_ERR_CUDA;
+  wbem_context* h = new wbem_context();
+  h->device = device;
+  wbem_default_options(&h->opt);
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete h;
+    return WBEM_ERR_CUDA;
+  }
+  if (cudaMalloc(&h->d_err, sizeof(DevErr)) != cudaSuccess) {
+    cudaStreamDestroy(h->stream);
+    delete h;
+    return WBEM_ERR_NOMEM;
+  }
+  cudaMemset(h->d_err, 0, sizeof(DevErr));
+  *out = h;
+  return WBEM_OK;
+}
+
+int wbem_destroy(wbem_handle h) {
+  if (!h) return WBEM_ERR_ARG;
+  cudaSetDevice(h->device);
+  cudaStreamSynchronize(h->stream);
+  void* ptrs[] = {h->d_X, h->d_cell_dofs, h->d_dnset, h->d_tile_ptr, h->d_tile_ent, h->d_sptr,
+                  h->d_scell, h->d_perm, h->d_iperm, h->d_ncptr, h->d_ncent, h->d_mask, h->d_rec,
+                  h->d_rec32, h->d_cellc, h->d_cellgeo, h->d_N, h->d_D, h->d_N2, h->d_D2,
+                  h->d_alpha, h->d_alpha_part, h->d_alpha_near, h->d_alpha_sing, h->d_near_cnt,
+                  h->d_near_cells, h->d_crow, h->d_cptr, h->d_ccol, h->d_cval, h->d_cinh,
+                  h->d_cflag, h->d_cptr_full, h->d_ccol_full, h->d_cval_full, h->d_tptr,
+                  h->d_tsrc, h->d_tval, h->d_binv, h->d_V, h->d_part, h->d_small, h->d_lu,
+                  h->d_split, h->d_lutmp, h->d_info, h->d_sol, h->d_rhs, h->d_b, h->d_err};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  for (int k = 0; k < 8; ++k)
+    if (h->d_vec[k]) cudaFree(h->d_vec[k]);
+  cudaStreamDestroy(h->stream);
+  delete h;
+  return WBEM_OK;
+}
+
+const char* wbem_last_error(wbem_handle h) {
+  if (!h) return "invalid handle";
+  return h->err.c_str();
+}
+
+int wbem_set_geometry(wbem_handle h, const double* X, int n_dofs, const int* cells, int n_cells,
+                      const int* dn_ptr, const int* dn_idx) {
+  if (!h) return WBEM_ERR_ARG;
+  if (!X || !cells || n_dofs < 1 || n_cells < 1)
+    return fail(h, WBEM_ERR_ARG, "wbem_set_geometry: empty mesh or NULL pointer");
+  if ((long long)n_dofs * n_dofs > (1LL << 34))
+    return fail(h, WBEM_ERR_ARG, "wbem_set_geometry: n_dofs too large for a dense N x N matrix");
+  if ((dn_ptr == nullptr) != (dn_idx == nullptr))
+    return fail(h, WBEM_ERR_ARG, "wbem_set_geometry: dn_ptr and dn_idx must both be given or both NULL");
+  for (long long k = 0; k < 3LL * n_dofs; ++k)
+    if (!std::isfinite(X[k])) return fail(h, WBEM_ERR_NONFINITE, "wbem_set_geometry: non-finite support point");
+  for (long long k = 0; k < 4LL * n_cells; ++k)
+    if (cells[k] < 0 || cells[k] >= n_dofs)
+      return fail(h, WBEM_ERR_ARG, "wbem_set_geometry: cell vertex index out of range");
+  for (int c = 0; c < n_cells; ++c)
+    for (int a = 0; a < 4; ++a)
+      for (int b = a + 1; b < 4; ++b)
+        if (cells[4 * c + a] == cells[4 * c + b])
+          return fail(h, WBEM_ERR_ARG, "wbem_set_geometry: repeated vertex in a cell");
+  cudaSetDevice(h->device);
+  h->N = n_dofs;
+  h->C = n_cells;
+  h->X.assign(X, X + 3 * (size_t)n_dofs);
+  h->cells.assign(cells, cells + 4 * (size_t)n_cells);
+  if (dn_ptr) {
+    if (dn_ptr[0] != 0) return fail(h, WBEM_ERR_ARG, "wbem_set_geometry: dn_ptr[0] must be 0");
+    h->dn_ptr.assign(dn_ptr, dn_ptr + n_dofs + 1);
+    h->dn_idx.assign(dn_idx, dn_idx + dn_ptr[n_dofs]);
+    for (int i = 0; i < n_dofs; ++i) {
+      const int a = dn_ptr[i], b = dn_ptr[i + 1];
+      if (b <= a || b - a > kMaxSet)
+        return fail(h, WBEM_ERR_ARG, "wbem_set_geometry: double-node set empty or larger than 8");
+      bool self = false;
+      for (int k = a; k < b; ++k) {
+        if (dn_idx[k] < 0 || dn_idx[k] >= n_dofs)
+          return fail(h, WBEM_ERR_ARG, "wbem_set_geometry: double-node index out of range");
+        if (k > a && dn_idx[k] <= dn_idx[k - 1])
+          return fail(h, WBEM_ERR_ARG, "wbem_set_geometry: double-node set not strictly ascending");
+        self |= dn_idx[k] == i;
+      }
+      if (!self) return fail(h, WBEM_ERR_ARG, "wbem_set_geometry: double-node set must contain its own dof");
+    }
+  } else {
+    find_double_nodes(n_dofs, X, n_cells, cells, h->dn_ptr, h->dn_idx);
+    for (int i = 0; i < n_dofs; ++i)
+      if (h->dn_ptr[i + 1] - h->dn_ptr[i] > kMaxSet)
+        return fail(h, WBEM_ERR_ARG, "wbem_set_geometry: more than 8 coincident nodes");
+  }
+  h->assembled_prec = -1;
+  h->factors_valid = false;
+  h->have_solution = false;
+  CHK(build_quadrature(h, h->opt.quadrature_order, h->opt.singular_quadrature_order));
+  CHK(build_topology(h));
+  if (h->have_mask && (int)h->mask.size() == n_dofs) {
+    std::vector<uint8_t> mi(n_dofs);
+    for (int i = 0; i < n_dofs; ++i) mi[i] = h->mask[h->perm[i]];
+    CHK(upload(h, &h->d_mask, mi));
+  } else {
+    h->have_mask = false;
+  }
+  return WBEM_OK;
+}
+
+int wbem_update_nodes(wbem_handle h, const double* X) {
+  if (!h) return WBEM_ERR_ARG;
+  if (!X || h->N == 0) return fail(h, WBEM_ERR_STATE, "wbem_update_nodes: no geometry");
+  for (long long k = 0; k < 3LL * h->N; ++k)
+    if (!std::isfinite(X[k])) return fail(h, WBEM_ERR_NONFINITE, "wbem_update_nodes: non-finite support point");
+  cudaSetDevice(h->device);
+  h->X.assign(X, X + 3 * (size_t)h->N);
+  std::vector<double> Xi((size_t)h->N * 3);
+  for (int i = 0; i < h->N; ++i)
+    for (int d = 0; d < 3; ++d) Xi[3 * (size_t)i + d] = X[3 * (size_t)h->perm[i] + d];
+  CU(cudaMemcpy(h->d_X, Xi.data(), Xi.size() * sizeof(double), cudaMemcpyHostToDevice));
+  h->assembled_prec = -1;
+  h->factors_valid = false;
+  h->have_solution = false;
+  return WBEM_OK;
+}
+
+int wbem_set_bc(wbem_handle h, const unsigned char* m) {
+  if (!h) return WBEM_ERR_ARG;
+  if (!m || h->N == 0) return fail(h, WBEM_ERR_STATE, "wbem_set_bc: set the geometry first");
+  cudaSetDevice(h->device);
+  h->mask.assign(m, m + h->N);
+  for (auto& v : h->mask) v = v ? 1 : 0;
+  std::vector<uint8_t> mi(h->N);
+  for (int i = 0; i < h->N; ++i) mi[i] = h->mask[h->perm[i]];
+  CHK(upload(h, &h->d_mask, mi));
+  h->have_mask = true;
+  h->factors_valid = false;
+  h->have_solution = false;
+  return WBEM_OK;
+}
+
+int wbem_assemble(wbem_handle h, const wbem_options* opt) {
+  if (!h) return WBEM_ERR_ARG;
+  if (h->N == 0) return fail(h, WBEM_ERR_STATE, "wbem_assemble: set the geometry first");
+  wbem_options o;
+  if (opt) o = *opt;
+  else wbem_default_options(&o);
+  if (o.precision != WBEM_PREC_FP64 && o.precision != WBEM_PREC_MIXED)
+    return fail(h, WBEM_ERR_ARG, "wbem_assemble: unknown precision");
+  if (o.gmres_restart < 1 || o.gmres_restart > 250)
+    return fail(h, WBEM_ERR_ARG, "wbem_assemble: gmres_restart must be in [1,250]");
+  if (o.max_steps < 1) return fail(h, WBEM_ERR_ARG, "wbem_assemble: max_steps must be >= 1");
+  if (!(o.tolerance >= 0)) return fail(h, WBEM_ERR_ARG, "wbem_assemble: tolerance must be >= 0");
+  h->opt = o;
+  cudaSetDevice(h->device);
+  CHK(build_quadrature(h, o.quadrature_order, o.singular_quadrature_order));
+  h->launches = 0;
+  h->stats = wbem_stats{};
+  h->stats.n_dofs = h->N;
+  h->stats.n_cells = h->C;
+  h->factors_valid = false;
+  h->have_solution = false;
+  const int N = h->N;
+  Timer tm(h->stream);
+  if (o.precision == WBEM_PREC_FP64) {
+    free_mixed(h);
+    const size_t nn = (size_t)N * N;
+    if (!h->d_N || h->mat_elems != nn || h->d_N2) {
+      if (h->d_N2) { cudaFree(h->d_N2); h->d_N2 = nullptr; }
+      if (h->d_D2) { cudaFree(h->d_D2); h->d_D2 = nullptr; }
+      CHK(dev_alloc(h, &h->d_N, nn));
+      CHK(dev_alloc(h, &h->d_D, nn));
+      h->mat_elems = nn;
+    }
+    if (!h->d_alpha) CHK(dev_alloc(h, &h->d_alpha, (size_t)N));
+    const int nq = o.quadrature_order * o.quadrature_order;
+    if (h->rec_cells != (size_t)h->C * nq || !h->d_rec) {
+      CHK(dev_alloc(h, &h->d_rec, (size_t)h->C * nq * 8));
+      h->rec_cells = (size_t)h->C * nq;
+    }
+    CU(launch_cell_records_fp64(h->C, h->d_X, h->d_cell_dofs, h->d_rec, o.quadrature_order, h->stream));
+    h->stats.t_geometry_ms = tm.ms();
+    CU(launch_tile_fp64(N, o.quadrature_order, h->d_X, h->d_dnset, h->n_tiles, h->d_tile_ptr,
+                        h->d_tile_ent, h->d_cell_dofs, h->d_rec, h->d_N, h->d_D, h->d_err, h->stream));
+    h->stats.t_assemble_ms = tm.ms();
+    CU(launch_singular_fp64(N, h->d_X, h->d_dnset, h->d_sptr, h->d_scell, h->d_cell_dofs, h->d_N,
+                            h->d_D, h->d_err, h->stream));
+    h->stats.t_singular_ms = tm.ms();
+    CU(launch_alpha_rowsum(N, h->d_N, h->d_alpha, h->stream));
+    h->stats.t_alpha_ms = tm.ms();
+    h->launches += 4;
+    CHK(check_device_error(h, "wbem_assemble"));
+    h->assembled_prec = WBEM_PREC_FP64;
+  } else {
+    CHK(assemble_mixed(h));
+    h->assembled_prec = WBEM_PREC_MIXED;
+  }
+  return WBEM_OK;
+}
+
+static int prepare_rhs(wbem_handle h, const double* tmp_rhs) {
+  // known data in internal order, rhs = compute_rhs(tmp_rhs), constraints
+  const int N = h->N;
+  CHK(build_constraints(h, tmp_rhs));
+  std::vector<double> bi(N);
+  for (int i = 0; i < N; ++i) bi[i] = tmp_rhs[h->perm[i]];
+  CU(cudaMemcpyAsync(h->d_b, bi.data(), sizeof(double) * N, cudaMemcpyHostToDevice, h->stream));
+  if (h->assembled_prec == WBEM_PREC_FP64)
+    CU(launch_matvec_fp64(N, 1, h->d_N, h->d_D, h->d_mask, h->d_alpha, h->d_b, h->d_rhs, h->stream));
+  else
+    CU(launch_matvec_mixed(N, 1, h->d_N2, h->d_D2, h->d_mask, h->d_alpha, h->d_b, h->d_rhs, h->stream));
+  CU(launch_set_rows(h->n_crows, h->d_crow, h->d_cinh, h->d_rhs, h->stream));
+  h->launches += 2;
+  CU(cudaStreamSynchronize(h->stream));
+  return WBEM_OK;
+}
+
+int wbem_solve_system(wbem_handle h, const double* tmp_rhs, double* phi, double* dphi_dn) {
+  if (!h) return WBEM_ERR_ARG;
+  if (!tmp_rhs || !phi || !dphi_dn) return fail(h, WBEM_ERR_ARG, "wbem_solve_system: NULL pointer");
+  if (h->assembled_prec < 0) return fail(h, WBEM_ERR_STATE, "wbem_solve_system: assemble first");
+  if (!h->have_mask) return fail(h, WBEM_ERR_STATE, "wbem_solve_system: set the boundary conditions first");
+  const int N = h->N;
+  for (int i = 0; i < N; ++i)
+    if (!std::isfinite(tmp_rhs[i])) return fail(h, WBEM_ERR_NONFINITE, "wbem_solve_system: non-finite tmp_rhs");
+  bool any_dir = false;
+  for (int i = 0; i < N; ++i) any_dir |= h->mask[i] != 0;
+  if (!any_dir)
+    return fail(h, WBEM_ERR_ARG,
+                "wbem_solve_system: all-Neumann problems are singular (the reference's norm shift is not a linear operator)");
+  cudaSetDevice(h->device);
+  CHK(ensure_vectors(h, h->opt.gmres_restart));
+  Timer tm(h->stream);
+  CHK(prepare_rhs(h, tmp_rhs));
+  int solver = h->opt.solver;
+  if (solver == WBEM_SOLVER_AUTO) solver = h->assembled_prec == WBEM_PREC_FP64 ? WBEM_SOLVER_GMRES : WBEM_SOLVER_LU;
+  if (h->assembled_prec == WBEM_PREC_FP64) {
+    if (!h->factors_valid) {
+      CHK(build_block_jacobi(h));
+      h->factors_valid = true;
+    }
+    h->stats.t_factor_ms = tm.ms();
+    CHK(gmres_fp64(h, h->d_rhs, h->d_sol, 0));
+  } else {
+    if (!h->factors_valid) {
+      CHK(factor_mixed(h));
+      h->factors_valid = true;
+    }
+    h->stats.t_factor_ms = tm.ms();
+    CHK(solve_mixed(h, h->d_rhs, h->d_sol, 0));
+  }
+  h->stats.t_solve_ms = tm.ms();
+  CHK(check_device_error(h, "wbem_solve_system"));
+  // unpack (source/bem_problem.cc:869-879)
+  std::vector<double> si(N);
+  CU(cudaMemcpy(si.data(), h->d_sol, sizeof(double) * N, cudaMemcpyDeviceToHost));
+  for (int i = 0; i < N; ++i) {
+    if (!std::isfinite(si[i])) return fail(h, WBEM_ERR_NONFINITE, "wbem_solve_system: non-finite solution");
+    const int p = h->perm[i];
+    if (h->mask[p] == 0) phi[p] = si[i];
+    else dphi_dn[p] = si[i];
+  }
+  h->have_solution = true;
+  h->stats.kernel_launches = h->launches;
+  return WBEM_OK;
+}
+
+int wbem_solve(wbem_handle h, const wbem_options* opt, const double* tmp_rhs, double* phi,
+               double* dphi_dn) {
+  CHK(wbem_assemble(h, opt));
+  return wbem_solve_system(h, tmp_rhs, phi, dphi_dn);
+}
+
+int wbem_get_alpha(wbem_handle h, double* alpha) {
+  if (!h) return WBEM_ERR_ARG;
+  if (!alpha) return fail(h, WBEM_ERR_ARG, "wbem_get_alpha: NULL pointer");
+  if (h->assembled_prec < 0) return fail(h, WBEM_ERR_STATE, "wbem_get_alpha: assemble first");
+  cudaSetDevice(h->device);
+  std::vector<double> a(h->N);
+  CU(cudaMemcpy(a.data(), h->d_alpha, sizeof(double) * h->N, cudaMemcpyDeviceToHost));
+  for (int i = 0; i < h->N; ++i) alpha[h->perm[i]] = a[i];
+  return WBEM_OK;
+}
+
+int wbem_get_matrices(wbem_handle h, double* neumann, double* dirichlet) {
+  if (!h) return WBEM_ERR_ARG;
+  if (h->assembled_prec < 0) return fail(h, WBEM_ERR_STATE, "wbem_get_matrices: assemble first");
+  cudaSetDevice(h->device);
+  const int N = h->N;
+  const int rows_per = std::max(1, (int)std::min<size_t>((size_t)N, (size_t)(64u << 20) / (8 * (size_t)N)));
+  double* buf = nullptr;
+  CU(cudaMalloc(&buf, sizeof(double) * (size_t)rows_per * N));
+  int st = WBEM_OK;
+  for (int which = 0; which < 2 && st == WBEM_OK; ++which) {
+    double* out = which == 0 ? neumann : dirichlet;
+    if (!out) continue;
+    const double* A = which == 0 ? h->d_N : h->d_D;
+    const float2* A2 = which == 0 ? h->d_N2 : h->d_D2;
+    for (int r0 = 0; r0 < N && st == WBEM_OK; r0 += rows_per) {
+      const int nr = std::min(rows_per, N - r0);
+      cudaError_t e = launch_gather_rows(N, r0, nr, h->d_iperm, A, A2, buf, h->stream);
+      if (e != cudaSuccess) st = fail(h, WBEM_ERR_CUDA, cudaGetErrorString(e));
+      if (st == WBEM_OK) {
+        e = cudaMemcpyAsync(out + (size_t)r0 * N, buf, sizeof(double) * (size_t)nr * N,
+                            cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) st = fail(h, WBEM_ERR_CUDA, cudaGetErrorString(e));
+      }
+    }
+  }
+  cudaFree(buf);
+  return st;
+}
+
+static int op_caller(wbem_handle h, int mode, const double* src, double* dst) {
+  if (!h) return WBEM_ERR_ARG;
+  if (!src || !dst) return fail(h, WBEM_ERR_ARG, "NULL pointer");
+  if (h->assembled_prec < 0) return fail(h, WBEM_ERR_STATE, "assemble first");
+  if (!h->have_mask) return fail(h, WBEM_ERR_STATE, "set the boundary conditions first");
+  cudaSetDevice(h->device);
+  CHK(ensure_vectors(h, h->opt.gmres_restart));
+  const int N = h->N;
+  std::vector<double> xi(N), yi(N);
+  for (int i = 0; i < N; ++i) xi[i] = src[h->perm[i]];
+  CU(cudaMemcpy(h->d_vec[3], xi.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+  if (h->assembled_prec == WBEM_PREC_FP64)
+    CU(launch_matvec_fp64(N, mode, h->d_N, h->d_D, h->d_mask, h->d_alpha, h->d_vec[3], h->d_vec[4], h->stream));
+  else
+    CU(launch_matvec_mixed(N, mode, h->d_N2, h->d_D2, h->d_mask, h->d_alpha, h->d_vec[3], h->d_vec[4], h->stream));
+  CU(cudaMemcpy(yi.data(), h->d_vec[4], sizeof(double) * N, cudaMemcpyDeviceToHost));
+  for (int i = 0; i < N; ++i) dst[h->perm[i]] = yi[i];
+  if (mode == 0) {
+    // all-Neumann case of the reference: dst -= ||dst||_2 (source/bem_problem.cc:667-668)
+    bool any = false;
+    for (int i = 0; i < N; ++i) any |= h->mask[i] != 0;
+    if (!any) {
+      double s = 0;
+      for (int i = 0; i < N; ++i) s += dst[i] * dst[i];
+      s = std::sqrt(s);
+      for (int i = 0; i < N; ++i) dst[i] -= s;
+    }
+  }
+  return WBEM_OK;
+}
+
+int wbem_vmult(wbem_handle h, const double* src, double* dst) { return op_caller(h, 0, src, dst); }
+int wbem_compute_rhs(wbem_handle h, const double* src, double* dst) { return op_caller(h, 1, src, dst); }
+
+int wbem_hull_force(wbem_handle h, const int* hull_cells, int n_hull, const double* U, int dir,
+                    const double* phi, const double* dphi_dn, double* force) {
+  if (!h) return WBEM_ERR_ARG;
+  if (!hull_cells || !U || !phi || !dphi_dn || !force || n_hull < 0 || dir < 0 || dir > 2)
+    return fail(h, WBEM_ERR_ARG, "wbem_hull_force: bad argument");
+  if (h->N == 0) return fail(h, WBEM_ERR_STATE, "wbem_hull_force: set the geometry first");
+  cudaSetDevice(h->device);
+  CHK(ensure_vectors(h, h->opt.gmres_restart));
+  const int N = h->N;
+  std::vector<double> pi(N), qi(N);
+  for (int i = 0; i < N; ++i) {
+    pi[i] = phi[h->perm[i]];
+    qi[i] = dphi_dn[h->perm[i]];
+  }
+  CU(cudaMemcpy(h->d_vec[3], pi.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(h->d_vec[4], qi.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+  return hull_force_dev(h, hull_cells, n_hull, U, dir, h->d_vec[3], h->d_vec[4], force);
+}
+
+int wbem_force_adjoint(wbem_handle h, const int* hull_cells, int n_hull, const double* U, int dir,
+                       const double* tmp_rhs, double* dF_dX, double* dF_drhs) {
+  if (!h) return WBEM_ERR_ARG;
+  if (!hull_cells || !U || !tmp_rhs || !dF_dX || !dF_drhs || n_hull < 0 || dir < 0 || dir > 2)
+    return fail(h, WBEM_ERR_ARG, "wbem_force_adjoint: bad argument");
+  if (!h->have_solution) return fail(h, WBEM_ERR_STATE, "wbem_force_adjoint: solve first");
+  cudaSetDevice(h->device);
+  return adjoint_force(h, hull_cells, n_hull, U, dir, tmp_rhs, dF_dX, dF_drhs);
+}
+
+int wbem_get_stats(wbem_handle h, wbem_stats* st) {
+  if (!h || !st) return WBEM_ERR_ARG;
+  *st = h->stats;
+  return WBEM_OK;
+}
+
+}  // extern "C"
