@@ -7,14 +7,19 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def declared_symbols():
-    txt = open(os.path.join(ROOT, "include", "wbem.h")).read()
-    return sorted(set(re.findall(r"\b(wbem_[a-z_]+)\s*\(", txt)))
+def declared_symbols(header=None):
+    names = [header] if header else sorted(f for f in os.listdir(os.path.join(ROOT, "include"))
+                                           if f.endswith(".h"))
+    out = set()
+    for n in names:
+        txt = open(os.path.join(ROOT, "include", n)).read()
+        out |= set(re.findall(r"\b(wbem_[a-z0-9_]+)\s*\(", txt))
+    return sorted(out)
 
 
 def test_header_lists_match_wrapper():
     from wavebem_gb300.bem_problem import EXPORTS
-    assert sorted(EXPORTS) == declared_symbols()
+    assert sorted(EXPORTS) == declared_symbols("wbem.h")
 
 
 def test_library_exports_every_declared_symbol():

@@ -1,0 +1,63 @@
+"""Mixed-precision form against the FP64 oracle.
+
+Entries: double-float panel base + FP32 point differences; tolerance 5e-9
+relative to the largest entry (measured ~1e-9). Solution: FP32 LU (BF16x3
+trailing updates) + FP64 GMRES refinement; tolerance 1e-8 relative 2-norm
+(the spec bar)."""
+import numpy as np
+import pytest
+
+from helpers import oracle_problem, rel2, relmax
+from wavebem_gb300 import meshes as M
+from wavebem_gb300.bem_problem import PREC_MIXED, BEMProblem
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("kind,n", [("wigley", 2000), ("sphere", 12)])
+def test_mixed_matrices_alpha(kind, n):
+    P, m, b = oracle_problem(kind, n)
+    g = BEMProblem(m.X, m.cells, m.dirichlet, P.dn_ptr, P.dn_idx, precision=PREC_MIXED)
+    g.assemble_system()
+    Nm, Dm = g.matrices()
+    a = g.compute_alpha()
+    assert relmax(Nm, P.Nm) <= 5e-9
+    assert relmax(Dm, P.Dm) <= 5e-9
+    assert relmax(a, P.alpha) <= 5e-9
+
+
+@pytest.mark.parametrize("kind,n", [("wigley", 2000), ("sphere", 12)])
+def test_mixed_solve_within_1e8(kind, n):
+    P, m, b = oracle_problem(kind, n)
+    phi_o, dphi_o, _ = P.solve_system(b)
+    g = BEMProblem(m.X, m.cells, m.dirichlet, P.dn_ptr, P.dn_idx, precision=PREC_MIXED)
+    phi, dphi = b.copy(), b.copy()
+    g.solve(phi, dphi, b)
+    st = g.stats()
+    assert rel2(phi, phi_o) <= 1e-8
+    assert rel2(dphi, dphi_o) <= 1e-8
+    assert st["iterations"] <= 20
+
+
+def test_mixed_hull_force_within_1e8():
+    P, m, b = oracle_problem("wigley", 2000)
+    phi_o, dphi_o, _ = P.solve_system(b)
+    hull = np.nonzero(m.face == M.HULL)[0].astype(np.int32)
+    F_o = P.hull_force(m.cells[hull], phi_o, dphi_o)
+    g = BEMProblem(m.X, m.cells, m.dirichlet, P.dn_ptr, P.dn_idx, precision=PREC_MIXED)
+    phi, dphi = b.copy(), b.copy()
+    g.solve(phi, dphi, b)
+    F = g.hull_force(hull, phi, dphi)
+    assert abs(F - F_o) <= 1e-8 * abs(F_o)
+
+
+def test_mixed_solve_system_reuses_factors():
+    P, m, b = oracle_problem("wigley", 2000)
+    g = BEMProblem(m.X, m.cells, m.dirichlet, P.dn_ptr, P.dn_idx, precision=PREC_MIXED)
+    g.assemble_system()
+    for seed in (1, 2):
+        b2 = M.wigley_bc(m, seed=seed)
+        phi_o, dphi_o, _ = P.solve_system(b2)
+        phi, dphi = b2.copy(), b2.copy()
+        g.solve_system(phi, dphi, b2)
+        assert rel2(phi, phi_o) <= 1e-8 and rel2(dphi, dphi_o) <= 1e-8

@@ -13,7 +13,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libwbem.so")
 PEAKS_LIB = os.path.join(HERE, "libwbem_peaks.so")
-SOURCES = ["wbem_api.cu", "assemble_fp64.cu", "solve.cu", "mixed.cu", "force.cu", "adjoint.cu"]
+SOURCES = ["wbem_api.cu", "assemble_fp64.cu", "solve.cu", "mixed.cu", "lu.cu", "force.cu", "adjoint.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-Xptxas", "-warn-spills"]
@@ -39,7 +39,7 @@ def build(verbose: bool = False, extra=()) -> str:
     os.makedirs(BUILD, exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 1)) as ex:
         objs = list(ex.map(lambda s: _compile(s, extra), SOURCES))
-    cmd = [_nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcuda"]
+    cmd = [_nvcc(), *ARCH, "-shared", "-o", LIB, *objs]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -28,7 +28,8 @@ static int hull_dofs_upload(wbem_context* h, const int* hull_cells, int n_hull, 
     h->err = "cudaMalloc failed";
     return WBEM_ERR_NOMEM;
   }
-  cudaMemcpy(*out, hd.data(), sizeof(int4) * hd.size(), cudaMemcpyHostToDevice);
+  cudaMemcpyAsync(*out, hd.data(), sizeof(int4) * hd.size(), cudaMemcpyHostToDevice, h->stream);
+  cudaStreamSynchronize(h->stream);
   return WBEM_OK;
 }
 

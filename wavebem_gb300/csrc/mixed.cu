@@ -1,23 +1,551 @@
-// Mixed-precision form (placeholder until the kernels land).
+// Mixed-precision assembly of N (dG/dn) and D (G).
+//
+// Regular panels far from the collocation point are integrated with the same
+// Gauss rule as the reference (source/bem_problem.cc:241-260), but evaluated as
+//     k(x_q - x_i) = k(c - x_i) + [k(x_q - x_i) - k(c - x_i)]
+// with c the panel centre: the panel term k(c - x_i) (and its contraction with
+// the exact panel moments sum_q phi_j(q) JxW_q) is computed once per
+// (row, panel) pair in double-float arithmetic on FP32 units, and the
+// per-quadrature-point differences are computed in FP32 from cancellation-free
+// forms (1/a - 1/b = (b^2 - a^2) / (a b (a + b)) etc.). The FP32 rounding
+// then only touches the O(h/r) difference terms, which keeps entries accurate
+// to about 1e-9 relative instead of the 1e-7 of plain FP32 evaluation.
+// Panels within `ratio` diameters of the collocation point and the singular
+// panels are integrated in FP64 (k_near_mixed, k_singular_mixed).
+// Entries are stored as (hi, lo) float pairs; alpha = -sum_j N_ij is
+// accumulated in FP64 from the three parts.
 #include <cuda_runtime.h>
+#include <stdint.h>
 #include "context.h"
+#include "host_util.h"
+#include "kernels.h"
 
 namespace wbem {
+
 static __constant__ QuadTables c_qm;
 cudaError_t upload_quadrature_mixed(const QuadTables& t) {
   return cudaMemcpyToSymbol(c_qm, &t, sizeof(QuadTables));
 }
+
+constexpr double kInv4PiM = 0.07957747154594766788;
+
+__host__ __device__ constexpr int mixed_rec_floats(int nq) { return ((9 * nq + 24 + 3) / 4) * 4; }
+
+// Same near test in every kernel (no contraction: explicit round-to-nearest ops).
+__device__ __forceinline__ bool near_test(float xi, float yi, float zi, float4 g) {
+  const float dx = __fsub_rn(g.x, xi), dy = __fsub_rn(g.y, yi), dz = __fsub_rn(g.z, zi);
+  const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+  return d2 < g.w;
+}
+
+__device__ __forceinline__ bool in_set_m(const int set[kMaxSet], int v) {
+  bool r = false;
+#pragma unroll
+  for (int k = 0; k < kMaxSet; ++k) r |= (set[k] == v);
+  return r;
+}
+
+__device__ __forceinline__ void q1_geo(const double P[4][3], double s, double t, double x[3],
+                                       double cr[3]) {
+  const double a0 = (1 - s) * (1 - t), a1 = s * (1 - t), a2 = (1 - s) * t, a3 = s * t;
+  double jx[3], je[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    x[d] = a0 * P[0][d] + a1 * P[1][d] + a2 * P[2][d] + a3 * P[3][d];
+    jx[d] = (1 - t) * (P[1][d] - P[0][d]) + t * (P[3][d] - P[2][d]);
+    je[d] = (1 - s) * (P[2][d] - P[0][d]) + s * (P[3][d] - P[1][d]);
+  }
+  cr[0] = jx[1] * je[2] - jx[2] * je[1];
+  cr[1] = jx[2] * je[0] - jx[0] * je[2];
+  cr[2] = jx[0] * je[1] - jx[1] * je[0];
+}
+
+// One thread per panel: FP64 geometry -> mixed record + near-test data.
+__global__ void k_cell_records_mixed(int C, const double* __restrict__ X,
+                                     const int4* __restrict__ cell_dofs, float* __restrict__ rec,
+                                     float4* __restrict__ cellgeo, float ratio) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= C) return;
+  const int nq = c_qm.q1 * c_qm.q1;
+  const int RF = mixed_rec_floats(nq);
+  const int4 d = cell_dofs[c];
+  const int id[4] = {d.x, d.y, d.z, d.w};
+  double P[4][3];
+  for (int k = 0; k < 4; ++k)
+    for (int e = 0; e < 3; ++e) P[k][e] = X[3 * (size_t)id[k] + e];
+  double cen[3], nu[3] = {0, 0, 0};
+  for (int e = 0; e < 3; ++e) cen[e] = 0.25 * (P[0][e] + P[1][e] + P[2][e] + P[3][e]);
+  double M[4] = {0, 0, 0, 0};
+  for (int q = 0; q < nq; ++q) {
+    double x[3], cr[3];
+    q1_geo(P, c_qm.gp[q][0], c_qm.gp[q][1], x, cr);
+    const double w = c_qm.gp[q][2];
+    for (int e = 0; e < 3; ++e) nu[e] += cr[e] * w;
+    const double jw = sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]) * w * kInv4PiM;
+    for (int j = 0; j < 4; ++j) M[j] += c_qm.phi[q][j] * jw;
+  }
+  const double nl = sqrt(nu[0] * nu[0] + nu[1] * nu[1] + nu[2] * nu[2]);
+  for (int e = 0; e < 3; ++e) nu[e] /= nl;
+  float* r = rec + (size_t)c * RF;
+  for (int q = 0; q < nq; ++q) {
+    double x[3], cr[3];
+    q1_geo(P, c_qm.gp[q][0], c_qm.gp[q][1], x, cr);
+    const double det = sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+    double del[3], n[3];
+    for (int e = 0; e < 3; ++e) {
+      del[e] = x[e] - cen[e];
+      n[e] = cr[e] / det;
+    }
+    r[4 * q + 0] = (float)del[0];
+    r[4 * q + 1] = (float)del[1];
+    r[4 * q + 2] = (float)del[2];
+    r[4 * q + 3] = (float)(del[0] * del[0] + del[1] * del[1] + del[2] * del[2]);
+    r[4 * nq + 4 * q + 0] = (float)(n[0] - nu[0]);
+    r[4 * nq + 4 * q + 1] = (float)(n[1] - nu[1]);
+    r[4 * nq + 4 * q + 2] = (float)(n[2] - nu[2]);
+    r[4 * nq + 4 * q + 3] = (float)(del[0] * n[0] + del[1] * n[1] + del[2] * n[2]);
+    r[8 * nq + q] = (float)(det * c_qm.gp[q][2] * kInv4PiM);
+  }
+  float* cd = r + 9 * nq;
+  for (int e = 0; e < 3; ++e) {
+    const df a = df_from_double(cen[e]);
+    cd[e] = a.hi;
+    cd[3 + e] = a.lo;
+    const df b = df_from_double(nu[e]);
+    cd[6 + e] = b.hi;
+    cd[9 + e] = b.lo;
+  }
+  double Mt = 0;
+  for (int j = 0; j < 4; ++j) {
+    const df a = df_from_double(M[j]);
+    cd[12 + j] = a.hi;
+    cd[16 + j] = a.lo;
+    Mt += M[j];
+  }
+  const df t = df_from_double(Mt);
+  cd[20] = t.hi;
+  cd[21] = t.lo;
+  cd[22] = 0.f;
+  cd[23] = 0.f;
+  for (int k = 9 * nq + 24; k < RF; ++k) r[k] = 0.f;
+  // near test: centre (float) and (ratio * largest diagonal)^2
+  double d1 = 0, d2 = 0;
+  for (int e = 0; e < 3; ++e) {
+    d1 += (P[3][e] - P[0][e]) * (P[3][e] - P[0][e]);
+    d2 += (P[2][e] - P[1][e]) * (P[2][e] - P[1][e]);
+  }
+  const double diam = sqrt(d1 > d2 ? d1 : d2);
+  const double rad = (double)ratio * diam;
+  cellgeo[c] = make_float4((float)cen[0], (float)cen[1], (float)cen[2], (float)(rad * rad));
+}
+
+constexpr int kChunkM = 8;
+
+template <int Q1>
+__global__ void __launch_bounds__(kRowsPerTile)
+    k_tile_mixed(int N, const double* __restrict__ X, const int* __restrict__ dnset,
+                 const int* __restrict__ tile_ptr, const int2* __restrict__ tile_ent,
+                 const int4* __restrict__ cell_dofs, const float* __restrict__ rec,
+                 const float4* __restrict__ cellgeo, float2* __restrict__ N2,
+                 float2* __restrict__ D2, double* __restrict__ alpha_part, DevErr* err) {
+  constexpr int NQ = Q1 * Q1;
+  constexpr int RF = mixed_rec_floats(NQ);
+  constexpr int RT = kRowsPerTile, CT = kColsPerTile, LDA = RT + 1;
+  extern __shared__ __align__(128) unsigned char smem[];
+  float* stage = reinterpret_cast<float*>(smem);  // [2][kChunkM][RF]
+  float* aNh = stage + 2 * kChunkM * RF;          // [CT][LDA] x 4
+  float* aNl = aNh + CT * LDA;
+  float* aDh = aNl + CT * LDA;
+  float* aDl = aDh + CT * LDA;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(aDl + CT * LDA + ((CT * LDA) & 1));
+
+  const int tid = threadIdx.x;
+  const int tile = blockIdx.x;
+  const int row0 = blockIdx.y * RT;
+  const int row = row0 + tid;
+  const bool active = row < N;
+  df xr[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+  int set[kMaxSet];
+#pragma unroll
+  for (int k = 0; k < kMaxSet; ++k) set[k] = -2;
+  if (active) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) xr[d] = df_from_double(X[3 * (size_t)row + d]);
+#pragma unroll
+    for (int k = 0; k < kMaxSet; ++k) set[k] = dnset[(size_t)row * kMaxSet + k];
+  }
+  const float xf = active ? __double2float_rn(X[3 * (size_t)row]) : 0.f;
+  const float yf = active ? __double2float_rn(X[3 * (size_t)row + 1]) : 0.f;
+  const float zf = active ? __double2float_rn(X[3 * (size_t)row + 2]) : 0.f;
+  for (int k = tid; k < CT * LDA; k += RT) {
+    aNh[k] = 0.f;
+    aNl[k] = 0.f;
+    aDh[k] = 0.f;
+    aDl[k] = 0.f;
+  }
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  df alpha_acc = {0.f, 0.f};
+
+  const int e0 = tile_ptr[tile], e1 = tile_ptr[tile + 1];
+  const int nch = (e1 - e0 + kChunkM - 1) / kChunkM;
+  auto issue = [&](int c) {
+    const int sidx = c & 1;
+    const int base = e0 + c * kChunkM;
+    const int cnt = min(kChunkM, e1 - base);
+    mbar_arrive_expect_tx(&bar[sidx], (uint32_t)(cnt * RF * 4));
+    for (int k = 0; k < cnt; ++k) {
+      const int cell = tile_ent[base + k].x & 0x7fffffff;
+      bulk_g2s(stage + (size_t)(sidx * kChunkM + k) * RF, rec + (size_t)cell * RF,
+               (uint32_t)(RF * 4), &bar[sidx]);
+    }
+  };
+  if (tid == 0 && nch > 0) issue(0);
+
+  for (int c = 0; c < nch; ++c) {
+    if (tid == 0 && c + 1 < nch) {
+      fence_proxy_async_smem();
+      issue(c + 1);
+    }
+    const bool ok = mbar_wait_bounded(&bar[c & 1], (uint32_t)((c >> 1) & 1));
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) {
+        dev_fail(err, WBEM_ERR_TIMEOUT, 41, tile, c);
+        if (c + 1 < nch) mbar_wait_bounded(&bar[(c + 1) & 1], (uint32_t)(((c + 1) >> 1) & 1));
+      }
+      return;
+    }
+    const int base = e0 + c * kChunkM;
+    const int cnt = min(kChunkM, e1 - base);
+    for (int k = 0; k < cnt; ++k) {
+      const int2 ent = tile_ent[base + k];
+      const int cell = ent.x & 0x7fffffff;
+      const bool owner = ent.x < 0;
+      const uint32_t slots = (uint32_t)ent.y;
+      const int4 dd = cell_dofs[cell];
+      const bool sing = in_set_m(set, dd.x) || in_set_m(set, dd.y) || in_set_m(set, dd.z) ||
+                        in_set_m(set, dd.w);
+      if (!active || sing || near_test(xf, yf, zf, cellgeo[cell])) continue;
+      const float* r = stage + (size_t)((c & 1) * kChunkM + k) * RF;
+      const float4* qa = reinterpret_cast<const float4*>(r);
+      const float4* qb = reinterpret_cast<const float4*>(r + 4 * NQ);
+      const float* qj = r + 8 * NQ;
+      const float* cd = r + 9 * NQ;
+      // ---- panel base term in double-float
+      df R[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        df s = two_sum(cd[d], -xr[d].hi);
+        s.lo += cd[3 + d] - xr[d].lo;
+        R[d] = fast_two_sum(s.hi, s.lo);
+      }
+      df r2 = two_prod(R[0].hi, R[0].hi);
+      r2.lo = __fmaf_rn(2.f * R[0].hi, R[0].lo, r2.lo);
+#pragma unroll
+      for (int d = 1; d < 3; ++d) {
+        df p = two_prod(R[d].hi, R[d].hi);
+        p.lo = __fmaf_rn(2.f * R[d].hi, R[d].lo, p.lo);
+        r2 = df_add_fast(r2, p);
+      }
+      const float y0 = rsqrtf(r2.hi);
+      const df t = df_mul(r2, two_prod(y0, y0));
+      const float ecor = (1.0f - t.hi) - t.lo;
+      const df rinv = fast_two_sum(y0, 0.5f * y0 * ecor);
+      const df ri3 = df_mul(df_mul(rinv, rinv), rinv);
+      df Rn = df_mul(R[0], df{cd[6], cd[9]});
+      Rn = df_add(Rn, df_mul(R[1], df{cd[7], cd[10]}));
+      Rn = df_add(Rn, df_mul(R[2], df{cd[8], cd[11]}));
+      df gR = df_mul(Rn, ri3);
+      gR.hi = -gR.hi;
+      gR.lo = -gR.lo;
+      // ---- per-point differences in FP32
+      const float Rcx = R[0].hi, Rcy = R[1].hi, Rcz = R[2].hi;
+      const float rcinv = rinv.hi;
+      const float rc = r2.hi * rcinv;
+      const float rc2 = r2.hi;
+      const float rcinv3 = ri3.hi;
+      const float Rnf = Rn.hi;
+      float ls0 = 0.f, ls1 = 0.f, ls2 = 0.f, ls3 = 0.f, ln0 = 0.f, ln1 = 0.f, ln2 = 0.f, ln3 = 0.f;
+      float fnsum = 0.f;
+#pragma unroll 4
+      for (int q = 0; q < NQ; ++q) {
+        const float4 A = qa[q];
+        const float4 B = qb[q];
+        const float J = qj[q];
+        const float Rx = Rcx + A.x, Ry = Rcy + A.y, Rz = Rcz + A.z;
+        const float rq2 = __fmaf_rn(Rx, Rx, __fmaf_rn(Ry, Ry, Rz * Rz));
+        const float rqinv = rsqrtf(rq2);
+        const float rq = rq2 * rqinv;
+        const float Rd = __fmaf_rn(Rcx, A.x, __fmaf_rn(Rcy, A.y, Rcz * A.z));
+        const float num = -__fmaf_rn(2.f, Rd, A.w);
+        const float dr = __fdividef(num, rc + rq);
+        const float ds = dr * rqinv * rcinv;
+        const float rqinv3 = rqinv * rqinv * rqinv;
+        const float tsum = __fmaf_rn(rc, rq, rc2) + rq2;
+        const float dg = -(dr * tsum) * rqinv3 * rcinv3;
+        const float t2 = __fmaf_rn(Rcx, B.x, __fmaf_rn(Rcy, B.y, __fmaf_rn(Rcz, B.z, B.w)));
+        const float ddn = __fmaf_rn(Rnf, dg, -t2 * rqinv3);
+        const float fs = ds * J, fn = ddn * J;
+        fnsum += fn;
+        ls0 = __fmaf_rn(fs, (float)c_qm.phi[q][0], ls0);
+        ls1 = __fmaf_rn(fs, (float)c_qm.phi[q][1], ls1);
+        ls2 = __fmaf_rn(fs, (float)c_qm.phi[q][2], ls2);
+        ls3 = __fmaf_rn(fs, (float)c_qm.phi[q][3], ls3);
+        ln0 = __fmaf_rn(fn, (float)c_qm.phi[q][0], ln0);
+        ln1 = __fmaf_rn(fn, (float)c_qm.phi[q][1], ln1);
+        ln2 = __fmaf_rn(fn, (float)c_qm.phi[q][2], ln2);
+        ln3 = __fmaf_rn(fn, (float)c_qm.phi[q][3], ln3);
+      }
+      const float lsv[4] = {ls0, ls1, ls2, ls3}, lnv[4] = {ln0, ln1, ln2, ln3};
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const uint32_t sl = (slots >> (8 * j)) & 255u;
+        if (sl != 255u) {
+          const df Mj = {cd[12 + j], cd[16 + j]};
+          const df vs = df_add_f(df_mul(rinv, Mj), lsv[j]);
+          const df vn = df_add_f(df_mul(gR, Mj), lnv[j]);
+          const int o = sl * LDA + tid;
+          df a = df_add_fast(df{aNh[o], aNl[o]}, vn);
+          aNh[o] = a.hi;
+          aNl[o] = a.lo;
+          a = df_add_fast(df{aDh[o], aDl[o]}, vs);
+          aDh[o] = a.hi;
+          aDl[o] = a.lo;
+        }
+      }
+      if (owner) alpha_acc = df_add(alpha_acc, df_add_f(df_mul(gR, df{cd[20], cd[21]}), fnsum));
+    }
+    __syncthreads();
+  }
+  if (active) alpha_part[(size_t)tile * N + row] = df_to_double(alpha_acc);
+  const int col0 = tile * CT;
+  for (int idx = tid; idx < RT * CT; idx += RT) {
+    const int rr = idx / CT, cc = idx % CT;
+    const int gr = row0 + rr, gc = col0 + cc;
+    if (gr < N && gc < N) {
+      const int o = cc * LDA + rr;
+      N2[(size_t)gr * N + gc] = make_float2(aNh[o], aNl[o]);
+      D2[(size_t)gr * N + gc] = make_float2(aDh[o], aDl[o]);
+    }
+  }
+}
+
+template <int Q1>
+static cudaError_t launch_tile_mixed_t(int N, const double* X, const int* dnset, int n_tiles,
+                                       const int* tile_ptr, const int2* tile_ent,
+                                       const int4* cell_dofs, const float* rec,
+                                       const float4* cellgeo, float2* N2, float2* D2,
+                                       double* alpha_part, DevErr* err, cudaStream_t s) {
+  constexpr int RF = mixed_rec_floats(Q1 * Q1);
+  const size_t acc = (size_t)kColsPerTile * (kRowsPerTile + 1);
+  const size_t smem = (size_t)2 * kChunkM * RF * 4 + 4 * acc * 4 + 8 + 2 * sizeof(uint64_t);
+  cudaError_t e = cudaFuncSetAttribute(k_tile_mixed<Q1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  dim3 grid(n_tiles, (N + kRowsPerTile - 1) / kRowsPerTile);
+  k_tile_mixed<Q1><<<grid, kRowsPerTile, smem, s>>>(N, X, dnset, tile_ptr, tile_ent, cell_dofs, rec,
+                                                    cellgeo, N2, D2, alpha_part, err);
+  return cudaGetLastError();
+}
+
+// FP64 near field: one thread per row scans the panels, integrates those that
+// pass the near test (and are not singular) with the regular rule in FP64,
+// and adds them to the (hi, lo) entries.
+__global__ void k_near_mixed(int N, int C, const double* __restrict__ X, const int* __restrict__ dnset,
+                             const int4* __restrict__ cell_dofs, const float4* __restrict__ cellgeo,
+                             const double* __restrict__ rec64, float2* __restrict__ N2,
+                             float2* __restrict__ D2, double* __restrict__ alpha_near) {
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= N) return;
+  const double xi = X[3 * (size_t)row], yi = X[3 * (size_t)row + 1], zi = X[3 * (size_t)row + 2];
+  const float xf = __double2float_rn(xi), yf = __double2float_rn(yi), zf = __double2float_rn(zi);
+  int set[kMaxSet];
+#pragma unroll
+  for (int k = 0; k < kMaxSet; ++k) set[k] = dnset[(size_t)row * kMaxSet + k];
+  const int nq = c_qm.q1 * c_qm.q1;
+  double asum = 0.0;
+  for (int c = 0; c < C; ++c) {
+    if (!near_test(xf, yf, zf, cellgeo[c])) continue;
+    const int4 d = cell_dofs[c];
+    if (in_set_m(set, d.x) || in_set_m(set, d.y) || in_set_m(set, d.z) || in_set_m(set, d.w))
+      continue;
+    const double* r = rec64 + (size_t)c * nq * 8;
+    double ln[4] = {0, 0, 0, 0}, ld[4] = {0, 0, 0, 0};
+    for (int q = 0; q < nq; ++q) {
+      const double Rx = r[8 * q] - xi, Ry = r[8 * q + 1] - yi, Rz = r[8 * q + 2] - zi;
+      const double ri = rsqrt(fma(Rx, Rx, fma(Ry, Ry, Rz * Rz)));
+      const double sq = ri * r[8 * q + 3];
+      const double dq = -fma(Rx, r[8 * q + 4], fma(Ry, r[8 * q + 5], Rz * r[8 * q + 6])) * (ri * ri * ri);
+      for (int j = 0; j < 4; ++j) {
+        ln[j] = fma(dq, c_qm.phi[q][j], ln[j]);
+        ld[j] = fma(sq, c_qm.phi[q][j], ld[j]);
+      }
+    }
+    const int id[4] = {d.x, d.y, d.z, d.w};
+    for (int j = 0; j < 4; ++j) {
+      const size_t o = (size_t)row * N + id[j];
+      float2 v = N2[o];
+      double s = (double)v.x + (double)v.y + ln[j];
+      float h = __double2float_rn(s);
+      N2[o] = make_float2(h, __double2float_rn(s - (double)h));
+      v = D2[o];
+      s = (double)v.x + (double)v.y + ld[j];
+      h = __double2float_rn(s);
+      D2[o] = make_float2(h, __double2float_rn(s - (double)h));
+      asum += ln[j];
+    }
+  }
+  alpha_near[row] = asum;
+}
+
+// FP64 vertex-singular panels, added to the (hi, lo) entries.
+__global__ void k_singular_mixed(int N, const double* __restrict__ X, const int* __restrict__ dnset,
+                                 const int* __restrict__ sptr, const int* __restrict__ scell,
+                                 const int4* __restrict__ cell_dofs, float2* __restrict__ N2,
+                                 float2* __restrict__ D2, double* __restrict__ alpha_sing,
+                                 DevErr* err) {
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= N) return;
+  const double xi = X[3 * (size_t)row], yi = X[3 * (size_t)row + 1], zi = X[3 * (size_t)row + 2];
+  int set[kMaxSet];
+#pragma unroll
+  for (int k = 0; k < kMaxSet; ++k) set[k] = dnset[(size_t)row * kMaxSet + k];
+  const int nsp = c_qm.nsp;
+  double asum = 0.0;
+  for (int e = sptr[row]; e < sptr[row + 1]; ++e) {
+    const int cell = scell[e];
+    const int4 d = cell_dofs[cell];
+    const int id[4] = {d.x, d.y, d.z, d.w};
+    int v = -1;
+    for (int j = 0; j < 4 && v < 0; ++j)
+      if (in_set_m(set, id[j])) v = j;
+    if (v < 0) {
+      dev_fail(err, WBEM_ERR_ARG, 42, row, cell);
+      continue;
+    }
+    double P[4][3];
+    for (int k = 0; k < 4; ++k)
+      for (int c = 0; c < 3; ++c) P[k][c] = X[3 * (size_t)id[k] + c];
+    double ln[4] = {0, 0, 0, 0}, ld[4] = {0, 0, 0, 0};
+    for (int q = 0; q < nsp; ++q) {
+      const double s = c_qm.sp[v][q][0], t = c_qm.sp[v][q][1], w = c_qm.sp[v][q][2] * kInv4PiM;
+      double x[3], cr[3];
+      q1_geo(P, s, t, x, cr);
+      const double det = sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+      const double Rx = x[0] - xi, Ry = x[1] - yi, Rz = x[2] - zi;
+      const double ri = rsqrt(fma(Rx, Rx, fma(Ry, Ry, Rz * Rz)));
+      const double sq = ri * det * w;
+      const double dq = -(Rx * cr[0] + Ry * cr[1] + Rz * cr[2]) * (ri * ri * ri) * w;
+      const double ph[4] = {(1 - s) * (1 - t), s * (1 - t), (1 - s) * t, s * t};
+      for (int j = 0; j < 4; ++j) {
+        ln[j] = fma(dq, ph[j], ln[j]);
+        ld[j] = fma(sq, ph[j], ld[j]);
+      }
+    }
+    for (int j = 0; j < 4; ++j) {
+      const size_t o = (size_t)row * N + id[j];
+      float2 vv = N2[o];
+      double sN = (double)vv.x + (double)vv.y + ln[j];
+      float h = __double2float_rn(sN);
+      N2[o] = make_float2(h, __double2float_rn(sN - (double)h));
+      vv = D2[o];
+      double sD = (double)vv.x + (double)vv.y + ld[j];
+      h = __double2float_rn(sD);
+      D2[o] = make_float2(h, __double2float_rn(sD - (double)h));
+      asum += ln[j];
+    }
+  }
+  alpha_sing[row] = asum;
+}
+
+__global__ void k_alpha_mixed(int N, int n_tiles, const double* __restrict__ part,
+                              const double* __restrict__ an, const double* __restrict__ as,
+                              double* __restrict__ alpha) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  double s = 0;
+  for (int t = 0; t < n_tiles; ++t) s += part[(size_t)t * N + i];
+  alpha[i] = -(s + an[i] + as[i]);
+}
+
+#define CUM WB_CU
+#define CHKM WB_CHK
+
+void free_mixed(wbem_context* h) {
+  if (h->d_N2) { cudaFree(h->d_N2); h->d_N2 = nullptr; }
+  if (h->d_D2) { cudaFree(h->d_D2); h->d_D2 = nullptr; }
+  if (h->d_lu) { cudaFree(h->d_lu); h->d_lu = nullptr; }
+  h->lu_elems = 0;
+}
+
 int assemble_mixed(wbem_context* h) {
-  h->err = "mixed precision form not available";
-  return WBEM_ERR_ARG;
+  const int N = h->N, C = h->C;
+  const wbem_options& o = h->opt;
+  const int q1 = o.quadrature_order;
+  if (q1 < 2 || q1 > 6) {
+    h->err = "mixed form supports quadrature orders 2..6";
+    return WBEM_ERR_ARG;
+  }
+  if (!(o.near_field_ratio >= 1.0)) {
+    h->err = "near_field_ratio must be >= 1";
+    return WBEM_ERR_ARG;
+  }
+  const size_t nn = (size_t)N * N;
+  if (h->d_N) { cudaFree(h->d_N); h->d_N = nullptr; }
+  if (h->d_D) { cudaFree(h->d_D); h->d_D = nullptr; }
+  if (!h->d_N2 || h->mat_elems != nn) {
+    CHKM(dev_alloc(h, &h->d_N2, nn));
+    CHKM(dev_alloc(h, &h->d_D2, nn));
+    h->mat_elems = nn;
+  }
+  if (!h->d_alpha) CHKM(dev_alloc(h, &h->d_alpha, (size_t)N));
+  CHKM(dev_alloc(h, &h->d_alpha_part, (size_t)h->n_tiles * N));
+  CHKM(dev_alloc(h, &h->d_alpha_near, (size_t)N));
+  CHKM(dev_alloc(h, &h->d_alpha_sing, (size_t)N));
+  const int nq = q1 * q1;
+  const int RF = mixed_rec_floats(nq);
+  CHKM(dev_alloc(h, &h->d_rec32, (size_t)C * RF));
+  CHKM(dev_alloc(h, &h->d_cellgeo, (size_t)C * 4));
+  CHKM(dev_alloc(h, &h->d_rec, (size_t)C * nq * 8));
+  h->rec_cells = (size_t)C * nq;
+  EvTimer tm(h->stream);
+  CUM(launch_cell_records_fp64(C, h->d_X, h->d_cell_dofs, h->d_rec, q1, h->stream));
+  k_cell_records_mixed<<<(C + 127) / 128, 128, 0, h->stream>>>(
+      C, h->d_X, h->d_cell_dofs, h->d_rec32, reinterpret_cast<float4*>(h->d_cellgeo),
+      (float)o.near_field_ratio);
+  CUM(cudaGetLastError());
+  h->stats.t_geometry_ms = tm.ms();
+  const float4* geo = reinterpret_cast<const float4*>(h->d_cellgeo);
+  cudaError_t e;
+  switch (q1) {
+    case 2: e = launch_tile_mixed_t<2>(N, h->d_X, h->d_dnset, h->n_tiles, h->d_tile_ptr, h->d_tile_ent, h->d_cell_dofs, h->d_rec32, geo, h->d_N2, h->d_D2, h->d_alpha_part, h->d_err, h->stream); break;
+    case 3: e = launch_tile_mixed_t<3>(N, h->d_X, h->d_dnset, h->n_tiles, h->d_tile_ptr, h->d_tile_ent, h->d_cell_dofs, h->d_rec32, geo, h->d_N2, h->d_D2, h->d_alpha_part, h->d_err, h->stream); break;
+    case 4: e = launch_tile_mixed_t<4>(N, h->d_X, h->d_dnset, h->n_tiles, h->d_tile_ptr, h->d_tile_ent, h->d_cell_dofs, h->d_rec32, geo, h->d_N2, h->d_D2, h->d_alpha_part, h->d_err, h->stream); break;
+    case 5: e = launch_tile_mixed_t<5>(N, h->d_X, h->d_dnset, h->n_tiles, h->d_tile_ptr, h->d_tile_ent, h->d_cell_dofs, h->d_rec32, geo, h->d_N2, h->d_D2, h->d_alpha_part, h->d_err, h->stream); break;
+    default: e = launch_tile_mixed_t<6>(N, h->d_X, h->d_dnset, h->n_tiles, h->d_tile_ptr, h->d_tile_ent, h->d_cell_dofs, h->d_rec32, geo, h->d_N2, h->d_D2, h->d_alpha_part, h->d_err, h->stream); break;
+  }
+  CUM(e);
+  h->stats.t_assemble_ms = tm.ms();
+  k_near_mixed<<<(N + 127) / 128, 128, 0, h->stream>>>(N, C, h->d_X, h->d_dnset, h->d_cell_dofs,
+                                                        geo, h->d_rec, h->d_N2, h->d_D2,
+                                                        h->d_alpha_near);
+  CUM(cudaGetLastError());
+  k_singular_mixed<<<(N + 63) / 64, 64, 0, h->stream>>>(N, h->d_X, h->d_dnset, h->d_sptr,
+                                                         h->d_scell, h->d_cell_dofs, h->d_N2,
+                                                         h->d_D2, h->d_alpha_sing, h->d_err);
+  CUM(cudaGetLastError());
+  h->stats.t_singular_ms = tm.ms();
+  k_alpha_mixed<<<(N + 255) / 256, 256, 0, h->stream>>>(N, h->n_tiles, h->d_alpha_part,
+                                                         h->d_alpha_near, h->d_alpha_sing,
+                                                         h->d_alpha);
+  CUM(cudaGetLastError());
+  h->stats.t_alpha_ms = tm.ms();
+  h->launches += 6;
+  return check_device_error(h, "assemble (mixed)");
 }
-int factor_mixed(wbem_context* h) {
-  h->err = "mixed precision form not available";
-  return WBEM_ERR_ARG;
-}
-int solve_mixed(wbem_context* h, const double*, double*, int) {
-  h->err = "mixed precision form not available";
-  return WBEM_ERR_ARG;
-}
-void free_mixed(wbem_context*) {}
+
 }  // namespace wbem

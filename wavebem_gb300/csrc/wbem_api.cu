@@ -14,6 +14,7 @@
 #include <unordered_map>
 #include <vector>
 #include "context.h"
+#include "host_util.h"
 
 using namespace wbem;
 
@@ -32,33 +33,24 @@ int hull_force_dev(wbem_context* h, const int* hull_cells, int n_hull, const dou
 }  // namespace wbem
 
 // ------------------------------------------------------------------ errors
-static int fail(wbem_context* h, int code, const std::string& msg) {
-  if (h) h->err = msg;
-  return code;
-}
-
-#define CU(call)                                                                            \
-  do {                                                                                      \
-    cudaError_t e_ = (call);                                                                \
-    if (e_ != cudaSuccess)                                                                  \
-      return fail(h, e_ == cudaErrorMemoryAllocation ? WBEM_ERR_NOMEM : WBEM_ERR_CUDA,      \
-                  std::string(#call) + ": " + cudaGetErrorString(e_));                      \
-  } while (0)
-
-#define CHK(expr)               \
-  do {                          \
-    int s_ = (expr);            \
-    if (s_ != WBEM_OK) return s_; \
-  } while (0)
+#define CU WB_CU
+#define CHK WB_CHK
 
 namespace wbem {
+// Copies ordered on the handle's (non-blocking) stream, then waited for.
+static cudaError_t copy_sync(wbem_context* h, void* dst, const void* src, size_t bytes,
+                             cudaMemcpyKind kind) {
+  cudaError_t e = cudaMemcpyAsync(dst, src, bytes, kind, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  return e;
+}
 
 int check_device_error(wbem_context* h, const char* what) {
   cudaError_t e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess)
     return fail(h, WBEM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
   DevErr de;
-  e = cudaMemcpy(&de, h->d_err, sizeof(DevErr), cudaMemcpyDeviceToHost);
+  e = copy_sync(h, &de, h->d_err, sizeof(DevErr), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess)
     return fail(h, WBEM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
   if (de.code != 0) {
@@ -66,34 +58,11 @@ int check_device_error(wbem_context* h, const char* what) {
     snprintf(buf, sizeof buf, "%s: device error %d at site %d (%d, %d)", what, de.code, de.where,
              de.a, de.b);
     DevErr z{};
-    cudaMemcpy(h->d_err, &z, sizeof z, cudaMemcpyHostToDevice);
+    copy_sync(h, h->d_err, &z, sizeof z, cudaMemcpyHostToDevice);
     return fail(h, de.code, buf);
   }
   return WBEM_OK;
 }
-
-template <typename T>
-int dev_alloc(wbem_context* h, T** p, size_t n) {
-  if (*p) {
-    cudaFree(*p);
-    *p = nullptr;
-  }
-  if (n == 0) n = 1;
-  cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
-  if (e != cudaSuccess) {
-    *p = nullptr;
-    return fail(h, WBEM_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
-  }
-  return WBEM_OK;
-}
-
-template <typename T>
-int upload(wbem_context* h, T** p, const std::vector<T>& v) {
-  CHK(dev_alloc(h, p, v.size()));
-  if (!v.empty()) CU(cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
-  return WBEM_OK;
-}
-
 }  // namespace wbem
 
 // ------------------------------------------------------------ quadrature
@@ -828,6 +797,24 @@ int gmres_fp64(wbem_context* h, const double* rhs, double* x, int transpose) {
   return st;
 }
 
+int lu_apply(wbem_context* h, const double* v, double* z, int transpose);
+
+// GMRES iterative refinement in FP64 on the mixed-storage operator,
+// preconditioned by the FP32 LU factors (right preconditioning).
+int gmres_mixed_driver(wbem_context* h, const double* rhs, double* x, int transpose) {
+  auto op = [&](const double* a, double* b) {
+    return transpose ? apply_system_t(h, a, b) : apply_system(h, a, b);
+  };
+  auto prec = [&](const double* a, double* b) { return lu_apply(h, a, b, transpose); };
+  int it = 0;
+  double res = 0;
+  int st = gmres(h, rhs, x, h->opt.gmres_restart, h->opt.max_steps, h->opt.tolerance, op, prec,
+                 &it, &res);
+  h->stats.iterations = it;
+  h->stats.residual = res;
+  return st;
+}
+
 int build_block_jacobi(wbem_context* h) {
   const int nb = (h->N + kBJ - 1) / kBJ;
   CHK(dev_alloc(h, &h->d_binv, (size_t)nb * kBJ * kBJ));
@@ -1006,7 +993,7 @@ int wbem_update_nodes(wbem_handle h, const double* X) {
   std::vector<double> Xi((size_t)h->N * 3);
   for (int i = 0; i < h->N; ++i)
     for (int d = 0; d < 3; ++d) Xi[3 * (size_t)i + d] = X[3 * (size_t)h->perm[i] + d];
-  CU(cudaMemcpy(h->d_X, Xi.data(), Xi.size() * sizeof(double), cudaMemcpyHostToDevice));
+  CU(copy_sync(h, h->d_X, Xi.data(), Xi.size() * sizeof(double), cudaMemcpyHostToDevice));
   h->assembled_prec = -1;
   h->factors_valid = false;
   h->have_solution = false;
@@ -1142,7 +1129,7 @@ int wbem_solve_system(wbem_handle h, const double* tmp_rhs, double* phi, double*
   CHK(check_device_error(h, "wbem_solve_system"));
   // unpack (source/bem_problem.cc:869-879)
   std::vector<double> si(N);
-  CU(cudaMemcpy(si.data(), h->d_sol, sizeof(double) * N, cudaMemcpyDeviceToHost));
+  CU(copy_sync(h, si.data(), h->d_sol, sizeof(double) * N, cudaMemcpyDeviceToHost));
   for (int i = 0; i < N; ++i) {
     if (!std::isfinite(si[i])) return fail(h, WBEM_ERR_NONFINITE, "wbem_solve_system: non-finite solution");
     const int p = h->perm[i];
@@ -1166,7 +1153,7 @@ int wbem_get_alpha(wbem_handle h, double* alpha) {
   if (h->assembled_prec < 0) return fail(h, WBEM_ERR_STATE, "wbem_get_alpha: assemble first");
   cudaSetDevice(h->device);
   std::vector<double> a(h->N);
-  CU(cudaMemcpy(a.data(), h->d_alpha, sizeof(double) * h->N, cudaMemcpyDeviceToHost));
+  CU(copy_sync(h, a.data(), h->d_alpha, sizeof(double) * h->N, cudaMemcpyDeviceToHost));
   for (int i = 0; i < h->N; ++i) alpha[h->perm[i]] = a[i];
   return WBEM_OK;
 }
@@ -1211,12 +1198,12 @@ static int op_caller(wbem_handle h, int mode, const double* src, double* dst) {
   const int N = h->N;
   std::vector<double> xi(N), yi(N);
   for (int i = 0; i < N; ++i) xi[i] = src[h->perm[i]];
-  CU(cudaMemcpy(h->d_vec[3], xi.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+  CU(copy_sync(h, h->d_vec[3], xi.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
   if (h->assembled_prec == WBEM_PREC_FP64)
     CU(launch_matvec_fp64(N, mode, h->d_N, h->d_D, h->d_mask, h->d_alpha, h->d_vec[3], h->d_vec[4], h->stream));
   else
     CU(launch_matvec_mixed(N, mode, h->d_N2, h->d_D2, h->d_mask, h->d_alpha, h->d_vec[3], h->d_vec[4], h->stream));
-  CU(cudaMemcpy(yi.data(), h->d_vec[4], sizeof(double) * N, cudaMemcpyDeviceToHost));
+  CU(copy_sync(h, yi.data(), h->d_vec[4], sizeof(double) * N, cudaMemcpyDeviceToHost));
   for (int i = 0; i < N; ++i) dst[h->perm[i]] = yi[i];
   if (mode == 0) {
     // all-Neumann case of the reference: dst -= ||dst||_2 (source/bem_problem.cc:667-668)
@@ -1249,8 +1236,8 @@ int wbem_hull_force(wbem_handle h, const int* hull_cells, int n_hull, const doub
     pi[i] = phi[h->perm[i]];
     qi[i] = dphi_dn[h->perm[i]];
   }
-  CU(cudaMemcpy(h->d_vec[3], pi.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
-  CU(cudaMemcpy(h->d_vec[4], qi.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+  CU(copy_sync(h, h->d_vec[3], pi.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+  CU(copy_sync(h, h->d_vec[4], qi.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
   return hull_force_dev(h, hull_cells, n_hull, U, dir, h->d_vec[3], h->d_vec[4], force);
 }
 
