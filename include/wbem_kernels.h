@@ -19,6 +19,12 @@ extern "C" {
  * synchronizes. Returns a wbem.h status. */
 int wbem_test_gemm_bf16x3(int M, int Nc, int K, const float* dA, const float* dB, float* dC);
 
+/* Run all later work of the handle on the given cudaStream_t (NULL: back to
+ * a private non-blocking stream). Lets a caller order the library's kernels
+ * with its own work and time them with events on that stream. */
+struct wbem_context;
+int wbem_set_stream(struct wbem_context* h, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,7 +1,27 @@
-// Hull force evaluation and the adjoint of assemble + solve + force.
+// Hull force evaluation and the hand-written adjoint of
+// assemble_system + solve_system + hull force.
+//
+// With x the unknowns (phi on Neumann nodes, dphi/dn on Dirichlet nodes), b
+// the known data (tmp_rhs) and G(x, b, X) = 0 the constrained collocation
+// system, the force F(X, phi, dphi/dn) has
+//     dF/dX = dF/dX|direct - lambda^T dG/dX,     A^T lambda = dF/dx,
+//     dF/db = dF/db|direct - lambda^T dG/db.
+// Row i of the unconstrained system is (source/bem_problem.cc:620-706 with
+// alpha_i = -sum_j N_ij, :594-618)
+//     R_i = sum_panels sum_q w_q [ DL(x_q - x_i, c_q) (phi(q) - phi_i) - SL(x_q - x_i) |c_q| dphi(q) ]
+// with c_q the (unnormalised) cross product of the Q1 map, so lambda^T dR/dX
+// is obtained by recomputing every (row, panel, point) term with its
+// derivatives with respect to the collocation point and the 4 panel vertices
+// (k_adj_tile, k_adj_singular): no dG/dX is stored. The transposed solve
+// reuses the LU factors (mixed form) or the block-Jacobi blocks (FP64 form).
+// Constraint inhomogeneities are taken as functions of b only (exact for the
+// Dirichlet-Neumann and Neumann-Neumann double nodes of the tank meshes).
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <vector>
 #include "context.h"
+#include "host_util.h"
+#include "kernels.h"
 
 namespace wbem {
 cudaError_t upload_quadrature_force(const QuadTables& t);
@@ -12,54 +32,543 @@ cudaError_t upload_quadrature_adjoint(const QuadTables& t) {
   return upload_quadrature_force(t);
 }
 int ensure_vectors(wbem_context* h, int restart);
+int solve_mixed(wbem_context* h, const double* d_rhs, double* d_x, int transpose);
+int gmres_fp64(wbem_context* h, const double* rhs, double* x, int transpose);
 
-static int hull_dofs_upload(wbem_context* h, const int* hull_cells, int n_hull, int4** out) {
+constexpr double kI4P = 0.07957747154594766788;
+
+static int hull_dofs_upload(wbem_context* h, const int* hull_cells, int n_hull, int4** out,
+                            std::vector<int>* cell_ids = nullptr) {
   std::vector<int4> hd(n_hull > 0 ? n_hull : 1);
   for (int k = 0; k < n_hull; ++k) {
     const int c = hull_cells[k];
-    if (c < 0 || c >= h->C) {
-      h->err = "hull cell index out of range";
-      return WBEM_ERR_ARG;
-    }
+    if (c < 0 || c >= h->C) return fail(h, WBEM_ERR_ARG, "hull cell index out of range");
     const int* v = &h->cells[4 * (size_t)c];
     hd[k] = make_int4(h->iperm[v[0]], h->iperm[v[1]], h->iperm[v[2]], h->iperm[v[3]]);
+    if (cell_ids) cell_ids->push_back(c);
   }
-  if (cudaMalloc(out, sizeof(int4) * hd.size()) != cudaSuccess) {
-    h->err = "cudaMalloc failed";
-    return WBEM_ERR_NOMEM;
-  }
-  cudaMemcpyAsync(*out, hd.data(), sizeof(int4) * hd.size(), cudaMemcpyHostToDevice, h->stream);
-  cudaStreamSynchronize(h->stream);
+  WB_CU(cudaMalloc(out, sizeof(int4) * hd.size()));
+  WB_CU(cudaMemcpyAsync(*out, hd.data(), sizeof(int4) * hd.size(), cudaMemcpyHostToDevice, h->stream));
+  WB_CU(cudaStreamSynchronize(h->stream));
   return WBEM_OK;
 }
 
 int hull_force_dev(wbem_context* h, const int* hull_cells, int n_hull, const double* U, int dir,
                    const double* d_phi, const double* d_dphi, double* force) {
   int4* hd = nullptr;
-  int st = hull_dofs_upload(h, hull_cells, n_hull, &hd);
-  if (st) return st;
+  WB_CHK(hull_dofs_upload(h, hull_cells, n_hull, &hd));
   double* part = nullptr;
-  if (cudaMalloc(&part, sizeof(double) * (n_hull + 1)) != cudaSuccess) {
-    cudaFree(hd);
-    h->err = "cudaMalloc failed";
-    return WBEM_ERR_NOMEM;
-  }
-  cudaError_t e = launch_hull_force(n_hull, hd, h->d_X, U, dir, d_phi, d_dphi, part, h->stream);
+  cudaError_t e = cudaMalloc(&part, sizeof(double) * (n_hull + 1));
+  if (e == cudaSuccess) e = launch_hull_force(n_hull, hd, h->d_X, U, dir, d_phi, d_dphi, part, h->stream);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(force, part + n_hull, sizeof(double), cudaMemcpyDeviceToHost, h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-  cudaFree(part);
+  if (part) cudaFree(part);
   cudaFree(hd);
-  if (e != cudaSuccess) {
-    h->err = cudaGetErrorString(e);
-    return WBEM_ERR_CUDA;
-  }
+  if (e != cudaSuccess) return fail(h, WBEM_ERR_CUDA, cudaGetErrorString(e));
   return WBEM_OK;
 }
 
-int adjoint_force(wbem_context* h, const int*, int, const double*, int, const double*, double*,
-                  double*) {
-  h->err = "adjoint not available";
-  return WBEM_ERR_ARG;
+// ------------------------------------------------------------ K7: panel terms
+__device__ __forceinline__ bool near_test_a(float xi, float yi, float zi, float4 g) {
+  const float dx = __fsub_rn(g.x, xi), dy = __fsub_rn(g.y, yi), dz = __fsub_rn(g.z, zi);
+  const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+  return d2 < g.w;
 }
+
+// Derivatives of f = w' lam [ -(R.c)/r^3 dphi - |c|/r dn ] (w' = w/(4 pi)):
+//   df/dR = -s1 c / r^3 + (3 s1 (R.c) / r^5 + s2 |c| / r^3) R
+//   df/dc = -s1 R / r^3 - (s2 / (|c| r)) c
+// with s1 = w' lam dphi, s2 = w' lam dn.
+template <typename T>
+__device__ __forceinline__ void point_grad(const T R[3], const T c[3], T J, T s1, T s2, T aR[3],
+                                           T ac[3]) {
+  const T r2 = R[0] * R[0] + R[1] * R[1] + R[2] * R[2];
+  T ri;
+  if constexpr (sizeof(T) == 8) ri = rsqrt(r2);
+  else ri = rsqrtf(r2);
+  const T ri3 = ri * ri * ri;
+  const T ri5 = ri3 * ri * ri;
+  const T u = R[0] * c[0] + R[1] * c[1] + R[2] * c[2];
+  const T kr = 3 * s1 * u * ri5 + s2 * J * ri3;
+  const T kc = s2 * ri / J;
+  for (int d = 0; d < 3; ++d) {
+    aR[d] = -s1 * ri3 * c[d] + kr * R[d];
+    ac[d] = -s1 * ri3 * R[d] - kc * c[d];
+  }
+}
+
+// smem point data per panel and point: x (3), jx (3), je (3), |c|, w'phi(q), w'dn(q)
+constexpr int kAdjChunk = 8;
+constexpr int kPt = 12;
+
+// One CTA: 128 rows x a chunk of panels. FP64 everywhere when MIXED == false;
+// otherwise FP32 for panels that fail the near test and FP64 for the rest.
+template <int Q1, bool MIXED>
+__global__ void __launch_bounds__(128)
+    k_adj_tile(int N, int C, const double* __restrict__ X, const int* __restrict__ dnset,
+               const int4* __restrict__ cell_dofs, const float4* __restrict__ cellgeo,
+               const double* __restrict__ lam, const double* __restrict__ phi,
+               const double* __restrict__ dn, double* __restrict__ grow_part,
+               double* __restrict__ gcell_part, int cells_per_block) {
+  constexpr int NQ = Q1 * Q1;
+  __shared__ double pt[kAdjChunk][NQ][kPt];
+  __shared__ float ptf[kAdjChunk][NQ][kPt];
+  __shared__ double wred[4][kAdjChunk][12];
+  __shared__ double cT[3];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int row = blockIdx.y * 128 + tid;
+  const bool active = row < N;
+  if (tid == 0) {
+    const int r0 = blockIdx.y * 128;
+    for (int d = 0; d < 3; ++d) cT[d] = X[3 * (size_t)r0 + d];
+  }
+  double xi[3] = {0, 0, 0}, li = 0, phii = 0;
+  int set[kMaxSet];
+  for (int k = 0; k < kMaxSet; ++k) set[k] = -2;
+  if (active) {
+    for (int d = 0; d < 3; ++d) xi[d] = X[3 * (size_t)row + d];
+    li = lam[row];
+    phii = phi[row];
+    for (int k = 0; k < kMaxSet; ++k) set[k] = dnset[(size_t)row * kMaxSet + k];
+  }
+  __syncthreads();
+  const float xf = (float)xi[0], yf = (float)xi[1], zf = (float)xi[2];
+  const float xr[3] = {(float)(xi[0] - cT[0]), (float)(xi[1] - cT[1]), (float)(xi[2] - cT[2])};
+  double grow[3] = {0, 0, 0};
+  const int c_begin = blockIdx.x * cells_per_block;
+  const int c_end = min(C, c_begin + cells_per_block);
+  for (int cb = c_begin; cb < c_end; cb += kAdjChunk) {
+    const int cnt = min(kAdjChunk, c_end - cb);
+    __syncthreads();
+    // point data of the chunk
+    for (int t = tid; t < cnt * NQ; t += 128) {
+      const int k = t / NQ, q = t % NQ;
+      const int4 d = cell_dofs[cb + k];
+      const int id[4] = {d.x, d.y, d.z, d.w};
+      const double s = c_qa.gp[q][0], u = c_qa.gp[q][1], w = c_qa.gp[q][2] * kI4P;
+      const double Ns[4] = {-(1 - u), (1 - u), -u, u};
+      const double Nt[4] = {-(1 - s), -s, (1 - s), s};
+      double x[3] = {0, 0, 0}, jx[3] = {0, 0, 0}, je[3] = {0, 0, 0}, fp = 0, fn = 0;
+      for (int v = 0; v < 4; ++v) {
+        const double nv = c_qa.phi[q][v];
+        for (int e = 0; e < 3; ++e) {
+          const double P = X[3 * (size_t)id[v] + e];
+          x[e] += nv * P;
+          jx[e] += Ns[v] * P;
+          je[e] += Nt[v] * P;
+        }
+        fp += nv * phi[id[v]];
+        fn += nv * dn[id[v]];
+      }
+      double* p = pt[k][q];
+      float* pf = ptf[k][q];
+      for (int e = 0; e < 3; ++e) {
+        p[e] = x[e];
+        p[3 + e] = jx[e];
+        p[6 + e] = je[e];
+        pf[e] = (float)(x[e] - cT[e]);
+        pf[3 + e] = (float)jx[e];
+        pf[6 + e] = (float)je[e];
+      }
+      const double cr0 = jx[1] * je[2] - jx[2] * je[1], cr1 = jx[2] * je[0] - jx[0] * je[2],
+                   cr2 = jx[0] * je[1] - jx[1] * je[0];
+      p[9] = sqrt(cr0 * cr0 + cr1 * cr1 + cr2 * cr2);
+      p[10] = w * fp;
+      p[11] = w * fn;
+      pf[9] = (float)p[9];
+      pf[10] = (float)p[10];
+      pf[11] = (float)p[11];
+    }
+    __syncthreads();
+    for (int k = 0; k < cnt; ++k) {
+      const int cell = cb + k;
+      const int4 d = cell_dofs[cell];
+      bool sing = false;
+      for (int s = 0; s < kMaxSet; ++s)
+        sing |= (set[s] == d.x) | (set[s] == d.y) | (set[s] == d.z) | (set[s] == d.w);
+      double g[12];
+      for (int t = 0; t < 12; ++t) g[t] = 0;
+      if (active && !sing && li != 0.0) {
+        const bool use64 = !MIXED || near_test_a(xf, yf, zf, cellgeo[cell]);
+        if (use64) {
+          for (int q = 0; q < NQ; ++q) {
+            const double* p = pt[k][q];
+            const double R[3] = {p[0] - xi[0], p[1] - xi[1], p[2] - xi[2]};
+            const double c[3] = {p[4] * p[8] - p[5] * p[7], p[5] * p[6] - p[3] * p[8],
+                                 p[3] * p[7] - p[4] * p[6]};
+            const double w = c_qa.gp[q][2] * kI4P;
+            const double s1 = li * (p[10] - w * phii), s2 = li * p[11];
+            double aR[3], ac[3];
+            point_grad<double>(R, c, p[9], s1, s2, aR, ac);
+            const double s = c_qa.gp[q][0], u = c_qa.gp[q][1];
+            const double Ns[4] = {-(1 - u), (1 - u), -u, u};
+            const double Nt[4] = {-(1 - s), -s, (1 - s), s};
+            const double gjx[3] = {p[7] * ac[2] - p[8] * ac[1], p[8] * ac[0] - p[6] * ac[2],
+                                   p[6] * ac[1] - p[7] * ac[0]};
+            const double gje[3] = {ac[1] * p[5] - ac[2] * p[4], ac[2] * p[3] - ac[0] * p[5],
+                                   ac[0] * p[4] - ac[1] * p[3]};
+            for (int e = 0; e < 3; ++e) grow[e] -= aR[e];
+            for (int v = 0; v < 4; ++v)
+              for (int e = 0; e < 3; ++e)
+                g[3 * v + e] += c_qa.phi[q][v] * aR[e] + Ns[v] * gjx[e] + Nt[v] * gje[e];
+          }
+        } else {
+          float gf[12];
+          for (int t = 0; t < 12; ++t) gf[t] = 0.f;
+          float grf[3] = {0.f, 0.f, 0.f};
+          const float lif = (float)li, phif = (float)phii;
+#pragma unroll 4
+          for (int q = 0; q < NQ; ++q) {
+            const float* p = ptf[k][q];
+            const float R[3] = {p[0] - xr[0], p[1] - xr[1], p[2] - xr[2]};
+            const float jx[3] = {p[3], p[4], p[5]};
+            const float je[3] = {p[6], p[7], p[8]};
+            const float c[3] = {jx[1] * je[2] - jx[2] * je[1], jx[2] * je[0] - jx[0] * je[2],
+                                jx[0] * je[1] - jx[1] * je[0]};
+            const float w = c_qa.gpf[q][2] * (float)kI4P;
+            const float s1 = lif * (p[10] - w * phif), s2 = lif * p[11];
+            float aR[3], ac[3];
+            point_grad<float>(R, c, p[9], s1, s2, aR, ac);
+            const float s = c_qa.gpf[q][0], u = c_qa.gpf[q][1];
+            const float Ns[4] = {-(1 - u), (1 - u), -u, u};
+            const float Nt[4] = {-(1 - s), -s, (1 - s), s};
+            const float gjx[3] = {je[1] * ac[2] - je[2] * ac[1], je[2] * ac[0] - je[0] * ac[2],
+                                  je[0] * ac[1] - je[1] * ac[0]};
+            const float gje[3] = {ac[1] * jx[2] - ac[2] * jx[1], ac[2] * jx[0] - ac[0] * jx[2],
+                                  ac[0] * jx[1] - ac[1] * jx[0]};
+            for (int e = 0; e < 3; ++e) grf[e] -= aR[e];
+            for (int v = 0; v < 4; ++v) {
+              const float nv = c_qa.phif[q][v];
+              for (int e = 0; e < 3; ++e)
+                gf[3 * v + e] += nv * aR[e] + Ns[v] * gjx[e] + Nt[v] * gje[e];
+            }
+          }
+          for (int e = 0; e < 3; ++e) grow[e] += grf[e];
+          for (int t = 0; t < 12; ++t) g[t] = gf[t];
+        }
+      }
+      // sum the 12 panel-vertex terms over the 32 rows of the warp
+      for (int t = 0; t < 12; ++t) {
+        double v = g[t];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) wred[warp][k][t] = v;
+      }
+    }
+    __syncthreads();
+    for (int t = tid; t < cnt * 12; t += 128) {
+      const int k = t / 12, e = t % 12;
+      const double v = wred[0][k][e] + wred[1][k][e] + wred[2][k][e] + wred[3][k][e];
+      gcell_part[((size_t)blockIdx.y * C + cb + k) * 12 + e] = v;
+    }
+  }
+  if (active)
+    for (int e = 0; e < 3; ++e) grow_part[((size_t)blockIdx.x * N + row) * 3 + e] = grow[e];
+}
+
+// Singular panels of each row (FP64, vertex rule): row part into grow_sing,
+// panel-vertex part per (row, panel) pair into gpair[e][12].
+__global__ void k_adj_singular(int N, const double* __restrict__ X, const int* __restrict__ dnset,
+                               const int* __restrict__ sptr, const int* __restrict__ scell,
+                               const int4* __restrict__ cell_dofs, const double* __restrict__ lam,
+                               const double* __restrict__ phi, const double* __restrict__ dn,
+                               double* __restrict__ grow_sing, double* __restrict__ gpair) {
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= N) return;
+  double xi[3];
+  for (int d = 0; d < 3; ++d) xi[d] = X[3 * (size_t)row + d];
+  const double li = lam[row], phii = phi[row];
+  int set[kMaxSet];
+  for (int k = 0; k < kMaxSet; ++k) set[k] = dnset[(size_t)row * kMaxSet + k];
+  double grow[3] = {0, 0, 0};
+  for (int e = sptr[row]; e < sptr[row + 1]; ++e) {
+    const int cell = scell[e];
+    const int4 d = cell_dofs[cell];
+    const int id[4] = {d.x, d.y, d.z, d.w};
+    int v = -1;
+    for (int j = 0; j < 4 && v < 0; ++j)
+      for (int s = 0; s < kMaxSet; ++s)
+        if (set[s] == id[j]) v = j;
+    double g[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    if (v >= 0 && li != 0.0) {
+      double P[4][3], ph[4], pn[4];
+      for (int k = 0; k < 4; ++k) {
+        for (int c = 0; c < 3; ++c) P[k][c] = X[3 * (size_t)id[k] + c];
+        ph[k] = phi[id[k]];
+        pn[k] = dn[id[k]];
+      }
+      for (int q = 0; q < c_qa.nsp; ++q) {
+        const double s = c_qa.sp[v][q][0], u = c_qa.sp[v][q][1], w = c_qa.sp[v][q][2] * kI4P;
+        const double N4[4] = {(1 - s) * (1 - u), s * (1 - u), (1 - s) * u, s * u};
+        const double Ns[4] = {-(1 - u), (1 - u), -u, u};
+        const double Nt[4] = {-(1 - s), -s, (1 - s), s};
+        double x[3] = {0, 0, 0}, jx[3] = {0, 0, 0}, je[3] = {0, 0, 0}, fp = 0, fn = 0;
+        for (int k = 0; k < 4; ++k) {
+          for (int c = 0; c < 3; ++c) {
+            x[c] += N4[k] * P[k][c];
+            jx[c] += Ns[k] * P[k][c];
+            je[c] += Nt[k] * P[k][c];
+          }
+          fp += N4[k] * ph[k];
+          fn += N4[k] * pn[k];
+        }
+        const double R[3] = {x[0] - xi[0], x[1] - xi[1], x[2] - xi[2]};
+        const double c[3] = {jx[1] * je[2] - jx[2] * je[1], jx[2] * je[0] - jx[0] * je[2],
+                             jx[0] * je[1] - jx[1] * je[0]};
+        const double J = sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+        double aR[3], ac[3];
+        point_grad<double>(R, c, J, w * li * (fp - phii), w * li * fn, aR, ac);
+        const double gjx[3] = {je[1] * ac[2] - je[2] * ac[1], je[2] * ac[0] - je[0] * ac[2],
+                               je[0] * ac[1] - je[1] * ac[0]};
+        const double gje[3] = {ac[1] * jx[2] - ac[2] * jx[1], ac[2] * jx[0] - ac[0] * jx[2],
+                               ac[0] * jx[1] - ac[1] * jx[0]};
+        for (int c2 = 0; c2 < 3; ++c2) grow[c2] -= aR[c2];
+        for (int k = 0; k < 4; ++k)
+          for (int c2 = 0; c2 < 3; ++c2) g[3 * k + c2] += N4[k] * aR[c2] + Ns[k] * gjx[c2] + Nt[k] * gje[c2];
+      }
+    }
+    for (int t = 0; t < 12; ++t) gpair[(size_t)e * 12 + t] = g[t];
+  }
+  for (int c = 0; c < 3; ++c) grow_sing[3 * (size_t)row + c] = grow[c];
+}
+
+// lambda^T dG/dX per node (deterministic sums), minus, plus the direct force
+// term of the hull panels:  out[p] = gdirect[p] - (row terms + panel-vertex terms).
+__global__ void k_adj_reduce(int N, int C, int n_cb, int n_rb, const double* __restrict__ grow_part,
+                             const double* __restrict__ grow_sing, const double* __restrict__ gcell_part,
+                             const double* __restrict__ gpair, const int* __restrict__ cpair_ptr,
+                             const int* __restrict__ cpair_idx, const int* __restrict__ ncptr,
+                             const int* __restrict__ ncent, const int* __restrict__ hull_of_cell,
+                             const double* __restrict__ ghull, double* __restrict__ out) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= N) return;
+  double s[3] = {0, 0, 0}, dir[3] = {0, 0, 0};
+  for (int b = 0; b < n_cb; ++b)
+    for (int e = 0; e < 3; ++e) s[e] += grow_part[((size_t)b * N + p) * 3 + e];
+  for (int e = 0; e < 3; ++e) s[e] += grow_sing[3 * (size_t)p + e];
+  for (int t = ncptr[p]; t < ncptr[p + 1]; ++t) {
+    const int cell = ncent[t] >> 2, v = ncent[t] & 3;
+    for (int b = 0; b < n_rb; ++b)
+      for (int e = 0; e < 3; ++e) s[e] += gcell_part[((size_t)b * C + cell) * 12 + 3 * v + e];
+    for (int k = cpair_ptr[cell]; k < cpair_ptr[cell + 1]; ++k)
+      for (int e = 0; e < 3; ++e) s[e] += gpair[(size_t)cpair_idx[k] * 12 + 3 * v + e];
+    const int hc = hull_of_cell[cell];
+    if (hc >= 0)
+      for (int e = 0; e < 3; ++e) dir[e] += ghull[(size_t)hc * 12 + 3 * v + e];
+  }
+  for (int e = 0; e < 3; ++e) out[3 * (size_t)p + e] = dir[e] - s[e];
+}
+
+// direct force derivatives with respect to nodal phi / dphi_dn (per node)
+__global__ void k_hull_node_sum(int N, const int* __restrict__ ncptr, const int* __restrict__ ncent,
+                                const int* __restrict__ hull_of_cell, const double* __restrict__ gph,
+                                const double* __restrict__ gpn, double* __restrict__ out_ph,
+                                double* __restrict__ out_pn) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= N) return;
+  double a = 0, b = 0;
+  for (int t = ncptr[p]; t < ncptr[p + 1]; ++t) {
+    const int hc = hull_of_cell[ncent[t] >> 2];
+    if (hc >= 0) {
+      a += gph[(size_t)hc * 4 + (ncent[t] & 3)];
+      b += gpn[(size_t)hc * 4 + (ncent[t] & 3)];
+    }
+  }
+  out_ph[p] = a;
+  out_pn[p] = b;
+}
+
+// g_x = o * dF/dphi + s * dF/ddn ; fields phi / dn from sol and b
+__global__ void k_fields(int N, const uint8_t* __restrict__ mask, const double* __restrict__ sol,
+                         const double* __restrict__ b, double* __restrict__ phi,
+                         double* __restrict__ dn) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  if (mask[i]) {
+    phi[i] = b[i];
+    dn[i] = sol[i];
+  } else {
+    phi[i] = sol[i];
+    dn[i] = b[i];
+  }
+}
+__global__ void k_gx(int N, const uint8_t* __restrict__ mask, const double* __restrict__ gph,
+                     const double* __restrict__ gpn, double* __restrict__ gx) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  gx[i] = mask[i] ? gpn[i] : gph[i];
+}
+// dF/db = s*gph + o*gpn + B^T lam_u - alpha s lam_u  (B^T lam_u given in bt)
+__global__ void k_gb(int N, const uint8_t* __restrict__ mask, const double* __restrict__ gph,
+                     const double* __restrict__ gpn, const double* __restrict__ bt,
+                     const double* __restrict__ alpha, const double* __restrict__ lamu,
+                     double* __restrict__ gb) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  double v = (mask[i] ? gph[i] : gpn[i]) + bt[i];
+  if (mask[i]) v -= alpha[i] * lamu[i];
+  gb[i] = v;
+}
+
+template <int Q1, bool MIXED>
+static cudaError_t launch_adj_tile_t(int N, int C, const double* X, const int* dnset,
+                                     const int4* cd, const float4* geo, const double* lam,
+                                     const double* phi, const double* dn, double* grow_part,
+                                     double* gcell_part, int cpb, cudaStream_t s) {
+  dim3 grid((C + cpb - 1) / cpb, (N + 127) / 128);
+  k_adj_tile<Q1, MIXED><<<grid, 128, 0, s>>>(N, C, X, dnset, cd, geo, lam, phi, dn, grow_part,
+                                             gcell_part, cpb);
+  return cudaGetLastError();
+}
+
+int adjoint_force(wbem_context* h, const int* hull_cells, int n_hull, const double* U, int dir,
+                  const double* tmp_rhs, double* dF_dX, double* dF_drhs) {
+  const int N = h->N, C = h->C;
+  const int q1 = h->opt.quadrature_order;
+  if (q1 < 2 || q1 > 6) return fail(h, WBEM_ERR_ARG, "adjoint supports quadrature orders 2..6");
+  const bool mixed = h->assembled_prec == WBEM_PREC_MIXED;
+  WB_CHK(ensure_vectors(h, h->opt.gmres_restart));
+  EvTimer tm(h->stream);
+  // hull panel data
+  std::vector<int> hull_ids;
+  int4* hd = nullptr;
+  WB_CHK(hull_dofs_upload(h, hull_cells, n_hull, &hd, &hull_ids));
+  std::vector<int> hoc(C, -1);
+  for (int k = 0; k < n_hull; ++k) hoc[hull_ids[k]] = k;
+  int* d_hoc = nullptr;
+  double *d_ghull = nullptr, *d_gph = nullptr, *d_gpn = nullptr;
+  const int cpb = 64;
+  const int n_cb = (C + cpb - 1) / cpb, n_rb = (N + 127) / 128;
+  double *grow_part = nullptr, *gcell_part = nullptr, *grow_sing = nullptr, *gpair = nullptr;
+  int *d_cpptr = nullptr, *d_cpidx = nullptr;
+  double* d_out = nullptr;
+  double* d_nph = nullptr;
+  int st = WBEM_OK;
+  // cell -> singular pair index lists (inverse of the per-row singular lists)
+  std::vector<int> sptr(N + 1), scell;
+  WB_CU(cudaMemcpyAsync(sptr.data(), h->d_sptr, sizeof(int) * (N + 1), cudaMemcpyDeviceToHost, h->stream));
+  WB_CU(cudaStreamSynchronize(h->stream));
+  scell.resize(sptr[N]);
+  if (sptr[N] > 0)
+    WB_CU(cudaMemcpyAsync(scell.data(), h->d_scell, sizeof(int) * sptr[N], cudaMemcpyDeviceToHost, h->stream));
+  WB_CU(cudaStreamSynchronize(h->stream));
+  std::vector<int> cpptr(C + 1, 0), cpidx(scell.size());
+  for (int c : scell) cpptr[c + 1]++;
+  for (int c = 0; c < C; ++c) cpptr[c + 1] += cpptr[c];
+  {
+    std::vector<int> fill(cpptr.begin(), cpptr.end() - 1);
+    for (int e = 0; e < (int)scell.size(); ++e) cpidx[fill[scell[e]]++] = e;
+  }
+  do {
+    if ((st = upload(h, &d_hoc, hoc)) != WBEM_OK) break;
+    if ((st = upload(h, &d_cpptr, cpptr)) != WBEM_OK) break;
+    if ((st = upload(h, &d_cpidx, cpidx)) != WBEM_OK) break;
+    if ((st = dev_alloc(h, &d_ghull, (size_t)std::max(1, n_hull) * 12)) != WBEM_OK) break;
+    if ((st = dev_alloc(h, &d_gph, (size_t)std::max(1, n_hull) * 4)) != WBEM_OK) break;
+    if ((st = dev_alloc(h, &d_gpn, (size_t)std::max(1, n_hull) * 4)) != WBEM_OK) break;
+    if ((st = dev_alloc(h, &grow_part, (size_t)n_cb * N * 3)) != WBEM_OK) break;
+    if ((st = dev_alloc(h, &gcell_part, (size_t)n_rb * C * 12)) != WBEM_OK) break;
+    if ((st = dev_alloc(h, &grow_sing, (size_t)N * 3)) != WBEM_OK) break;
+    if ((st = dev_alloc(h, &gpair, (size_t)std::max<size_t>(1, scell.size()) * 12)) != WBEM_OK) break;
+    if ((st = dev_alloc(h, &d_out, (size_t)N * 3)) != WBEM_OK) break;
+    if ((st = dev_alloc(h, &d_nph, (size_t)N * 2)) != WBEM_OK) break;
+    double* phi = h->d_vec[3];
+    double* dn = h->d_vec[4];
+    double* gx = h->d_vec[5];
+    double* lam = h->d_vec[6];
+    double* nph = d_nph;  // per-node dF/dphi, dF/ddn
+    double* npn = d_nph + N;
+    const int bs = 256, nb = (N + bs - 1) / bs;
+    // fields and direct force derivatives
+    k_fields<<<nb, bs, 0, h->stream>>>(N, h->d_mask, h->d_sol, h->d_b, phi, dn);
+    WB_CU(launch_hull_force_grad(n_hull, hd, h->d_X, U, dir, phi, dn, d_ghull, d_gph, d_gpn, h->stream));
+    k_hull_node_sum<<<nb, bs, 0, h->stream>>>(N, h->d_ncptr, h->d_ncent, d_hoc, d_gph, d_gpn, nph, npn);
+    k_gx<<<nb, bs, 0, h->stream>>>(N, h->d_mask, nph, npn, gx);
+    WB_CU(cudaGetLastError());
+    // transposed solve A^T lambda = g_x (constrained operator)
+    st = mixed ? solve_mixed(h, gx, lam, 1) : gmres_fp64(h, gx, lam, 1);
+    if (st != WBEM_OK) break;
+    // lam_u: constrained rows take no part in dG/dX; keep lam for the b-terms
+    double* lamu = h->d_vec[2];
+    WB_CU(cudaMemcpyAsync(lamu, lam, sizeof(double) * N, cudaMemcpyDeviceToDevice, h->stream));
+    if (h->n_crows) {
+      WB_CU(cudaMemsetAsync(d_out, 0, sizeof(double) * h->n_crows, h->stream));
+      WB_CU(launch_set_rows(h->n_crows, h->d_crow, d_out, lamu, h->stream));
+    }
+    // K7: recompute the panel terms with their derivatives
+    const float4* geo = reinterpret_cast<const float4*>(h->d_cellgeo);
+    cudaError_t e;
+    if (mixed) {
+      switch (q1) {
+        case 2: e = launch_adj_tile_t<2, true>(N, C, h->d_X, h->d_dnset, h->d_cell_dofs, geo, lamu, phi, dn, grow_part, gcell_part, cpb, h->stream); break;
+        case 3: e = launch_adj_tile_t<3, true>(N, C, h->d_X, h->d_dnset, h->d_cell_dofs, geo, lamu, phi, dn, grow_part, gcell_part, cpb, h->stream); break;
+        case 4: e = launch_adj_tile_t<4, true>(N, C, h->d_X, h->d_dnset, h->d_cell_dofs, geo, lamu, phi, dn, grow_part, gcell_part, cpb, h->stream); break;
+        case 5: e = launch_adj_tile_t<5, true>(N, C, h->d_X, h->d_dnset, h->d_cell_dofs, geo, lamu, phi, dn, grow_part, gcell_part, cpb, h->stream); break;
+        default: e = launch_adj_tile_t<6, true>(N, C, h->d_X, h->d_dnset, h->d_cell_dofs, geo, lamu, phi, dn, grow_part, gcell_part, cpb, h->stream); break;
+      }
+    } else {
+      switch (q1) {
+        case 2: e = launch_adj_tile_t<2, false>(N, C, h->d_X, h->d_dnset, h->d_cell_dofs, geo, lamu, phi, dn, grow_part, gcell_part, cpb, h->stream); break;
+        case 3: e = launch_adj_tile_t<3, false>(N, C, h->d_X, h->d_dnset, h->d_cell_dofs, geo, lamu, phi, dn, grow_part, gcell_part, cpb, h->stream); break;
+        case 4: e = launch_adj_tile_t<4, false>(N, C, h->d_X, h->d_dnset, h->d_cell_dofs, geo, lamu, phi, dn, grow_part, gcell_part, cpb, h->stream); break;
+        case 5: e = launch_adj_tile_t<5, false>(N, C, h->d_X, h->d_dnset, h->d_cell_dofs, geo, lamu, phi, dn, grow_part, gcell_part, cpb, h->stream); break;
+        default: e = launch_adj_tile_t<6, false>(N, C, h->d_X, h->d_dnset, h->d_cell_dofs, geo, lamu, phi, dn, grow_part, gcell_part, cpb, h->stream); break;
+      }
+    }
+    WB_CU(e);
+    k_adj_singular<<<(N + 63) / 64, 64, 0, h->stream>>>(N, h->d_X, h->d_dnset, h->d_sptr, h->d_scell,
+                                                        h->d_cell_dofs, lamu, phi, dn, grow_sing, gpair);
+    k_adj_reduce<<<nb, bs, 0, h->stream>>>(N, C, n_cb, n_rb, grow_part, grow_sing, gcell_part, gpair,
+                                           d_cpptr, d_cpidx, h->d_ncptr, h->d_ncent, d_hoc, d_ghull,
+                                           d_out);
+    WB_CU(cudaGetLastError());
+    // dF/db: complementary transposed operator B^T lam_u (B = mask ? -N : D, no alpha)
+    double* bt = h->d_vec[7];
+    double* part = h->d_part + 256 * 128;
+    if (mixed)
+      WB_CU(launch_matvec_t_mixed(N, h->d_D2, h->d_N2, h->d_mask, nullptr, lamu, bt, part, h->stream));
+    else
+      WB_CU(launch_matvec_t_fp64(N, h->d_D, h->d_N, h->d_mask, nullptr, lamu, bt, part, h->stream));
+    double* gb = h->d_vec[0];
+    k_gb<<<nb, bs, 0, h->stream>>>(N, h->d_mask, nph, npn, bt, h->d_alpha, lamu, gb);
+    WB_CU(cudaGetLastError());
+    h->launches += 12;
+    WB_CHK(check_device_error(h, "adjoint"));
+    // back to the caller's order; constraint inhomogeneities tied to b
+    std::vector<double> gXi(3 * (size_t)N), gbi(N), li(N);
+    WB_CU(cudaMemcpyAsync(gXi.data(), d_out, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, h->stream));
+    WB_CU(cudaMemcpyAsync(gbi.data(), gb, sizeof(double) * N, cudaMemcpyDeviceToHost, h->stream));
+    WB_CU(cudaMemcpyAsync(li.data(), lam, sizeof(double) * N, cudaMemcpyDeviceToHost, h->stream));
+    WB_CU(cudaStreamSynchronize(h->stream));
+    for (int i = 0; i < N; ++i) {
+      const int p = h->perm[i];
+      for (int d = 0; d < 3; ++d) dF_dX[3 * (size_t)p + d] = gXi[3 * (size_t)i + d];
+      dF_drhs[p] = gbi[i];
+    }
+    // Dirichlet-Neumann lines x_m = b_first: -lambda_m * d(-b_first)/db = +lambda_m
+    const auto& P = h->dn_ptr;
+    const auto& I = h->dn_idx;
+    for (int i = 0; i < N; ++i) {
+      int first = I[P[i]];
+      for (int k = P[i]; k < P[i + 1]; ++k)
+        if (h->mask[I[k]]) {
+          first = I[k];
+          break;
+        }
+      if (i != first || !h->mask[i]) continue;
+      for (int k = P[i]; k < P[i + 1]; ++k) {
+        const int o = I[k];
+        if (o != i && !h->mask[o]) dF_drhs[i] += li[h->iperm[o]];
+      }
+    }
+    (void)tmp_rhs;
+    h->stats.t_adjoint_ms = tm.ms();
+  } while (0);
+  void* fr[] = {hd, d_hoc, d_ghull, d_gph, d_gpn, grow_part, gcell_part, grow_sing, gpair,
+                d_cpptr, d_cpidx, d_out, d_nph};
+  for (void* p : fr)
+    if (p) cudaFree(p);
+  return st;
+}
+
 }  // namespace wbem

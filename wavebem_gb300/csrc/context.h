@@ -10,6 +10,7 @@
 struct wbem_context {
   int device = 0;
   cudaStream_t stream = nullptr;
+  bool own_stream = false;
   std::string err;
   wbem_stats stats{};
   wbem_options opt{};
@@ -96,4 +97,5 @@ struct wbem_context {
 
   wbem::DevErr* d_err = nullptr;
   int launches = 0;
+  void* lu_state = nullptr;  // mixed LU workspaces (lu.cu)
 };

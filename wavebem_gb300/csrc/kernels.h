@@ -22,6 +22,8 @@ struct QuadTables {
   double gp[kMaxQ1 * kMaxQ1][3];     // regular rule: xi, eta, w
   double phi[kMaxQ1 * kMaxQ1][4];    // shape values at the regular points
   double sp[4][kMaxSingular][3];     // singular rules per vertex: xi, eta, w
+  float gpf[kMaxQ1 * kMaxQ1][3];     // FP32 copies of gp / phi
+  float phif[kMaxQ1 * kMaxQ1][4];
 };
 
 cudaError_t upload_quadrature(const QuadTables& t);

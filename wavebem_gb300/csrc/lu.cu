@@ -505,22 +505,21 @@ struct LuState {
 };
 
 static LuState& lu_state(wbem_context* h) {
-  static thread_local std::vector<std::pair<wbem_context*, LuState*>> tbl;
-  for (auto& e : tbl)
-    if (e.first == h) return *e.second;
-  tbl.push_back({h, new LuState()});
-  return *tbl.back().second;
+  if (!h->lu_state) h->lu_state = new LuState();
+  return *static_cast<LuState*>(h->lu_state);
 }
 
 void free_lu(wbem_context* h) {
-  LuState& L = lu_state(h);
+  if (!h->lu_state) return;
+  LuState& L = *static_cast<LuState*>(h->lu_state);
   if (L.linv) cudaFree(L.linv);
   if (L.uinv) cudaFree(L.uinv);
   if (L.split) cudaFree(L.split);
   if (L.w) cudaFree(L.w);
   for (auto& g : L.graph)
     if (g) cudaGraphExecDestroy(g);
-  L = LuState();
+  delete &L;
+  h->lu_state = nullptr;
 }
 
 static int enqueue_tri_solve(wbem_context* h, LuState& L, int transpose) {
@@ -561,11 +560,9 @@ static int enqueue_tri_solve(wbem_context* h, LuState& L, int transpose) {
 int factor_mixed(wbem_context* h) {
   const int N = h->N;
   const size_t nn = (size_t)N * N;
+  if (h->lu_state && lu_state(h).N != N) free_lu(h);
   LuState& L = lu_state(h);
-  if (L.N != N) {
-    free_lu(h);
-    L.N = N;
-  }
+  L.N = N;
   if (!h->d_lu || h->lu_elems != nn) {
     WB_CHK(dev_alloc(h, &h->d_lu, nn));
     h->lu_elems = nn;

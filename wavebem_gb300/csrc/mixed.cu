@@ -291,14 +291,14 @@ __global__ void __launch_bounds__(kRowsPerTile)
         const float ddn = __fmaf_rn(Rnf, dg, -t2 * rqinv3);
         const float fs = ds * J, fn = ddn * J;
         fnsum += fn;
-        ls0 = __fmaf_rn(fs, (float)c_qm.phi[q][0], ls0);
-        ls1 = __fmaf_rn(fs, (float)c_qm.phi[q][1], ls1);
-        ls2 = __fmaf_rn(fs, (float)c_qm.phi[q][2], ls2);
-        ls3 = __fmaf_rn(fs, (float)c_qm.phi[q][3], ls3);
-        ln0 = __fmaf_rn(fn, (float)c_qm.phi[q][0], ln0);
-        ln1 = __fmaf_rn(fn, (float)c_qm.phi[q][1], ln1);
-        ln2 = __fmaf_rn(fn, (float)c_qm.phi[q][2], ln2);
-        ln3 = __fmaf_rn(fn, (float)c_qm.phi[q][3], ln3);
+        ls0 = __fmaf_rn(fs, c_qm.phif[q][0], ls0);
+        ls1 = __fmaf_rn(fs, c_qm.phif[q][1], ls1);
+        ls2 = __fmaf_rn(fs, c_qm.phif[q][2], ls2);
+        ls3 = __fmaf_rn(fs, c_qm.phif[q][3], ls3);
+        ln0 = __fmaf_rn(fn, c_qm.phif[q][0], ln0);
+        ln1 = __fmaf_rn(fn, c_qm.phif[q][1], ln1);
+        ln2 = __fmaf_rn(fn, c_qm.phif[q][2], ln2);
+        ln3 = __fmaf_rn(fn, c_qm.phif[q][3], ln3);
       }
       const float lsv[4] = {ls0, ls1, ls2, ls3}, lnv[4] = {ln0, ln1, ln2, ln3};
 #pragma unroll

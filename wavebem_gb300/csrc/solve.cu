@@ -176,7 +176,7 @@ __global__ void k_matvec_t_finish(int N, const uint8_t* __restrict__ mask,
   if (j >= N) return;
   double s = 0;
   for (int k = 0; k < kMvtSlices; ++k) s += part[(size_t)k * N + j];
-  if (!mask[j]) s = fma(alpha[j], x[j], s);
+  if (alpha && !mask[j]) s = fma(alpha[j], x[j], s);
   y[j] = s;
 }
 

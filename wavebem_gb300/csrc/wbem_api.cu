@@ -23,6 +23,7 @@ cudaError_t upload_quadrature_fp64(const QuadTables& t);
 cudaError_t upload_quadrature_mixed(const QuadTables& t);
 cudaError_t upload_quadrature_adjoint(const QuadTables& t);
 int solve_mixed(wbem_context* h, const double* d_rhs, double* d_x, int transpose);
+void free_lu(wbem_context* h);
 int assemble_mixed(wbem_context* h);
 int factor_mixed(wbem_context* h);
 void free_mixed(wbem_context* h);
@@ -114,6 +115,8 @@ static int build_quadrature(wbem_context* h, int q1, int sorder) {
       t.phi[q][1] = s * (1 - u);
       t.phi[q][2] = (1 - s) * u;
       t.phi[q][3] = s * u;
+      for (int k = 0; k < 3; ++k) t.gpf[q][k] = (float)t.gp[q][k];
+      for (int k = 0; k < 4; ++k) t.phif[q][k] = (float)t.phi[q][k];
     }
   // vertex-singular rules (polar map of the two triangles at the vertex, with
   // the 1/R weight folded into the weights), see the oracle for the derivation
@@ -624,7 +627,7 @@ int ensure_vectors(wbem_context* h, int restart) {
   const int N = h->N;
   for (int k = 0; k < 8; ++k)
     if (!h->d_vec[k]) CHK(dev_alloc(h, &h->d_vec[k], (size_t)N));
-  if (!h->d_part) CHK(dev_alloc(h, &h->d_part, (size_t)256 * 128 + (size_t)32 * N));
+  if (!h->d_part) CHK(dev_alloc(h, &h->d_part, (size_t)256 * 128 + (size_t)40 * N));
   if (!h->d_small) CHK(dev_alloc(h, &h->d_small, (size_t)512));
   if (!h->d_sol) CHK(dev_alloc(h, &h->d_sol, (size_t)N));
   if (!h->d_rhs) CHK(dev_alloc(h, &h->d_rhs, (size_t)N));
@@ -884,6 +887,7 @@ int wbem_create(wbem_handle* out, int device) {
     delete h;
     return WBEM_ERR_CUDA;
   }
+  h->own_stream = true;
   if (cudaMalloc(&h->d_err, sizeof(DevErr)) != cudaSuccess) {
     cudaStreamDestroy(h->stream);
     delete h;
@@ -898,6 +902,7 @@ int wbem_destroy(wbem_handle h) {
   if (!h) return WBEM_ERR_ARG;
   cudaSetDevice(h->device);
   cudaStreamSynchronize(h->stream);
+  free_lu(h);
   void* ptrs[] = {h->d_X, h->d_cell_dofs, h->d_dnset, h->d_tile_ptr, h->d_tile_ent, h->d_sptr,
                   h->d_scell, h->d_perm, h->d_iperm, h->d_ncptr, h->d_ncent, h->d_mask, h->d_rec,
                   h->d_rec32, h->d_cellc, h->d_cellgeo, h->d_N, h->d_D, h->d_N2, h->d_D2,
@@ -910,7 +915,7 @@ int wbem_destroy(wbem_handle h) {
     if (p) cudaFree(p);
   for (int k = 0; k < 8; ++k)
     if (h->d_vec[k]) cudaFree(h->d_vec[k]);
-  cudaStreamDestroy(h->stream);
+  if (h->own_stream) cudaStreamDestroy(h->stream);
   delete h;
   return WBEM_OK;
 }
@@ -1249,6 +1254,25 @@ int wbem_force_adjoint(wbem_handle h, const int* hull_cells, int n_hull, const d
   if (!h->have_solution) return fail(h, WBEM_ERR_STATE, "wbem_force_adjoint: solve first");
   cudaSetDevice(h->device);
   return adjoint_force(h, hull_cells, n_hull, U, dir, tmp_rhs, dF_dX, dF_drhs);
+}
+
+int wbem_set_stream(wbem_handle h, void* cuda_stream) {
+  if (!h) return WBEM_ERR_ARG;
+  cudaSetDevice(h->device);
+  cudaStreamSynchronize(h->stream);
+  if (h->own_stream) {
+    cudaStreamDestroy(h->stream);
+    h->own_stream = false;
+  }
+  if (cuda_stream) {
+    h->stream = static_cast<cudaStream_t>(cuda_stream);
+  } else {
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+      return fail(h, WBEM_ERR_CUDA, "wbem_set_stream: stream creation failed");
+    h->own_stream = true;
+  }
+  // graphs captured on the previous stream stay valid (they are launched on h->stream)
+  return WBEM_OK;
 }
 
 int wbem_get_stats(wbem_handle h, wbem_stats* st) {
