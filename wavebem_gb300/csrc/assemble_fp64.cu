@@ -90,7 +90,7 @@ __device__ __forceinline__ bool in_set(const int set[kMaxSet], int v) {
   return r;
 }
 
-constexpr int kChunk = 8;  // panels per staged chunk
+constexpr int kChunk = 6;  // panels per staged chunk
 
 template <int Q1>
 __global__ void __launch_bounds__(kRowsPerTile)
@@ -105,7 +105,8 @@ __global__ void __launch_bounds__(kRowsPerTile)
   double* stage = reinterpret_cast<double*>(smem);  // [2][kChunk][RECD], 128-byte aligned
   double* accN = stage + 2 * kChunk * RECD;         // [CT][LDA]
   double* accD = accN + CT * LDA;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(accD + CT * LDA);
+  ChunkMeta* meta = reinterpret_cast<ChunkMeta*>(accD + CT * LDA);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(meta + 2 * kChunk);
 
   const int tid = threadIdx.x;
   const int tile = blockIdx.x;
@@ -127,6 +128,24 @@ __global__ void __launch_bounds__(kRowsPerTile)
     accN[k] = 0.0;
     accD[k] = 0.0;
   }
+  const int e0 = tile_ptr[tile], e1 = tile_ptr[tile + 1];
+  const int nch = (e1 - e0 + kChunk - 1) / kChunk;
+  auto load_meta = [&](int c) {
+    const int k = tid - 32;
+    const int base = e0 + c * kChunk;
+    if (k >= 0 && k < kChunk && base + k < e1) {
+      const int2 ent = tile_ent[base + k];
+      ChunkMeta m;
+      m.cell = ent.x & 0x7fffffff;
+      m.slots = (uint32_t)ent.y;
+      m.owner = ent.x < 0;
+      m.pad = 0;
+      m.dofs = cell_dofs[m.cell];
+      m.geo = make_float4(0.f, 0.f, 0.f, 0.f);
+      meta[(c & 1) * kChunk + k] = m;
+    }
+  };
+  if (nch > 0) load_meta(0);
   if (tid == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
@@ -134,8 +153,6 @@ __global__ void __launch_bounds__(kRowsPerTile)
   }
   __syncthreads();
 
-  const int e0 = tile_ptr[tile], e1 = tile_ptr[tile + 1];
-  const int nch = (e1 - e0 + kChunk - 1) / kChunk;
   auto issue = [&](int c) {
     const int sidx = c & 1;
     const int base = e0 + c * kChunk;
@@ -155,6 +172,7 @@ __global__ void __launch_bounds__(kRowsPerTile)
       fence_proxy_async_smem();
       issue(c + 1);
     }
+    if (c + 1 < nch) load_meta(c + 1);
     in_flight_next = (c + 1 < nch);
     const bool ok = mbar_wait_bounded(&bar[c & 1], (uint32_t)((c >> 1) & 1));
     if (__syncthreads_or(!ok)) {
@@ -167,10 +185,9 @@ __global__ void __launch_bounds__(kRowsPerTile)
     const int base = e0 + c * kChunk;
     const int cnt = min(kChunk, e1 - base);
     for (int k = 0; k < cnt; ++k) {
-      const int2 ent = tile_ent[base + k];
-      const int cell = ent.x & 0x7fffffff;
-      const uint32_t slots = (uint32_t)ent.y;
-      const int4 d = cell_dofs[cell];
+      const ChunkMeta& mt = meta[(c & 1) * kChunk + k];
+      const uint32_t slots = mt.slots;
+      const int4 d = mt.dofs;
       const bool sing = in_set(set, d.x) || in_set(set, d.y) || in_set(set, d.z) || in_set(set, d.w);
       if (!active || sing) continue;
       const double* r = stage + (size_t)((c & 1) * kChunk + k) * RECD;
@@ -228,7 +245,8 @@ static cudaError_t launch_tile_fp64_t(int N, const double* X, const int* dnset, 
                                       double* Dm, DevErr* err, cudaStream_t s) {
   constexpr int RECD = Q1 * Q1 * 8;
   const size_t smem = (size_t)2 * kChunk * RECD * 8 +
-                      (size_t)2 * kColsPerTile * (kRowsPerTile + 1) * 8 + 2 * sizeof(uint64_t);
+                      (size_t)2 * kColsPerTile * (kRowsPerTile + 1) * 8 +
+                      2 * kChunk * sizeof(ChunkMeta) + 2 * sizeof(uint64_t);
   cudaError_t e = cudaFuncSetAttribute(k_tile_fp64<Q1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return e;

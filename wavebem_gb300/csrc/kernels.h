@@ -9,11 +9,21 @@
 namespace wbem {
 
 constexpr int kRowsPerTile = 128;  // collocation rows per assembly CTA (one per thread)
-constexpr int kColsPerTile = 64;   // matrix columns (dofs) per assembly CTA
+constexpr int kColsPerTile = 48;   // matrix columns (dofs) per assembly CTA
 constexpr int kMaxSet = 8;         // max size of a double-node set
 constexpr int kMaxQ1 = 8;          // max regular quadrature order per direction
 constexpr int kMaxSingular = 2 * 8 * 8;  // max points of a vertex-singular rule
 constexpr int kBJ = 128;           // block-Jacobi block size
+
+// per-panel metadata of a staged chunk (tile entry, vertex dofs, near-test data)
+struct ChunkMeta {
+  int cell;
+  uint32_t slots;
+  int owner;
+  int pad;
+  int4 dofs;
+  float4 geo;
+};
 
 // quadrature tables (constant memory, per translation unit that uses them)
 struct QuadTables {

@@ -31,7 +31,8 @@
 
 namespace wbem {
 
-constexpr int kNB = 128;  // LU block size (= GEMM K)
+constexpr int kNB = 128;   // inner LU block size (diagonal blocks, panels)
+constexpr int kNB2 = 512;  // outer block: K of the tensor-core trailing update
 
 // ------------------------------------------------------------------ input
 // LU input: hi part of the system operator, alpha on Neumann diagonals,
@@ -76,55 +77,156 @@ __global__ void k_lu_constraint_entries(int nrows, const int* __restrict__ crow,
 }
 
 // ------------------------------------------------------------ diagonal block
-// LU (no pivoting) of the kNB x kNB block at (k0, k0) in shared memory;
-// writes the factors back and inv(L) (unit lower), inv(U) to linv/uinv
-// (row-major kNB x kNB).
-__global__ void __launch_bounds__(kNB)
+// LU (no pivoting) of the kNB x kNB block at (k0, k0), then inv(L) (unit
+// lower) and inv(U), all register-tiled: 512 threads, thread t owns rows
+// 4*(t/16) .. +3 and columns 8*(t%16) .. +7; step k broadcasts the pivot row
+// and the multiplier column through double-buffered shared vectors.
+// Writes the factors back to A and the inverses row-major (linv, uinv) and
+// column-major (linvT, uinvT).
+constexpr int kDiagThreads = 512;
+__device__ __forceinline__ float sel4(const float (&v)[4][8], int i, int j) {
+  return i == 0 ? v[0][j] : i == 1 ? v[1][j] : i == 2 ? v[2][j] : v[3][j];
+}
+__device__ __forceinline__ float sel8(const float (&v)[4][8], int i, int j) {
+  float r = v[i][0];
+#pragma unroll
+  for (int u = 1; u < 8; ++u) r = (j == u) ? v[i][u] : r;
+  return r;
+}
+__global__ void __launch_bounds__(kDiagThreads, 1)
     k_diag_block(int N, int k0, int nb, float* __restrict__ A, float* __restrict__ linv,
-                 float* __restrict__ uinv, DevErr* err) {
-  extern __shared__ __align__(16) float sA[];  // [kNB][kNB+1]
-  constexpr int LD = kNB + 1;
-  const int r = threadIdx.x;
-  for (int c = 0; c < kNB; ++c)
-    sA[r * LD + c] = (r < nb && c < nb) ? A[(size_t)(k0 + r) * N + k0 + c] : (r == c ? 1.f : 0.f);
-  __syncthreads();
-  __shared__ int bad;
-  if (r == 0) bad = 0;
+                 float* __restrict__ uinv, float* __restrict__ linvT, float* __restrict__ uinvT,
+                 DevErr* err) {
+  __shared__ float rowb[2][kNB];
+  __shared__ float colb[2][kNB];
+  const int tid = threadIdx.x;
+  const int rb = tid >> 4, cb = tid & 15;
+  const int r0 = 4 * rb, c0 = 8 * cb;
+  float a[4][8], x[4][8];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int r = r0 + i, c = c0 + j;
+      a[i][j] = (r < nb && c < nb) ? A[(size_t)(k0 + r) * N + k0 + c] : (r == c ? 1.f : 0.f);
+    }
+  // ---- LU
+  for (int k = 0; k < kNB; ++k) {
+    const int bsel = k & 1;
+    if (rb == (k >> 2)) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) rowb[bsel][c0 + j] = sel4(a, k & 3, j);
+    }
+    __syncthreads();
+    const float piv = rowb[bsel][k];
+    if (!(fabsf(piv) > 0.f) || !isfinite(piv)) {
+      if (tid == 0) dev_fail(err, WBEM_ERR_SINGULAR, 51, k0, k);
+      return;  // uniform
+    }
+    if (cb == (k >> 3)) {
+      const int jj = k & 7;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int r = r0 + i;
+        const float l = (r > k) ? sel8(a, i, jj) / piv : 0.f;
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+          if (j == jj && r > k) a[i][j] = l;
+        colb[bsel][r] = l;
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const float l = colb[bsel][r0 + i];
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        if (c0 + j > k) a[i][j] = __fmaf_rn(-l, rowb[bsel][c0 + j], a[i][j]);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int r = r0 + i, c = c0 + j;
+      if (r < nb && c < nb) A[(size_t)(k0 + r) * N + k0 + c] = a[i][j];
+    }
+  // ---- inv(L): forward elimination of the identity with the multipliers
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) x[i][j] = (r0 + i == c0 + j) ? 1.f : 0.f;
   __syncthreads();
   for (int k = 0; k < kNB; ++k) {
-    const float piv = sA[k * LD + k];
-    if (r == 0 && (!(fabsf(piv) > 0.f) || !isfinite(piv))) bad = 1;
-    __syncthreads();
-    if (bad) break;
-    if (r > k) {
-      const float l = sA[r * LD + k] / piv;
-      sA[r * LD + k] = l;
-      for (int c = k + 1; c < kNB; ++c) sA[r * LD + c] = __fmaf_rn(-l, sA[k * LD + c], sA[r * LD + c]);
+    const int bsel = k & 1;
+    if (rb == (k >> 2)) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) rowb[bsel][c0 + j] = sel4(x, k & 3, j);
+    }
+    if (cb == (k >> 3)) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) colb[bsel][r0 + i] = (r0 + i > k) ? sel8(a, i, k & 7) : 0.f;
     }
     __syncthreads();
-  }
-  if (bad) {
-    if (r == 0) dev_fail(err, WBEM_ERR_SINGULAR, 51, k0, 0);
-    return;
-  }
-  if (r < nb)
-    for (int c = 0; c < nb; ++c) A[(size_t)(k0 + r) * N + k0 + c] = sA[r * LD + c];
-  // column r of inv(L): solve L x = e_r (forward); column r of inv(U): U y = e_r (backward)
-  float* Li = linv;
-  float* Ui = uinv;
-  for (int i = 0; i < kNB; ++i) {
-    float s = (i == r) ? 1.f : 0.f;
-    for (int j = r; j < i; ++j) s = __fmaf_rn(-sA[i * LD + j], Li[j * kNB + r], s);
-    Li[i * kNB + r] = (i < r) ? 0.f : s;
-  }
-  for (int i = kNB - 1; i >= 0; --i) {
-    float s = (i == r) ? 1.f : 0.f;
-    if (i <= r) {
-      for (int j = i + 1; j <= r; ++j) s = __fmaf_rn(-sA[i * LD + j], Ui[j * kNB + r], s);
-      s /= sA[i * LD + i];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const float l = colb[bsel][r0 + i];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) x[i][j] = __fmaf_rn(-l, rowb[bsel][c0 + j], x[i][j]);
     }
-    Ui[i * kNB + r] = (i > r) ? 0.f : s;
   }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int r = r0 + i, c = c0 + j;
+      linv[r * kNB + c] = x[i][j];
+      linvT[c * kNB + r] = x[i][j];
+    }
+  // ---- inv(U): backward elimination of the identity
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) x[i][j] = (r0 + i == c0 + j) ? 1.f : 0.f;
+  __syncthreads();
+  for (int kk = 0; kk < kNB; ++kk) {
+    const int k = kNB - 1 - kk;
+    const int bsel = kk & 1;
+    // U[k][k] and the column U[r][k], r < k
+    if (cb == (k >> 3)) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) colb[bsel][r0 + i] = (r0 + i <= k) ? sel8(a, i, k & 7) : 0.f;
+    }
+    __syncthreads();
+    const float ukk = colb[bsel][k];
+    if (rb == (k >> 2)) {
+      const int ii = k & 3;
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+          if (i == ii) x[i][j] = x[i][j] / ukk;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) rowb[bsel][c0 + j] = sel4(x, ii, j);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      if (r0 + i < k) {
+        const float u = colb[bsel][r0 + i];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) x[i][j] = __fmaf_rn(-u, rowb[bsel][c0 + j], x[i][j]);
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int r = r0 + i, c = c0 + j;
+      uinv[r * kNB + c] = x[i][j];
+      uinvT[c * kNB + r] = x[i][j];
+    }
 }
 
 // ------------------------------------------------------------- panel GEMM
@@ -141,15 +243,26 @@ __device__ __forceinline__ void split_bf16(float v, uint16_t* hi, uint16_t* lo) 
   *lo = __bfloat16_as_ushort(l);
 }
 
+struct SplitOut {
+  uint16_t* hi;   // BF16 hi part, row-major rows x ld
+  uint16_t* lo;
+  int row0;       // absolute matrix index of split row 0
+  int ld;         // row length (K of the GEMM that consumes it)
+  int coloff;     // column offset inside a row
+};
+
+//   mode 0 (row panel):  out[128 x ncols] = inv(L_kk) * A[k0:k0+128, cbeg:cbeg+ncols]
+//                        -> A, and split rows (cbeg + c - row0), columns (coloff + r)
+//   mode 1 (col panel):  out[nrows x 128] = A[rbeg:rbeg+nrows, k0:k0+128] * inv(U_kk)
+//                        -> A, and split rows (rbeg + r - row0) (rows >= row0 only),
+//                           columns (coloff + c)
 __global__ void __launch_bounds__(256)
-    k_panel_gemm(int N, int mode, int k0, int nrows, int ncols, float* __restrict__ A,
-                 const float* __restrict__ inv, uint16_t* __restrict__ Shi,
-                 uint16_t* __restrict__ Slo) {
+    k_panel_gemm(int N, int mode, int k0, int rbeg, int nrows, int cbeg, int ncols,
+                 float* __restrict__ A, const float* __restrict__ inv, SplitOut s1, SplitOut s2) {
   __shared__ float sL[64][33];
   __shared__ float sR[32][65];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   const int r0 = blockIdx.y * 64, c0 = blockIdx.x * 64;
-  const int k1 = k0 + kNB;
   float acc[4][4] = {};
   for (int kk = 0; kk < kNB; kk += 32) {
     for (int t = threadIdx.x; t < 64 * 32; t += 256) {
@@ -158,7 +271,7 @@ __global__ void __launch_bounds__(256)
       if (mode == 0) {
         v = (r0 + rr < kNB) ? inv[(r0 + rr) * kNB + kk + cc] : 0.f;
       } else if (r0 + rr < nrows) {
-        v = A[(size_t)(k1 + r0 + rr) * N + k0 + kk + cc];
+        v = A[(size_t)(rbeg + r0 + rr) * N + k0 + kk + cc];
       }
       sL[rr][cc] = v;
     }
@@ -166,7 +279,7 @@ __global__ void __launch_bounds__(256)
       const int rr = t / 64, cc = t % 64;
       float v = 0.f;
       if (mode == 0) {
-        if (c0 + cc < ncols) v = A[(size_t)(k0 + kk + rr) * N + k1 + c0 + cc];
+        if (c0 + cc < ncols) v = A[(size_t)(k0 + kk + rr) * N + cbeg + c0 + cc];
       } else if (c0 + cc < kNB) {
         v = inv[(kk + rr) * kNB + c0 + cc];
       }
@@ -193,17 +306,79 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
       const int rr = r0 + ty * 4 + u, cc = c0 + tx * 4 + v;
+      const float val = acc[u][v];
       if (mode == 0) {
         if (rr < kNB && cc < ncols) {
-          A[(size_t)(k0 + rr) * N + k1 + cc] = acc[u][v];
-          split_bf16(acc[u][v], &Shi[(size_t)cc * kNB + rr], &Slo[(size_t)cc * kNB + rr]);
+          const int col = cbeg + cc;
+          A[(size_t)(k0 + rr) * N + col] = val;
+          if (s1.hi) {
+            const size_t o = (size_t)(col - s1.row0) * s1.ld + s1.coloff + rr;
+            split_bf16(val, &s1.hi[o], &s1.lo[o]);
+          }
+          if (s2.hi) {
+            const size_t o = (size_t)(col - s2.row0) * s2.ld + s2.coloff + rr;
+            split_bf16(val, &s2.hi[o], &s2.lo[o]);
+          }
         }
       } else {
         if (rr < nrows && cc < kNB) {
-          A[(size_t)(k1 + rr) * N + k0 + cc] = acc[u][v];
-          split_bf16(acc[u][v], &Shi[(size_t)rr * kNB + cc], &Slo[(size_t)rr * kNB + cc]);
+          const int row = rbeg + rr;
+          A[(size_t)row * N + k0 + cc] = val;
+          if (s1.hi) {
+            const size_t o = (size_t)(row - s1.row0) * s1.ld + s1.coloff + cc;
+            split_bf16(val, &s1.hi[o], &s1.lo[o]);
+          }
+          if (s2.hi && row >= s2.row0) {
+            const size_t o = (size_t)(row - s2.row0) * s2.ld + s2.coloff + cc;
+            split_bf16(val, &s2.hi[o], &s2.lo[o]);
+          }
         }
       }
+    }
+}
+
+// C[128 x n] -= Lrow[128 x K] * U[K x n] (FP32 SIMT, all operands inside the
+// LU buffer, ld N): the contributions of the earlier 128-blocks of an outer
+// panel to the row panel of a later block.
+__global__ void __launch_bounds__(256)
+    k_rowpanel_update(int N, int K, const float* __restrict__ Lrow, const float* __restrict__ U,
+                      float* __restrict__ Cm, int n) {
+  __shared__ float sL[64][33];
+  __shared__ float sR[32][65];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int r0 = blockIdx.y * 64, c0 = blockIdx.x * 64;
+  float acc[4][4] = {};
+  for (int kk = 0; kk < K; kk += 32) {
+    for (int t = threadIdx.x; t < 64 * 32; t += 256) {
+      const int rr = t / 32, cc = t % 32;
+      sL[rr][cc] = Lrow[(size_t)(r0 + rr) * N + kk + cc];
+    }
+    for (int t = threadIdx.x; t < 32 * 64; t += 256) {
+      const int rr = t / 64, cc = t % 64;
+      sR[rr][cc] = (c0 + cc < n) ? U[(size_t)(kk + rr) * N + c0 + cc] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int k = 0; k < 32; ++k) {
+      float a[4], b[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        a[u] = sL[ty * 4 + u][k];
+        b[u] = sR[k][tx * 4 + u];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = __fmaf_rn(a[u], b[v], acc[u][v]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int rr = r0 + ty * 4 + u, cc = c0 + tx * 4 + v;
+      if (cc < n) Cm[(size_t)rr * N + cc] -= acc[u][v];
     }
 }
 
@@ -435,50 +610,130 @@ static cudaError_t run_gemm(const GemmMaps& mp, int M, int Nc, int K, float* Cm,
 }
 
 // ------------------------------------------------------------ triangular solves
-// Blocked FP32 forward / backward substitution with the stored diagonal-block
-// inverses. Work vector w (float, N). Forward (L, unit lower):
-//   y_k = inv(L_kk) w_k ;  w_i -= L_ik y_k (i > k).
-// Backward (U): x_k = inv(U_kk) w_k ; w_i -= U_ik x_k (i < k).
-// Transposed solves (A^T = U^T L^T) use the row blocks instead of the column
-// blocks: forward with U^T, backward with L^T.
-__global__ void k_tri_diag(int N, int k0, int nb, const float* __restrict__ inv, int transpose,
-                           float* __restrict__ w) {
-  __shared__ float xs[kNB];
-  const int r = threadIdx.x;
-  xs[r] = (r < nb) ? w[k0 + r] : 0.f;
-  __syncthreads();
-  float s = 0.f;
-  if (!transpose)
-    for (int c = 0; c < kNB; ++c) s = __fmaf_rn(inv[r * kNB + c], xs[c], s);
-  else
-    for (int c = 0; c < kNB; ++c) s = __fmaf_rn(inv[c * kNB + r], xs[c], s);
-  if (r < nb) w[k0 + r] = s;
+// One cooperative launch per triangular sweep: CTA k owns block row k. It
+// subtracts the contributions of the already solved blocks as they are
+// published (flag[j] == epoch, bounded spin), applies the stored inverse of
+// its diagonal block and publishes its own block. Modes:
+//   0: L y = w (forward),   1: U x = y (backward),
+//   2: U^T y = w (forward), 3: L^T x = y (backward).
+// Rows of a block (modes 0/1) or columns (2/3) are read with coalesced loads.
+constexpr int kTriThreads = 256;
+// Block tile of one step in registers (64 floats per thread), loaded before
+// the wait on the block's flag so that the DRAM latency overlaps the wait.
+//   modes 0/1 (rows of block (k, j)): warp w holds rows 16 w .. +15, lane l
+//       holds columns 4 l .. 4 l + 3 of each;
+//   modes 2/3 (columns of block (j, k)): thread t holds column t % 128 of rows
+//       t / 128, + 2, + 4, ...
+__device__ __forceinline__ void tri_load(float t[64], int mode, const float* __restrict__ LU, int N,
+                                         int k0, int nb, int j0, int jn, bool vec4) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (mode <= 1) {
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const int r = warp * 16 + i;
+      const int c = 4 * lane;
+      const float* p = LU + (size_t)(k0 + r) * N + j0 + c;
+      if (r < nb && c + 3 < jn && vec4) {
+        const float4 v = __ldcs(reinterpret_cast<const float4*>(p));
+        t[4 * i] = v.x; t[4 * i + 1] = v.y; t[4 * i + 2] = v.z; t[4 * i + 3] = v.w;
+      } else {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) t[4 * i + u] = (r < nb && c + u < jn) ? __ldcs(p + u) : 0.f;
+      }
+    }
+  } else {
+    const int c = tid & (kNB - 1), h = tid >> 7;
+#pragma unroll
+    for (int i = 0; i < 64; ++i) {
+      const int r = h + 2 * i;
+      t[i] = (c < nb && r < jn) ? __ldcs(LU + (size_t)(j0 + r) * N + k0 + c) : 0.f;
+    }
+  }
 }
 
-// w[rows] -= M[rows, k0:k0+nb] x  (column-block update; ld = N), or for the
-// transposed sweep w[cols] -= M[k0:k0+nb, cols]^T x (row-block update).
-__global__ void k_tri_update(int N, int k0, int nb, int lo, int hi, const float* __restrict__ LU,
-                             int rowblock, float* __restrict__ w) {
-  __shared__ float xs[kNB];
-  if (threadIdx.x < kNB) xs[threadIdx.x] = (threadIdx.x < nb) ? w[k0 + threadIdx.x] : 0.f;
+__global__ void __launch_bounds__(kTriThreads)
+    k_trsv_wave(int N, int nblk, int mode, const float* __restrict__ LU,
+                const float* __restrict__ dinv, const float* __restrict__ in,
+                float* __restrict__ out, unsigned* __restrict__ flags, unsigned epoch,
+                DevErr* err) {
+  extern __shared__ __align__(16) float tsm[];
+  float* sInv = tsm;               // kNB x kNB: thread r reads sInv[c * kNB + r]
+  float* acc = sInv + kNB * kNB;   // [kNB]
+  float* v = acc + kNB;            // [kNB]
+  float* part = v + kNB;           // [2][kNB]
+  __shared__ int bad;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const bool fwd = (mode == 0 || mode == 2);
+  const int k = fwd ? blockIdx.x : nblk - 1 - blockIdx.x;
+  const int k0 = k * kNB, nb = min(kNB, N - k0);
+  const bool vec4 = (N & 3) == 0;
+  const float* Dk = dinv + (size_t)k * kNB * kNB;
+  for (int idx = tid; idx < kNB * kNB; idx += kTriThreads) sInv[idx] = Dk[idx];
+  if (tid < kNB) acc[tid] = (tid < nb) ? in[k0 + tid] : 0.f;
+  if (tid == 0) bad = 0;
+  const int jbeg = fwd ? 0 : nblk - 1, jend = k, jstep = fwd ? 1 : -1;
+  float t[64];
+  if (jbeg != jend) {
+    const int j0 = jbeg * kNB;
+    tri_load(t, mode, LU, N, k0, nb, j0, min(kNB, N - j0), vec4);
+  }
   __syncthreads();
-  if (!rowblock) {
-    // one warp per row
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    const int i = lo + warp;
-    if (i >= hi) return;
-    const float* r = LU + (size_t)i * N + k0;
-    float s = 0.f;
-    for (int c = lane; c < nb; c += 32) s = __fmaf_rn(r[c], xs[c], s);
+  for (int j = jbeg; j != jend; j += jstep) {
+    const int j0 = j * kNB, jn = min(kNB, N - j0);
+    if (tid == 0 && !bad) {
+      uint32_t it = 0;
+      while (*((volatile unsigned*)&flags[j]) != epoch) {
+        if (++it > (1u << 26)) {
+          bad = 1;
+          dev_fail(err, WBEM_ERR_TIMEOUT, 71, k, j);
+          break;
+        }
+      }
+      __threadfence();
+    }
+    __syncthreads();
+    if (bad) break;
+    if (tid < kNB) v[tid] = (tid < jn) ? __ldcg(out + j0 + tid) : 0.f;
+    __syncthreads();
+    if (mode <= 1) {
+      const float4 vv = reinterpret_cast<const float4*>(v)[lane];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) w[i] -= s;
-  } else {
-    const int j = lo + blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= hi) return;
-    float s = 0.f;
-    for (int c = 0; c < nb; ++c) s = __fmaf_rn(LU[(size_t)(k0 + c) * N + j], xs[c], s);
-    w[j] -= s;
+      for (int i = 0; i < 16; ++i) {
+        float s2 = t[4 * i] * vv.x;
+        s2 = __fmaf_rn(t[4 * i + 1], vv.y, s2);
+        s2 = __fmaf_rn(t[4 * i + 2], vv.z, s2);
+        s2 = __fmaf_rn(t[4 * i + 3], vv.w, s2);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+        if (lane == 0) acc[warp * 16 + i] -= s2;
+      }
+    } else {
+      const int c = tid & (kNB - 1), h = tid >> 7;
+      float s2 = 0.f;
+#pragma unroll
+      for (int i = 0; i < 64; ++i) s2 = __fmaf_rn(t[i], v[h + 2 * i], s2);
+      part[h * kNB + c] = s2;
+    }
+    // prefetch the next block while the next flag is pending
+    const int jn2 = j + jstep;
+    if (jn2 != jend) {
+      const int j02 = jn2 * kNB;
+      tri_load(t, mode, LU, N, k0, nb, j02, min(kNB, N - j02), vec4);
+    }
+    __syncthreads();
+    if (mode >= 2 && tid < kNB) acc[tid] -= part[tid] + part[kNB + tid];
+    __syncthreads();
+  }
+  // diagonal block
+  if (tid < kNB) {
+    float s2 = 0.f;
+    for (int c = 0; c < kNB; ++c) s2 = __fmaf_rn(sInv[c * kNB + tid], acc[c], s2);
+    if (tid < nb) out[k0 + tid] = s2;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    __threadfence();
+    atomicExch(&flags[k], epoch);
   }
 }
 
@@ -495,11 +750,16 @@ __global__ void k_to_double(int N, const float* __restrict__ x, double* __restri
 int gmres_mixed_driver(wbem_context* h, const double* rhs, double* x, int transpose);
 
 struct LuState {
-  float* linv = nullptr;  // per block kNB x kNB
+  float* linv = nullptr;  // per block kNB x kNB, row-major
   float* uinv = nullptr;
-  uint16_t* split = nullptr;  // Lhi, Llo, Uhi, Ulo: each N x kNB
-  float* w = nullptr;
-  cudaGraphExec_t graph[2] = {nullptr, nullptr};  // forward+backward, transposed
+  float* linvT = nullptr;  // column-major copies
+  float* uinvT = nullptr;
+  uint16_t* split = nullptr;  // inner (K = 128) Lhi, Llo, Uhi, Ulo: each (N + GN) x kNB
+  uint16_t* split2 = nullptr; // outer (K = kNB2) L21hi, L21lo, U12Thi, U12Tlo
+  GemmMaps maps2;
+  float* w = nullptr;         // 2 x N ping-pong vectors
+  unsigned* flags = nullptr;  // 4 x nblk publication flags
+  unsigned epoch = 0;
   int N = 0;
   GemmMaps maps;
 };
@@ -514,47 +774,41 @@ void free_lu(wbem_context* h) {
   LuState& L = *static_cast<LuState*>(h->lu_state);
   if (L.linv) cudaFree(L.linv);
   if (L.uinv) cudaFree(L.uinv);
+  if (L.linvT) cudaFree(L.linvT);
+  if (L.uinvT) cudaFree(L.uinvT);
   if (L.split) cudaFree(L.split);
+  if (L.split2) cudaFree(L.split2);
   if (L.w) cudaFree(L.w);
-  for (auto& g : L.graph)
-    if (g) cudaGraphExecDestroy(g);
+  if (L.flags) cudaFree(L.flags);
   delete &L;
   h->lu_state = nullptr;
 }
 
-static int enqueue_tri_solve(wbem_context* h, LuState& L, int transpose) {
+static int tri_sweep(wbem_context* h, LuState& L, int mode, const float* in, float* out) {
   const int N = h->N;
   const int nblk = (N + kNB - 1) / kNB;
-  const float* LU = h->d_lu;
-  if (!transpose) {
-    // L y = w (forward): diag with inv(L_kk), update rows below from column block k
-    for (int k = 0; k < nblk; ++k) {
-      const int k0 = k * kNB, nb = std::min(kNB, N - k0);
-      k_tri_diag<<<1, kNB, 0, h->stream>>>(N, k0, nb, L.linv + (size_t)k * kNB * kNB, 0, L.w);
-      const int lo = k0 + nb, hi = N;
-      if (hi > lo) k_tri_update<<<(hi - lo + 7) / 8, 256, 0, h->stream>>>(N, k0, nb, lo, hi, LU, 0, L.w);
-    }
-    for (int k = nblk - 1; k >= 0; --k) {
-      const int k0 = k * kNB, nb = std::min(kNB, N - k0);
-      k_tri_diag<<<1, kNB, 0, h->stream>>>(N, k0, nb, L.uinv + (size_t)k * kNB * kNB, 0, L.w);
-      if (k0 > 0) k_tri_update<<<(k0 + 7) / 8, 256, 0, h->stream>>>(N, k0, nb, 0, k0, LU, 0, L.w);
-    }
-  } else {
-    // U^T y = w (forward): diag with inv(U_kk)^T, update columns right of k from row block k of U
-    for (int k = 0; k < nblk; ++k) {
-      const int k0 = k * kNB, nb = std::min(kNB, N - k0);
-      k_tri_diag<<<1, kNB, 0, h->stream>>>(N, k0, nb, L.uinv + (size_t)k * kNB * kNB, 1, L.w);
-      const int lo = k0 + nb, hi = N;
-      if (hi > lo) k_tri_update<<<(hi - lo + 255) / 256, 256, 0, h->stream>>>(N, k0, nb, lo, hi, LU, 1, L.w);
-    }
-    // L^T x = y (backward): diag with inv(L_kk)^T, update columns left of k from row block k of L
-    for (int k = nblk - 1; k >= 0; --k) {
-      const int k0 = k * kNB, nb = std::min(kNB, N - k0);
-      k_tri_diag<<<1, kNB, 0, h->stream>>>(N, k0, nb, L.linv + (size_t)k * kNB * kNB, 1, L.w);
-      if (k0 > 0) k_tri_update<<<(k0 + 255) / 256, 256, 0, h->stream>>>(N, k0, nb, 0, k0, LU, 1, L.w);
-    }
+  const float* dinv = (mode == 0) ? L.linvT : (mode == 1) ? L.uinvT : (mode == 2) ? L.uinv : L.linv;
+  unsigned* flags = L.flags + (size_t)mode * nblk;
+  unsigned epoch = ++L.epoch;
+  const size_t smem = (size_t)(kNB * kNB + 4 * kNB) * sizeof(float);
+  static bool attr = false;
+  if (!attr) {
+    WB_CU(cudaFuncSetAttribute(k_trsv_wave, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
   }
-  return cudaGetLastError() == cudaSuccess ? WBEM_OK : fail(h, WBEM_ERR_CUDA, "triangular solve launch");
+  int dev = 0, sms = 0, per_sm = 0;
+  WB_CU(cudaGetDevice(&dev));
+  WB_CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  WB_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trsv_wave, kTriThreads, smem));
+  if ((long long)per_sm * sms < nblk)
+    return fail(h, WBEM_ERR_ARG, "triangular sweep: too many blocks to be co-resident");
+  const float* LU = h->d_lu;
+  DevErr* err = h->d_err;
+  void* args[] = {(void*)&N, (void*)&nblk, (void*)&mode, (void*)&LU, (void*)&dinv, (void*)&in,
+                  (void*)&out, (void*)&flags, (void*)&epoch, (void*)&err};
+  WB_CU(cudaLaunchCooperativeKernel((const void*)k_trsv_wave, dim3(nblk), dim3(kTriThreads), args,
+                                    smem, h->stream));
+  return WBEM_OK;
 }
 
 int factor_mixed(wbem_context* h) {
@@ -568,25 +822,34 @@ int factor_mixed(wbem_context* h) {
     h->lu_elems = nn;
   }
   const int nblk = (N + kNB - 1) / kNB;
+  const size_t rows = (size_t)N + GN;
   if (!L.linv) {
     WB_CHK(dev_alloc(h, &L.linv, (size_t)nblk * kNB * kNB));
     WB_CHK(dev_alloc(h, &L.uinv, (size_t)nblk * kNB * kNB));
-    WB_CHK(dev_alloc(h, &L.split, (size_t)4 * ((size_t)N + GN) * kNB));
-    WB_CHK(dev_alloc(h, &L.w, (size_t)N));
-    WB_CU(cudaMemset(L.split, 0, sizeof(uint16_t) * 4 * ((size_t)N + GN) * kNB));
-    uint16_t* Lhi = L.split;
-    uint16_t* Llo = Lhi + ((size_t)N + GN) * kNB;
-    uint16_t* Uhi = Llo + ((size_t)N + GN) * kNB;
-    uint16_t* Ulo = Uhi + ((size_t)N + GN) * kNB;
-    const int rows = N + GN;
-    if (!encode_map(&L.maps.Ahi, Lhi, rows, kNB, GM) || !encode_map(&L.maps.Alo, Llo, rows, kNB, GM) ||
-        !encode_map(&L.maps.Bhi, Uhi, rows, kNB, GN) || !encode_map(&L.maps.Blo, Ulo, rows, kNB, GN))
+    WB_CHK(dev_alloc(h, &L.linvT, (size_t)nblk * kNB * kNB));
+    WB_CHK(dev_alloc(h, &L.uinvT, (size_t)nblk * kNB * kNB));
+    WB_CHK(dev_alloc(h, &L.split, (size_t)4 * rows * kNB));
+    WB_CHK(dev_alloc(h, &L.split2, (size_t)4 * rows * kNB2));
+    WB_CHK(dev_alloc(h, &L.w, (size_t)2 * N));
+    WB_CHK(dev_alloc(h, &L.flags, (size_t)4 * nblk));
+    WB_CU(cudaMemsetAsync(L.flags, 0, sizeof(unsigned) * 4 * nblk, h->stream));
+    WB_CU(cudaMemsetAsync(L.split, 0, sizeof(uint16_t) * 4 * rows * kNB, h->stream));
+    WB_CU(cudaMemsetAsync(L.split2, 0, sizeof(uint16_t) * 4 * rows * kNB2, h->stream));
+    L.epoch = 0;
+    uint16_t* b1 = L.split;
+    uint16_t* b2 = L.split2;
+    if (!encode_map(&L.maps.Ahi, b1, (int)rows, kNB, GM) ||
+        !encode_map(&L.maps.Alo, b1 + rows * kNB, (int)rows, kNB, GM) ||
+        !encode_map(&L.maps.Bhi, b1 + 2 * rows * kNB, (int)rows, kNB, GN) ||
+        !encode_map(&L.maps.Blo, b1 + 3 * rows * kNB, (int)rows, kNB, GN) ||
+        !encode_map(&L.maps2.Ahi, b2, (int)rows, kNB2, GM) ||
+        !encode_map(&L.maps2.Alo, b2 + rows * kNB2, (int)rows, kNB2, GM) ||
+        !encode_map(&L.maps2.Bhi, b2 + 2 * rows * kNB2, (int)rows, kNB2, GN) ||
+        !encode_map(&L.maps2.Blo, b2 + 3 * rows * kNB2, (int)rows, kNB2, GN))
       return fail(h, WBEM_ERR_CUDA, "cuTensorMapEncodeTiled failed");
   }
-  uint16_t* Lhi = L.split;
-  uint16_t* Llo = Lhi + ((size_t)N + GN) * kNB;
-  uint16_t* Uhi = Llo + ((size_t)N + GN) * kNB;
-  uint16_t* Ulo = Uhi + ((size_t)N + GN) * kNB;
+  uint16_t* b1 = L.split;
+  uint16_t* b2 = L.split2;
   EvTimer tm(h->stream);
   {
     dim3 g(std::min(64, (N + 255) / 256), N);
@@ -600,43 +863,62 @@ int factor_mixed(wbem_context* h) {
     }
   }
   h->stats.t_system_ms = tm.ms();
-  const size_t dsm = (size_t)kNB * (kNB + 1) * sizeof(float);
-  WB_CU(cudaFuncSetAttribute(k_diag_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm));
-  for (int k = 0; k < nblk; ++k) {
-    const int k0 = k * kNB, nb = std::min(kNB, N - k0);
-    const int k1 = k0 + nb, m = N - k1;
-    k_diag_block<<<1, kNB, dsm, h->stream>>>(N, k0, nb, h->d_lu, L.linv + (size_t)k * kNB * kNB,
-                                             L.uinv + (size_t)k * kNB * kNB, h->d_err);
+  float* A = h->d_lu;
+  const SplitOut none{nullptr, nullptr, 0, 0, 0};
+  for (int p0 = 0; p0 < N; p0 += kNB2) {
+    const int p1 = std::min(N, p0 + kNB2);
+    // ---- factor the panel columns [p0, p1): 128-wide blocks, right-looking
+    for (int k0 = p0; k0 < p1; k0 += kNB) {
+      const int k = k0 / kNB, nb = std::min(kNB, N - k0), k1 = k0 + nb;
+      const size_t bo = (size_t)k * kNB * kNB;
+      k_diag_block<<<1, kDiagThreads, 0, h->stream>>>(N, k0, nb, A, L.linv + bo, L.uinv + bo,
+                                                      L.linvT + bo, L.uinvT + bo, h->d_err);
+      h->launches++;
+      if (k1 >= N) break;
+      const int m = N - k1;
+      const SplitOut Lin{b1, b1 + rows * kNB, k1, kNB, 0};
+      const SplitOut Uin{b1 + 2 * rows * kNB, b1 + 3 * rows * kNB, k1, kNB, 0};
+      const SplitOut L21{b2, b2 + rows * kNB2, p1, kNB2, k0 - p0};
+      // column panel (full height), inner split + outer L21 split
+      dim3 gc(2, (m + 63) / 64);
+      k_panel_gemm<<<gc, 256, 0, h->stream>>>(N, 1, k0, k1, m, 0, 0, A, L.uinv + bo, Lin,
+                                              p1 < N ? L21 : none);
+      h->launches++;
+      if (k1 < p1) {
+        const int w = p1 - k1;
+        dim3 gr((w + 63) / 64, 2);
+        k_panel_gemm<<<gr, 256, 0, h->stream>>>(N, 0, k0, 0, 0, k1, w, A, L.linv + bo, Uin, none);
+        WB_CU(cudaGetLastError());
+        WB_CU(run_gemm(L.maps, m, w, kNB, A + (size_t)k1 * N + k1, N, h->d_err, h->stream));
+        h->launches += 2;
+      }
+      WB_CU(cudaGetLastError());
+    }
+    if (p1 >= N) break;
+    // ---- row panel U12 = inv(L11) A12, one 128-block row at a time
+    const int n = N - p1;
+    for (int k0 = p0; k0 < p1; k0 += kNB) {
+      const int k = k0 / kNB;
+      const size_t bo = (size_t)k * kNB * kNB;
+      if (k0 > p0) {
+        dim3 gu((n + 63) / 64, 2);
+        k_rowpanel_update<<<gu, 256, 0, h->stream>>>(N, k0 - p0, A + (size_t)k0 * N + p0,
+                                                     A + (size_t)p0 * N + p1,
+                                                     A + (size_t)k0 * N + p1, n);
+        h->launches++;
+      }
+      const SplitOut U12{b2 + 2 * rows * kNB2, b2 + 3 * rows * kNB2, p1, kNB2, k0 - p0};
+      dim3 gr((n + 63) / 64, 2);
+      k_panel_gemm<<<gr, 256, 0, h->stream>>>(N, 0, k0, 0, 0, p1, n, A, L.linv + bo, U12, none);
+      h->launches++;
+      WB_CU(cudaGetLastError());
+    }
+    // ---- trailing update A22 -= L21 U12 on the tensor cores (K = 512)
+    WB_CU(run_gemm(L.maps2, n, n, p1 - p0, A + (size_t)p1 * N + p1, N, h->d_err, h->stream));
     h->launches++;
-    if (m <= 0) break;
-    // row panel U_kj (128 x m) and column panel L_ik (m x 128)
-    dim3 gr((m + 63) / 64, (kNB + 63) / 64);
-    k_panel_gemm<<<gr, 256, 0, h->stream>>>(N, 0, k0, kNB, m, h->d_lu,
-                                            L.linv + (size_t)k * kNB * kNB, Uhi, Ulo);
-    dim3 gc((kNB + 63) / 64, (m + 63) / 64);
-    k_panel_gemm<<<gc, 256, 0, h->stream>>>(N, 1, k0, m, kNB, h->d_lu,
-                                            L.uinv + (size_t)k * kNB * kNB, Lhi, Llo);
-    WB_CU(cudaGetLastError());
-    WB_CU(run_gemm(L.maps, m, m, kNB, h->d_lu + (size_t)k1 * N + k1, N, h->d_err, h->stream));
-    h->launches += 3;
   }
   WB_CHK(check_device_error(h, "LU factorisation"));
   h->stats.t_factor_ms = tm.ms();
-  // capture the triangular sweeps as CUDA graphs (fixed launch sequence)
-  for (int t = 0; t < 2; ++t) {
-    if (L.graph[t]) {
-      cudaGraphExecDestroy(L.graph[t]);
-      L.graph[t] = nullptr;
-    }
-    cudaGraph_t g;
-    WB_CU(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    int st = enqueue_tri_solve(h, L, t);
-    cudaError_t e = cudaStreamEndCapture(h->stream, &g);
-    if (st != WBEM_OK) return st;
-    WB_CU(e);
-    WB_CU(cudaGraphInstantiate(&L.graph[t], g, 0));
-    cudaGraphDestroy(g);
-  }
   return WBEM_OK;
 }
 
@@ -644,12 +926,20 @@ int factor_mixed(wbem_context* h) {
 int lu_apply(wbem_context* h, const double* v, double* z, int transpose) {
   LuState& L = lu_state(h);
   const int N = h->N;
-  k_to_float<<<(N + 255) / 256, 256, 0, h->stream>>>(N, v, L.w);
+  float* w0 = L.w;
+  float* w1 = L.w + N;
+  k_to_float<<<(N + 255) / 256, 256, 0, h->stream>>>(N, v, w0);
   WB_CU(cudaGetLastError());
-  WB_CU(cudaGraphLaunch(L.graph[transpose ? 1 : 0], h->stream));
-  k_to_double<<<(N + 255) / 256, 256, 0, h->stream>>>(N, L.w, z);
+  if (!transpose) {
+    WB_CHK(tri_sweep(h, L, 0, w0, w1));  // L y = v
+    WB_CHK(tri_sweep(h, L, 1, w1, w0));  // U z = y
+  } else {
+    WB_CHK(tri_sweep(h, L, 2, w0, w1));  // U^T y = v
+    WB_CHK(tri_sweep(h, L, 3, w1, w0));  // L^T z = y
+  }
+  k_to_double<<<(N + 255) / 256, 256, 0, h->stream>>>(N, w0, z);
   WB_CU(cudaGetLastError());
-  h->launches += 2 + 4 * ((N + kNB - 1) / kNB);
+  h->launches += 4;
   return WBEM_OK;
 }
 

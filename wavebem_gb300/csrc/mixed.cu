@@ -157,7 +157,8 @@ __global__ void __launch_bounds__(kRowsPerTile)
   float* aNl = aNh + CT * LDA;
   float* aDh = aNl + CT * LDA;
   float* aDl = aDh + CT * LDA;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(aDl + CT * LDA + ((CT * LDA) & 1));
+  ChunkMeta* meta = reinterpret_cast<ChunkMeta*>(aDl + CT * LDA + ((4 - ((CT * LDA) & 3)) & 3));
+  uint64_t* bar = reinterpret_cast<uint64_t*>(meta + 2 * kChunkM);
 
   const int tid = threadIdx.x;
   const int tile = blockIdx.x;
@@ -183,6 +184,25 @@ __global__ void __launch_bounds__(kRowsPerTile)
     aDh[k] = 0.f;
     aDl[k] = 0.f;
   }
+  const int e0 = tile_ptr[tile], e1 = tile_ptr[tile + 1];
+  const int nch = (e1 - e0 + kChunkM - 1) / kChunkM;
+  // metadata of chunk c into meta[c & 1] (threads 32 .. 32 + kChunkM - 1)
+  auto load_meta = [&](int c) {
+    const int k = tid - 32;
+    const int base = e0 + c * kChunkM;
+    if (k >= 0 && k < kChunkM && base + k < e1) {
+      const int2 ent = tile_ent[base + k];
+      ChunkMeta m;
+      m.cell = ent.x & 0x7fffffff;
+      m.slots = (uint32_t)ent.y;
+      m.owner = ent.x < 0;
+      m.pad = 0;
+      m.dofs = cell_dofs[m.cell];
+      m.geo = cellgeo[m.cell];
+      meta[(c & 1) * kChunkM + k] = m;
+    }
+  };
+  if (nch > 0) load_meta(0);
   if (tid == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
@@ -191,8 +211,6 @@ __global__ void __launch_bounds__(kRowsPerTile)
   __syncthreads();
   df alpha_acc = {0.f, 0.f};
 
-  const int e0 = tile_ptr[tile], e1 = tile_ptr[tile + 1];
-  const int nch = (e1 - e0 + kChunkM - 1) / kChunkM;
   auto issue = [&](int c) {
     const int sidx = c & 1;
     const int base = e0 + c * kChunkM;
@@ -211,6 +229,7 @@ __global__ void __launch_bounds__(kRowsPerTile)
       fence_proxy_async_smem();
       issue(c + 1);
     }
+    if (c + 1 < nch) load_meta(c + 1);
     const bool ok = mbar_wait_bounded(&bar[c & 1], (uint32_t)((c >> 1) & 1));
     if (__syncthreads_or(!ok)) {
       if (tid == 0) {
@@ -222,14 +241,13 @@ __global__ void __launch_bounds__(kRowsPerTile)
     const int base = e0 + c * kChunkM;
     const int cnt = min(kChunkM, e1 - base);
     for (int k = 0; k < cnt; ++k) {
-      const int2 ent = tile_ent[base + k];
-      const int cell = ent.x & 0x7fffffff;
-      const bool owner = ent.x < 0;
-      const uint32_t slots = (uint32_t)ent.y;
-      const int4 dd = cell_dofs[cell];
+      const ChunkMeta& mt = meta[(c & 1) * kChunkM + k];
+      const bool owner = mt.owner != 0;
+      const uint32_t slots = mt.slots;
+      const int4 dd = mt.dofs;
       const bool sing = in_set_m(set, dd.x) || in_set_m(set, dd.y) || in_set_m(set, dd.z) ||
                         in_set_m(set, dd.w);
-      if (!active || sing || near_test(xf, yf, zf, cellgeo[cell])) continue;
+      if (!active || sing || near_test(xf, yf, zf, mt.geo)) continue;
       const float* r = stage + (size_t)((c & 1) * kChunkM + k) * RF;
       const float4* qa = reinterpret_cast<const float4*>(r);
       const float4* qb = reinterpret_cast<const float4*>(r + 4 * NQ);
@@ -342,7 +360,8 @@ static cudaError_t launch_tile_mixed_t(int N, const double* X, const int* dnset,
                                        double* alpha_part, DevErr* err, cudaStream_t s) {
   constexpr int RF = mixed_rec_floats(Q1 * Q1);
   const size_t acc = (size_t)kColsPerTile * (kRowsPerTile + 1);
-  const size_t smem = (size_t)2 * kChunkM * RF * 4 + 4 * acc * 4 + 8 + 2 * sizeof(uint64_t);
+  const size_t smem = (size_t)2 * kChunkM * RF * 4 + 4 * acc * 4 + 16 +
+                      2 * kChunkM * sizeof(ChunkMeta) + 2 * sizeof(uint64_t);
   cudaError_t e = cudaFuncSetAttribute(k_tile_mixed<Q1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return e;
@@ -352,14 +371,18 @@ static cudaError_t launch_tile_mixed_t(int N, const double* X, const int* dnset,
   return cudaGetLastError();
 }
 
-// FP64 near field: one thread per row scans the panels, integrates those that
-// pass the near test (and are not singular) with the regular rule in FP64,
-// and adds them to the (hi, lo) entries.
-__global__ void k_near_mixed(int N, int C, const double* __restrict__ X, const int* __restrict__ dnset,
-                             const int4* __restrict__ cell_dofs, const float4* __restrict__ cellgeo,
-                             const double* __restrict__ rec64, float2* __restrict__ N2,
-                             float2* __restrict__ D2, double* __restrict__ alpha_near) {
-  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+// FP64 near field: one warp per row. The lanes test 32 panels at a time
+// against the near criterion (same test as the tile kernel); each near,
+// non-singular panel is then integrated with the regular rule in FP64, one
+// quadrature point per lane, and added to the (hi, lo) entries by lane 0 in
+// ascending panel order.
+__global__ void __launch_bounds__(256)
+    k_near_mixed(int N, int C, const double* __restrict__ X, const int* __restrict__ dnset,
+                 const int4* __restrict__ cell_dofs, const float4* __restrict__ cellgeo,
+                 const double* __restrict__ rec64, float2* __restrict__ N2,
+                 float2* __restrict__ D2, double* __restrict__ alpha_near) {
+  const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (row >= N) return;
   const double xi = X[3 * (size_t)row], yi = X[3 * (size_t)row + 1], zi = X[3 * (size_t)row + 2];
   const float xf = __double2float_rn(xi), yf = __double2float_rn(yi), zf = __double2float_rn(zi);
@@ -368,38 +391,57 @@ __global__ void k_near_mixed(int N, int C, const double* __restrict__ X, const i
   for (int k = 0; k < kMaxSet; ++k) set[k] = dnset[(size_t)row * kMaxSet + k];
   const int nq = c_qm.q1 * c_qm.q1;
   double asum = 0.0;
-  for (int c = 0; c < C; ++c) {
-    if (!near_test(xf, yf, zf, cellgeo[c])) continue;
-    const int4 d = cell_dofs[c];
-    if (in_set_m(set, d.x) || in_set_m(set, d.y) || in_set_m(set, d.z) || in_set_m(set, d.w))
-      continue;
-    const double* r = rec64 + (size_t)c * nq * 8;
-    double ln[4] = {0, 0, 0, 0}, ld[4] = {0, 0, 0, 0};
-    for (int q = 0; q < nq; ++q) {
-      const double Rx = r[8 * q] - xi, Ry = r[8 * q + 1] - yi, Rz = r[8 * q + 2] - zi;
-      const double ri = rsqrt(fma(Rx, Rx, fma(Ry, Ry, Rz * Rz)));
-      const double sq = ri * r[8 * q + 3];
-      const double dq = -fma(Rx, r[8 * q + 4], fma(Ry, r[8 * q + 5], Rz * r[8 * q + 6])) * (ri * ri * ri);
-      for (int j = 0; j < 4; ++j) {
-        ln[j] = fma(dq, c_qm.phi[q][j], ln[j]);
-        ld[j] = fma(sq, c_qm.phi[q][j], ld[j]);
+  for (int c0 = 0; c0 < C; c0 += 32) {
+    const int c = c0 + lane;
+    bool nr = false;
+    if (c < C && near_test(xf, yf, zf, cellgeo[c])) {
+      const int4 d = cell_dofs[c];
+      nr = !(in_set_m(set, d.x) || in_set_m(set, d.y) || in_set_m(set, d.z) || in_set_m(set, d.w));
+    }
+    unsigned m = __ballot_sync(0xffffffffu, nr);
+    while (m) {
+      const int b = __ffs(m) - 1;
+      m &= m - 1;
+      const int cell = c0 + b;
+      const double* r = rec64 + (size_t)cell * nq * 8;
+      double ln[4] = {0, 0, 0, 0}, ld[4] = {0, 0, 0, 0};
+      for (int q = lane; q < nq; q += 32) {
+        const double Rx = r[8 * q] - xi, Ry = r[8 * q + 1] - yi, Rz = r[8 * q + 2] - zi;
+        const double ri = rsqrt(fma(Rx, Rx, fma(Ry, Ry, Rz * Rz)));
+        const double sq = ri * r[8 * q + 3];
+        const double dq = -fma(Rx, r[8 * q + 4], fma(Ry, r[8 * q + 5], Rz * r[8 * q + 6])) * (ri * ri * ri);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          ln[j] = fma(dq, c_qm.phi[q][j], ln[j]);
+          ld[j] = fma(sq, c_qm.phi[q][j], ld[j]);
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          ln[j] += __shfl_xor_sync(0xffffffffu, ln[j], o);
+          ld[j] += __shfl_xor_sync(0xffffffffu, ld[j], o);
+        }
+      if (lane == 0) {
+        const int4 d = cell_dofs[cell];
+        const int id[4] = {d.x, d.y, d.z, d.w};
+        for (int j = 0; j < 4; ++j) {
+          const size_t o = (size_t)row * N + id[j];
+          float2 v = N2[o];
+          double s = (double)v.x + (double)v.y + ln[j];
+          float h = __double2float_rn(s);
+          N2[o] = make_float2(h, __double2float_rn(s - (double)h));
+          v = D2[o];
+          s = (double)v.x + (double)v.y + ld[j];
+          h = __double2float_rn(s);
+          D2[o] = make_float2(h, __double2float_rn(s - (double)h));
+          asum += ln[j];
+        }
       }
     }
-    const int id[4] = {d.x, d.y, d.z, d.w};
-    for (int j = 0; j < 4; ++j) {
-      const size_t o = (size_t)row * N + id[j];
-      float2 v = N2[o];
-      double s = (double)v.x + (double)v.y + ln[j];
-      float h = __double2float_rn(s);
-      N2[o] = make_float2(h, __double2float_rn(s - (double)h));
-      v = D2[o];
-      s = (double)v.x + (double)v.y + ld[j];
-      h = __double2float_rn(s);
-      D2[o] = make_float2(h, __double2float_rn(s - (double)h));
-      asum += ln[j];
-    }
   }
-  alpha_near[row] = asum;
+  if (lane == 0) alpha_near[row] = asum;
 }
 
 // FP64 vertex-singular panels, added to the (hi, lo) entries.
@@ -530,9 +572,8 @@ int assemble_mixed(wbem_context* h) {
   }
   CUM(e);
   h->stats.t_assemble_ms = tm.ms();
-  k_near_mixed<<<(N + 127) / 128, 128, 0, h->stream>>>(N, C, h->d_X, h->d_dnset, h->d_cell_dofs,
-                                                        geo, h->d_rec, h->d_N2, h->d_D2,
-                                                        h->d_alpha_near);
+  k_near_mixed<<<(unsigned)(((size_t)N * 32 + 255) / 256), 256, 0, h->stream>>>(
+      N, C, h->d_X, h->d_dnset, h->d_cell_dofs, geo, h->d_rec, h->d_N2, h->d_D2, h->d_alpha_near);
   CUM(cudaGetLastError());
   k_singular_mixed<<<(N + 63) / 64, 64, 0, h->stream>>>(N, h->d_X, h->d_dnset, h->d_sptr,
                                                          h->d_scell, h->d_cell_dofs, h->d_N2,
