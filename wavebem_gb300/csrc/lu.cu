@@ -37,13 +37,13 @@ constexpr int kNB2 = 512;  // outer block: K of the tensor-core trailing update
 // ------------------------------------------------------------------ input
 // LU input: hi part of the system operator, alpha on Neumann diagonals,
 // constrained rows replaced by e_i - sum_j c_ij e_j.
-__global__ void k_form_lu(int N, const float2* __restrict__ N2, const float2* __restrict__ D2,
+__global__ void k_form_lu(int N, int ld, const float2* __restrict__ N2, const float2* __restrict__ D2,
                           const uint8_t* __restrict__ mask, const double* __restrict__ alpha,
                           const uint8_t* __restrict__ cflag, const int* __restrict__ cptr,
                           const int* __restrict__ ccol, const double* __restrict__ cval,
                           float* __restrict__ A) {
   const int i = blockIdx.y;
-  float* ar = A + (size_t)i * N;
+  float* ar = A + (size_t)i * ld;
   if (cflag[i]) {
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < N; j += gridDim.x * blockDim.x)
       ar[j] = (j == i) ? 1.f : 0.f;
@@ -77,156 +77,168 @@ __global__ void k_lu_constraint_entries(int nrows, const int* __restrict__ crow,
 }
 
 // ------------------------------------------------------------ diagonal block
-// LU (no pivoting) of the kNB x kNB block at (k0, k0), then inv(L) (unit
-// lower) and inv(U), all register-tiled: 512 threads, thread t owns rows
-// 4*(t/16) .. +3 and columns 8*(t%16) .. +7; step k broadcasts the pivot row
-// and the multiplier column through double-buffered shared vectors.
-// Writes the factors back to A and the inverses row-major (linv, uinv) and
-// column-major (linvT, uinvT).
+// LU (no pivoting) of the kNB x kNB block at (k0, k0) and the inverses of its
+// unit-lower and upper factors, blocked by 32 inside one CTA (16 warps):
+//   per 32-block s: warp 0 factors the diagonal sub-block in registers with
+//   shuffles (one column per lane) and inverts its two triangles; 6 warps do
+//   the 32x32 triangular panel products; 9 warps the trailing 32x32 updates.
+// The 128x128 inverses are then assembled block by block
+//   Linv_ts = -Linv_tt sum_{u=s}^{t-1} L_tu Linv_us (and the mirror for U).
+// 4 x 3 + 3 barriers in total. Writes the factors back to A, the inverses
+// row-major (linv, uinv) and column-major (linvT, uinvT).
 constexpr int kDiagThreads = 512;
-__device__ __forceinline__ float sel4(const float (&v)[4][8], int i, int j) {
-  return i == 0 ? v[0][j] : i == 1 ? v[1][j] : i == 2 ? v[2][j] : v[3][j];
-}
-__device__ __forceinline__ float sel8(const float (&v)[4][8], int i, int j) {
-  float r = v[i][0];
+constexpr int kDLD = kNB + 1;
+
+// C[32x32] (ld) = sign * A[32x32] * B[32x32] (+ C if acc), one warp; lane = column.
+__device__ __forceinline__ void w_gemm_col(float* C, const float* A, const float* B, float sign,
+                                           bool acc) {
+  const int lane = threadIdx.x & 31;
+  float col[32];
 #pragma unroll
-  for (int u = 1; u < 8; ++u) r = (j == u) ? v[i][u] : r;
-  return r;
+  for (int k = 0; k < 32; ++k) col[k] = B[k * kDLD + lane];
+#pragma unroll 4
+  for (int r = 0; r < 32; ++r) {
+    float sum = 0.f;
+#pragma unroll
+    for (int k = 0; k < 32; ++k) sum = __fmaf_rn(A[r * kDLD + k], col[k], sum);
+    C[r * kDLD + lane] = acc ? __fmaf_rn(sign, sum, C[r * kDLD + lane]) : sign * sum;
+  }
 }
+// C[32x32] = A[32x32] * B[32x32] with lane = row (A read by rows, in place on A allowed).
+__device__ __forceinline__ void w_gemm_row(float* C, const float* A, const float* B) {
+  const int lane = threadIdx.x & 31;
+  float row[32];
+#pragma unroll
+  for (int k = 0; k < 32; ++k) row[k] = A[lane * kDLD + k];
+#pragma unroll 4
+  for (int c = 0; c < 32; ++c) {
+    float sum = 0.f;
+#pragma unroll
+    for (int k = 0; k < 32; ++k) sum = __fmaf_rn(row[k], B[k * kDLD + c], sum);
+    C[lane * kDLD + c] = sum;
+  }
+}
+
 __global__ void __launch_bounds__(kDiagThreads, 1)
-    k_diag_block(int N, int k0, int nb, float* __restrict__ A, float* __restrict__ linv,
+    k_diag_block(int ld, int k0, int nb, float* __restrict__ A, float* __restrict__ linv,
                  float* __restrict__ uinv, float* __restrict__ linvT, float* __restrict__ uinvT,
                  DevErr* err) {
-  __shared__ float rowb[2][kNB];
-  __shared__ float colb[2][kNB];
-  const int tid = threadIdx.x;
-  const int rb = tid >> 4, cb = tid & 15;
-  const int r0 = 4 * rb, c0 = 8 * cb;
-  float a[4][8], x[4][8];
+  extern __shared__ __align__(16) float dsm[];
+  float* sA = dsm;                // [128][129] block, becomes L\U
+  float* sLi = sA + kNB * kDLD;   // [128][129] inv(L)
+  float* sUi = sLi + kNB * kDLD;  // [128][129] inv(U)
+  __shared__ int bad;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int idx = tid; idx < kNB * kNB; idx += kDiagThreads) {
+    const int r = idx >> 7, c = idx & 127;
+    sA[r * kDLD + c] = (r < nb && c < nb) ? A[(size_t)(k0 + r) * ld + k0 + c] : (r == c ? 1.f : 0.f);
+    sLi[r * kDLD + c] = 0.f;
+    sUi[r * kDLD + c] = 0.f;
+  }
+  if (tid == 0) bad = 0;
+  __syncthreads();
+  for (int s = 0; s < 4; ++s) {
+    const int o = 32 * s;
+    if (warp == 0) {
+      // ---- LU of the diagonal 32-block, lane = column
+      float col[32];
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+      for (int r = 0; r < 32; ++r) col[r] = sA[(o + r) * kDLD + o + lane];
+      bool okp = true;
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const int r = r0 + i, c = c0 + j;
-      a[i][j] = (r < nb && c < nb) ? A[(size_t)(k0 + r) * N + k0 + c] : (r == c ? 1.f : 0.f);
-    }
-  // ---- LU
-  for (int k = 0; k < kNB; ++k) {
-    const int bsel = k & 1;
-    if (rb == (k >> 2)) {
+      for (int k = 0; k < 32; ++k) {
+        const float piv = __shfl_sync(0xffffffffu, col[k], k);
+        okp = okp && (fabsf(piv) > 0.f) && isfinite(piv);
+        const float ip = 1.0f / piv;
 #pragma unroll
-      for (int j = 0; j < 8; ++j) rowb[bsel][c0 + j] = sel4(a, k & 3, j);
+        for (int r = k + 1; r < 32; ++r) {
+          const float l = __shfl_sync(0xffffffffu, col[r], k) * ip;
+          if (lane == k) col[r] = l;
+          else if (lane > k) col[r] = __fmaf_rn(-l, col[k], col[r]);
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < 32; ++r) sA[(o + r) * kDLD + o + lane] = col[r];
+      if (!okp && lane == 0) bad = 1;
+      __syncwarp();
+      // ---- inverses of the two triangles of the 32-block, lane = column
+      float x[32];
+#pragma unroll
+      for (int r = 0; r < 32; ++r) {
+        float sum = 0.f;
+#pragma unroll
+        for (int t = 0; t < r; ++t) sum = __fmaf_rn(sA[(o + r) * kDLD + o + t], x[t], sum);
+        x[r] = (r == lane) ? 1.f : (r > lane ? -sum : 0.f);
+      }
+#pragma unroll
+      for (int r = 0; r < 32; ++r) sLi[(o + r) * kDLD + o + lane] = x[r];
+#pragma unroll
+      for (int rr = 0; rr < 32; ++rr) {
+        const int r = 31 - rr;
+        float sum = 0.f;
+#pragma unroll
+        for (int t = r + 1; t < 32; ++t) sum = __fmaf_rn(sA[(o + r) * kDLD + o + t], x[t], sum);
+        const float d = sA[(o + r) * kDLD + o + r];
+        x[r] = (r == lane) ? 1.f / d : (r < lane ? -sum / d : 0.f);
+      }
+#pragma unroll
+      for (int r = 0; r < 32; ++r) sUi[(o + r) * kDLD + o + lane] = x[r];
     }
     __syncthreads();
-    const float piv = rowb[bsel][k];
-    if (!(fabsf(piv) > 0.f) || !isfinite(piv)) {
-      if (tid == 0) dev_fail(err, WBEM_ERR_SINGULAR, 51, k0, k);
+    if (bad) {
+      if (tid == 0) dev_fail(err, WBEM_ERR_SINGULAR, 51, k0, o);
       return;  // uniform
     }
-    if (cb == (k >> 3)) {
-      const int jj = k & 7;
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        const int r = r0 + i;
-        const float l = (r > k) ? sel8(a, i, jj) / piv : 0.f;
-#pragma unroll
-        for (int j = 0; j < 8; ++j)
-          if (j == jj && r > k) a[i][j] = l;
-        colb[bsel][r] = l;
-      }
+    // ---- panels: U_st = inv(L_ss) A_st (warps 0..), L_ts = A_ts inv(U_ss) (warps 3..)
+    const int np = 3 - s;
+    if (warp < np) {
+      const int t = s + 1 + warp;
+      w_gemm_col(sA + o * kDLD + 32 * t, sLi + o * kDLD + o, sA + o * kDLD + 32 * t, 1.f, false);
+    } else if (warp >= 3 && warp < 3 + np) {
+      const int t = s + 1 + (warp - 3);
+      w_gemm_row(sA + 32 * t * kDLD + o, sA + 32 * t * kDLD + o, sUi + o * kDLD + o);
     }
     __syncthreads();
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const float l = colb[bsel][r0 + i];
-#pragma unroll
-      for (int j = 0; j < 8; ++j)
-        if (c0 + j > k) a[i][j] = __fmaf_rn(-l, rowb[bsel][c0 + j], a[i][j]);
+    // ---- trailing: A_tu -= L_ts U_su
+    if (warp < np * np) {
+      const int t = s + 1 + warp / np, u = s + 1 + warp % np;
+      w_gemm_col(sA + 32 * t * kDLD + 32 * u, sA + 32 * t * kDLD + o, sA + o * kDLD + 32 * u, -1.f,
+                 true);
     }
+    __syncthreads();
   }
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const int r = r0 + i, c = c0 + j;
-      if (r < nb && c < nb) A[(size_t)(k0 + r) * N + k0 + c] = a[i][j];
-    }
-  // ---- inv(L): forward elimination of the identity with the multipliers
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = 0; j < 8; ++j) x[i][j] = (r0 + i == c0 + j) ? 1.f : 0.f;
-  __syncthreads();
-  for (int k = 0; k < kNB; ++k) {
-    const int bsel = k & 1;
-    if (rb == (k >> 2)) {
-#pragma unroll
-      for (int j = 0; j < 8; ++j) rowb[bsel][c0 + j] = sel4(x, k & 3, j);
-    }
-    if (cb == (k >> 3)) {
-#pragma unroll
-      for (int i = 0; i < 4; ++i) colb[bsel][r0 + i] = (r0 + i > k) ? sel8(a, i, k & 7) : 0.f;
+  // ---- off-diagonal blocks of the inverses, by distance d = t - s
+  for (int d = 1; d < 4; ++d) {
+    // Linv_ts = -Linv_tt sum_u L_tu Linv_us (warps 0..3-d), staged through
+    // the upper triangle of sUi's unused block (t, s) region of sLi first
+    const int npairs = 4 - d;
+    if (warp < npairs) {
+      const int sb = warp, tb = warp + d;
+      float* T = sLi + 32 * tb * kDLD + 32 * sb;  // accumulate sum_u L_tu Linv_us
+      for (int u = sb; u < tb; ++u)
+        w_gemm_col(T, sA + 32 * tb * kDLD + 32 * u, sLi + 32 * u * kDLD + 32 * sb, 1.f, u > sb);
+      __syncwarp();
+      // T <- -Linv_tt T (lane = column)
+      w_gemm_col(T, sLi + 32 * tb * kDLD + 32 * tb, T, -1.f, false);
+    } else if (warp >= 4 && warp < 4 + npairs) {
+      // Uinv_st = -Uinv_ss sum_{u=s+1}^{t} U_su Uinv_ut
+      const int sb = warp - 4, tb = sb + d;
+      float* T = sUi + 32 * sb * kDLD + 32 * tb;
+      for (int u = sb + 1; u <= tb; ++u)
+        w_gemm_col(T, sA + 32 * sb * kDLD + 32 * u, sUi + 32 * u * kDLD + 32 * tb, 1.f, u > sb + 1);
+      __syncwarp();
+      w_gemm_col(T, sUi + 32 * sb * kDLD + 32 * sb, T, -1.f, false);
     }
     __syncthreads();
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const float l = colb[bsel][r0 + i];
-#pragma unroll
-      for (int j = 0; j < 8; ++j) x[i][j] = __fmaf_rn(-l, rowb[bsel][c0 + j], x[i][j]);
-    }
   }
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const int r = r0 + i, c = c0 + j;
-      linv[r * kNB + c] = x[i][j];
-      linvT[c * kNB + r] = x[i][j];
-    }
-  // ---- inv(U): backward elimination of the identity
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = 0; j < 8; ++j) x[i][j] = (r0 + i == c0 + j) ? 1.f : 0.f;
-  __syncthreads();
-  for (int kk = 0; kk < kNB; ++kk) {
-    const int k = kNB - 1 - kk;
-    const int bsel = kk & 1;
-    // U[k][k] and the column U[r][k], r < k
-    if (cb == (k >> 3)) {
-#pragma unroll
-      for (int i = 0; i < 4; ++i) colb[bsel][r0 + i] = (r0 + i <= k) ? sel8(a, i, k & 7) : 0.f;
-    }
-    __syncthreads();
-    const float ukk = colb[bsel][k];
-    if (rb == (k >> 2)) {
-      const int ii = k & 3;
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 8; ++j)
-          if (i == ii) x[i][j] = x[i][j] / ukk;
-#pragma unroll
-      for (int j = 0; j < 8; ++j) rowb[bsel][c0 + j] = sel4(x, ii, j);
-    }
-    __syncthreads();
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      if (r0 + i < k) {
-        const float u = colb[bsel][r0 + i];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) x[i][j] = __fmaf_rn(-u, rowb[bsel][c0 + j], x[i][j]);
-      }
-    }
+  for (int idx = tid; idx < kNB * kNB; idx += kDiagThreads) {
+    const int r = idx >> 7, c = idx & 127;
+    if (r < nb && c < nb) A[(size_t)(k0 + r) * ld + k0 + c] = sA[r * kDLD + c];
+    linv[idx] = sLi[r * kDLD + c];
+    uinv[idx] = sUi[r * kDLD + c];
+    linvT[idx] = sLi[c * kDLD + r];
+    uinvT[idx] = sUi[c * kDLD + r];
   }
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const int r = r0 + i, c = c0 + j;
-      uinv[r * kNB + c] = x[i][j];
-      uinvT[c * kNB + r] = x[i][j];
-    }
 }
 
 // ------------------------------------------------------------- panel GEMM
@@ -383,7 +395,7 @@ __global__ void __launch_bounds__(256)
 }
 
 // ------------------------------------------------------- tcgen05 BF16x3 GEMM
-constexpr int GM = 128, GN = 256, GK = 64;
+constexpr int GM = 128, GN = 128, GK = 64;
 constexpr uint32_t kStageBytes = (GM + GM + GN + GN) * GK * 2;  // Ahi Alo Bhi Blo: 96 KB
 
 __device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
@@ -418,27 +430,42 @@ __device__ __forceinline__ void umma_commit(uint64_t* bar) {
       : "memory");
 }
 
+// C tile staging: 4 sub-tiles of 128 rows x 32 FP32 columns, 128-byte
+// swizzled (16-byte chunk index XOR row % 8), loaded by TMA while the MMAs
+// run and stored back by TMA after the subtraction.
+constexpr uint32_t kCSubBytes = GM * 32 * 4;   // 16 KB
+constexpr uint32_t kCBytes = 4 * kCSubBytes;    // 64 KB (GN = 128)
+
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int y, uint32_t src) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                   map),
+               "r"(x), "r"(y), "r"(src)
+               : "memory");
+}
+
 __global__ void __launch_bounds__(128, 1)
     k_gemm_bf16x3(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
                   const __grid_constant__ CUtensorMap mBhi, const __grid_constant__ CUtensorMap mBlo,
-                  int M, int Nc, int K, float* __restrict__ Cm, int ldc, DevErr* err) {
+                  const __grid_constant__ CUtensorMap mC, int crow0, int ccol0, int K,
+                  DevErr* err) {
   extern __shared__ __align__(1024) uint8_t gsm[];
-  // 1024-byte aligned operand stages
   const uint32_t base_s = smem_u32(gsm);
   const uint32_t pad = (1024 - (base_s & 1023)) & 1023;
-  uint8_t* sm = gsm + pad;
-  uint64_t* full = reinterpret_cast<uint64_t*>(sm + 2 * kStageBytes);
+  uint8_t* sm = gsm + pad;                 // [2 stages][Ahi Alo Bhi Blo] then C
+  uint8_t* csm = sm + 2 * kStageBytes;     // 4 x 16 KB, 1024-aligned
+  uint64_t* full = reinterpret_cast<uint64_t*>(csm + kCBytes);
   uint64_t* empty = full + 2;
   uint64_t* done = full + 4;
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(full + 5);
-  int* fail_flag = reinterpret_cast<int*>(full + 6);
+  uint64_t* cbar = full + 5;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(full + 6);
+  int* fail_flag = reinterpret_cast<int*>(full + 7);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m0 = blockIdx.x * GM, n0 = blockIdx.y * GN;
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tslot)),
-                 "r"(256)
+                 "r"(GN)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -448,6 +475,7 @@ __global__ void __launch_bounds__(128, 1)
     mbar_init(&empty[0], 1);
     mbar_init(&empty[1], 1);
     mbar_init(done, 1);
+    mbar_init(cbar, 1);
     *fail_flag = 0;
     fence_mbar_init();
   }
@@ -456,11 +484,15 @@ __global__ void __launch_bounds__(128, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tslot;
   const int nk = K / GK;
-  // instruction descriptor: D f32, A/B bf16, K-major both, N = 256, M = 128
+  // instruction descriptor: D f32, A/B bf16, K-major both, N = GN, M = GM
   const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(GN >> 3) << 17) |
                          ((uint32_t)(GM >> 4) << 24);
 
   if (tid == 0) {
+    // the C tile (read-modify-write target) streams in while the MMAs run
+    mbar_arrive_expect_tx(cbar, kCBytes);
+    for (int j = 0; j < 4; ++j)
+      tma_load_2d(smem_u32(csm + j * kCSubBytes), &mC, ccol0 + n0 + 32 * j, crow0 + m0, cbar);
     auto stage_ptr = [&](int s) { return smem_u32(sm + (size_t)s * kStageBytes); };
     auto load = [&](int c) {
       const int s = c & 1;
@@ -510,11 +542,13 @@ __global__ void __launch_bounds__(128, 1)
   }
   __syncwarp();
   const bool ok_done = mbar_wait_bounded(done, 0u);
+  const bool ok_c = mbar_wait_bounded(cbar, 0u);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   __syncthreads();
-  if (ok_done && *fail_flag == 0) {
-    const int row = m0 + warp * 32 + lane;
-    float* crow = Cm + (size_t)row * ldc;
+  const bool good = ok_done && ok_c && *fail_flag == 0;
+  if (good) {
+    const int r = warp * 32 + lane;  // tile row = TMEM lane
+    const uint32_t rsw = (uint32_t)(r & 7);
     for (int cc = 0; cc < GN; cc += 16) {
       uint32_t v[16];
       const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cc;
@@ -526,37 +560,39 @@ __global__ void __launch_bounds__(128, 1)
             "=r"(v[14]), "=r"(v[15])
           : "r"(taddr));
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (row < M) {
-        const int col = n0 + cc;
-        if (col + 16 <= Nc && ((ldc & 3) == 0)) {
-          float4* p = reinterpret_cast<float4*>(crow + col);
+      uint8_t* sub = csm + (cc >> 5) * kCSubBytes + (size_t)r * 128;
 #pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            float4 o = p[u];
-            o.x -= __uint_as_float(v[4 * u + 0]);
-            o.y -= __uint_as_float(v[4 * u + 1]);
-            o.z -= __uint_as_float(v[4 * u + 2]);
-            o.w -= __uint_as_float(v[4 * u + 3]);
-            p[u] = o;
-          }
-        } else {
-#pragma unroll
-          for (int t = 0; t < 16; ++t)
-            if (col + t < Nc) crow[col + t] -= __uint_as_float(v[t]);
-        }
+      for (int u = 0; u < 4; ++u) {
+        const uint32_t chunk = (uint32_t)(((cc & 31) >> 2) + u);  // logical 16-byte chunk
+        float4* q = reinterpret_cast<float4*>(sub + ((chunk ^ rsw) << 4));
+        float4 o = *q;
+        o.x -= __uint_as_float(v[4 * u + 0]);
+        o.y -= __uint_as_float(v[4 * u + 1]);
+        o.z -= __uint_as_float(v[4 * u + 2]);
+        o.w -= __uint_as_float(v[4 * u + 3]);
+        *q = o;
       }
     }
-  } else if (!ok_done && tid == 0) {
+  } else if (tid == 0) {
     dev_fail(err, WBEM_ERR_TIMEOUT, 62, blockIdx.x, blockIdx.y);
   }
+  fence_proxy_async_smem();
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
+  if (tid == 0) {
+    if (good) {
+      for (int j = 0; j < 4; ++j)
+        tma_store_2d(&mC, ccol0 + n0 + 32 * j, crow0 + m0, smem_u32(csm + j * kCSubBytes));
+      asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+    }
+    asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+  }
   if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(GN)
                  : "memory");
 }
 
-static size_t gemm_smem() { return 2 * (size_t)kStageBytes + 1024 + 64; }
+static size_t gemm_smem() { return 2 * (size_t)kStageBytes + kCBytes + 1024 + 128; }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (the
 // library does not link libcuda directly, so it loads on hosts without a
@@ -592,10 +628,28 @@ struct GemmMaps {
   CUtensorMap Ahi, Alo, Bhi, Blo;
 };
 
-// C[M x Nc] (ldc) -= A B^T with A rows in (Ahi, Alo) [rowsA x K], B rows in
-// (Bhi, Blo) [rowsB x K], both K-major BF16.
-static cudaError_t run_gemm(const GemmMaps& mp, int M, int Nc, int K, float* Cm, int ldc,
-                            DevErr* err, cudaStream_t s) {
+// FP32 matrix (rows x cols, leading dimension ld floats, ld % 4 == 0) seen by
+// TMA in 128 x 32 boxes with 128-byte swizzle.
+static bool encode_cmap(CUtensorMap* map, const float* base, int rows, int cols, int ld) {
+  const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)ld * 4};
+  const cuuint32_t box[2] = {32u, (cuuint32_t)GM};
+  const cuuint32_t es[2] = {1, 1};
+  PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
+  if (!enc || (ld & 3)) return false;
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides, box, es,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+// C[crow0 + (0..M), ccol0 + (0..Nc)] -= A B^T, with A rows in (Ahi, Alo)
+// [rowsA x K] and B rows in (Bhi, Blo) [rowsB x K], both K-major BF16. C is
+// addressed through its tensor map; rows and columns past the map's extent are
+// neither read (zero fill) nor written (clipped), so tiles may overhang M / Nc
+// only where the region ends at the matrix edge.
+static cudaError_t run_gemm(const GemmMaps& mp, const CUtensorMap& cmap, int crow0, int ccol0, int M,
+                            int Nc, int K, DevErr* err, cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(k_gemm_bf16x3, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -604,8 +658,8 @@ static cudaError_t run_gemm(const GemmMaps& mp, int M, int Nc, int K, float* Cm,
     attr = true;
   }
   dim3 grid((M + GM - 1) / GM, (Nc + GN - 1) / GN);
-  k_gemm_bf16x3<<<grid, 128, gemm_smem(), s>>>(mp.Ahi, mp.Alo, mp.Bhi, mp.Blo, M, Nc, K, Cm, ldc,
-                                               err);
+  k_gemm_bf16x3<<<grid, 128, gemm_smem(), s>>>(mp.Ahi, mp.Alo, mp.Bhi, mp.Blo, cmap, crow0, ccol0,
+                                               K, err);
   return cudaGetLastError();
 }
 
@@ -624,7 +678,7 @@ constexpr int kTriThreads = 256;
 //       holds columns 4 l .. 4 l + 3 of each;
 //   modes 2/3 (columns of block (j, k)): thread t holds column t % 128 of rows
 //       t / 128, + 2, + 4, ...
-__device__ __forceinline__ void tri_load(float t[64], int mode, const float* __restrict__ LU, int N,
+__device__ __forceinline__ void tri_load(float t[64], int mode, const float* __restrict__ LU, int ld,
                                          int k0, int nb, int j0, int jn, bool vec4) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (mode <= 1) {
@@ -632,7 +686,7 @@ __device__ __forceinline__ void tri_load(float t[64], int mode, const float* __r
     for (int i = 0; i < 16; ++i) {
       const int r = warp * 16 + i;
       const int c = 4 * lane;
-      const float* p = LU + (size_t)(k0 + r) * N + j0 + c;
+      const float* p = LU + (size_t)(k0 + r) * ld + j0 + c;
       if (r < nb && c + 3 < jn && vec4) {
         const float4 v = __ldcs(reinterpret_cast<const float4*>(p));
         t[4 * i] = v.x; t[4 * i + 1] = v.y; t[4 * i + 2] = v.z; t[4 * i + 3] = v.w;
@@ -646,13 +700,13 @@ __device__ __forceinline__ void tri_load(float t[64], int mode, const float* __r
 #pragma unroll
     for (int i = 0; i < 64; ++i) {
       const int r = h + 2 * i;
-      t[i] = (c < nb && r < jn) ? __ldcs(LU + (size_t)(j0 + r) * N + k0 + c) : 0.f;
+      t[i] = (c < nb && r < jn) ? __ldcs(LU + (size_t)(j0 + r) * ld + k0 + c) : 0.f;
     }
   }
 }
 
 __global__ void __launch_bounds__(kTriThreads)
-    k_trsv_wave(int N, int nblk, int mode, const float* __restrict__ LU,
+    k_trsv_wave(int N, int ld, int nblk, int mode, const float* __restrict__ LU,
                 const float* __restrict__ dinv, const float* __restrict__ in,
                 float* __restrict__ out, unsigned* __restrict__ flags, unsigned epoch,
                 DevErr* err) {
@@ -666,7 +720,7 @@ __global__ void __launch_bounds__(kTriThreads)
   const bool fwd = (mode == 0 || mode == 2);
   const int k = fwd ? blockIdx.x : nblk - 1 - blockIdx.x;
   const int k0 = k * kNB, nb = min(kNB, N - k0);
-  const bool vec4 = (N & 3) == 0;
+  const bool vec4 = (ld & 3) == 0;
   const float* Dk = dinv + (size_t)k * kNB * kNB;
   for (int idx = tid; idx < kNB * kNB; idx += kTriThreads) sInv[idx] = Dk[idx];
   if (tid < kNB) acc[tid] = (tid < nb) ? in[k0 + tid] : 0.f;
@@ -675,7 +729,7 @@ __global__ void __launch_bounds__(kTriThreads)
   float t[64];
   if (jbeg != jend) {
     const int j0 = jbeg * kNB;
-    tri_load(t, mode, LU, N, k0, nb, j0, min(kNB, N - j0), vec4);
+    tri_load(t, mode, LU, ld, k0, nb, j0, min(kNB, N - j0), vec4);
   }
   __syncthreads();
   for (int j = jbeg; j != jend; j += jstep) {
@@ -718,7 +772,7 @@ __global__ void __launch_bounds__(kTriThreads)
     const int jn2 = j + jstep;
     if (jn2 != jend) {
       const int j02 = jn2 * kNB;
-      tri_load(t, mode, LU, N, k0, nb, j02, min(kNB, N - j02), vec4);
+      tri_load(t, mode, LU, ld, k0, nb, j02, min(kNB, N - j02), vec4);
     }
     __syncthreads();
     if (mode >= 2 && tid < kNB) acc[tid] -= part[tid] + part[kNB + tid];
@@ -761,6 +815,8 @@ struct LuState {
   unsigned* flags = nullptr;  // 4 x nblk publication flags
   unsigned epoch = 0;
   int N = 0;
+  int ld = 0;       // leading dimension of the LU buffer (N rounded up to 32)
+  CUtensorMap cmap; // the LU buffer as the GEMM's C operand
   GemmMaps maps;
 };
 
@@ -804,8 +860,9 @@ static int tri_sweep(wbem_context* h, LuState& L, int mode, const float* in, flo
     return fail(h, WBEM_ERR_ARG, "triangular sweep: too many blocks to be co-resident");
   const float* LU = h->d_lu;
   DevErr* err = h->d_err;
-  void* args[] = {(void*)&N, (void*)&nblk, (void*)&mode, (void*)&LU, (void*)&dinv, (void*)&in,
-                  (void*)&out, (void*)&flags, (void*)&epoch, (void*)&err};
+  const int ld = L.ld;
+  void* args[] = {(void*)&N, (void*)&ld, (void*)&nblk, (void*)&mode, (void*)&LU, (void*)&dinv,
+                  (void*)&in, (void*)&out, (void*)&flags, (void*)&epoch, (void*)&err};
   WB_CU(cudaLaunchCooperativeKernel((const void*)k_trsv_wave, dim3(nblk), dim3(kTriThreads), args,
                                     smem, h->stream));
   return WBEM_OK;
@@ -813,14 +870,18 @@ static int tri_sweep(wbem_context* h, LuState& L, int mode, const float* in, flo
 
 int factor_mixed(wbem_context* h) {
   const int N = h->N;
-  const size_t nn = (size_t)N * N;
+  const int ld = (N + 31) / 32 * 32;
+  const size_t nn = (size_t)N * ld;
   if (h->lu_state && lu_state(h).N != N) free_lu(h);
   LuState& L = lu_state(h);
   L.N = N;
+  L.ld = ld;
   if (!h->d_lu || h->lu_elems != nn) {
     WB_CHK(dev_alloc(h, &h->d_lu, nn));
     h->lu_elems = nn;
   }
+  if (!encode_cmap(&L.cmap, h->d_lu, N, N, ld))
+    return fail(h, WBEM_ERR_CUDA, "cuTensorMapEncodeTiled (LU buffer) failed");
   const int nblk = (N + kNB - 1) / kNB;
   const size_t rows = (size_t)N + GN;
   if (!L.linv) {
@@ -853,25 +914,27 @@ int factor_mixed(wbem_context* h) {
   EvTimer tm(h->stream);
   {
     dim3 g(std::min(64, (N + 255) / 256), N);
-    k_form_lu<<<g, 256, 0, h->stream>>>(N, h->d_N2, h->d_D2, h->d_mask, h->d_alpha, h->d_cflag,
+    k_form_lu<<<g, 256, 0, h->stream>>>(N, ld, h->d_N2, h->d_D2, h->d_mask, h->d_alpha, h->d_cflag,
                                         h->d_cptr_full, h->d_ccol_full, h->d_cval_full, h->d_lu);
     WB_CU(cudaGetLastError());
     if (h->n_crows > 0) {
       k_lu_constraint_entries<<<(h->n_crows + 127) / 128, 128, 0, h->stream>>>(
-          h->n_crows, h->d_crow, h->d_cptr, h->d_ccol, h->d_cval, N, h->d_lu);
+          h->n_crows, h->d_crow, h->d_cptr, h->d_ccol, h->d_cval, ld, h->d_lu);
       WB_CU(cudaGetLastError());
     }
   }
   h->stats.t_system_ms = tm.ms();
   float* A = h->d_lu;
   const SplitOut none{nullptr, nullptr, 0, 0, 0};
+  const size_t kDiagSmem = (size_t)3 * kNB * kDLD * sizeof(float);
+  WB_CU(cudaFuncSetAttribute(k_diag_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDiagSmem));
   for (int p0 = 0; p0 < N; p0 += kNB2) {
     const int p1 = std::min(N, p0 + kNB2);
     // ---- factor the panel columns [p0, p1): 128-wide blocks, right-looking
     for (int k0 = p0; k0 < p1; k0 += kNB) {
       const int k = k0 / kNB, nb = std::min(kNB, N - k0), k1 = k0 + nb;
       const size_t bo = (size_t)k * kNB * kNB;
-      k_diag_block<<<1, kDiagThreads, 0, h->stream>>>(N, k0, nb, A, L.linv + bo, L.uinv + bo,
+      k_diag_block<<<1, kDiagThreads, kDiagSmem, h->stream>>>(ld, k0, nb, A, L.linv + bo, L.uinv + bo,
                                                       L.linvT + bo, L.uinvT + bo, h->d_err);
       h->launches++;
       if (k1 >= N) break;
@@ -881,15 +944,15 @@ int factor_mixed(wbem_context* h) {
       const SplitOut L21{b2, b2 + rows * kNB2, p1, kNB2, k0 - p0};
       // column panel (full height), inner split + outer L21 split
       dim3 gc(2, (m + 63) / 64);
-      k_panel_gemm<<<gc, 256, 0, h->stream>>>(N, 1, k0, k1, m, 0, 0, A, L.uinv + bo, Lin,
+      k_panel_gemm<<<gc, 256, 0, h->stream>>>(ld, 1, k0, k1, m, 0, 0, A, L.uinv + bo, Lin,
                                               p1 < N ? L21 : none);
       h->launches++;
       if (k1 < p1) {
         const int w = p1 - k1;
         dim3 gr((w + 63) / 64, 2);
-        k_panel_gemm<<<gr, 256, 0, h->stream>>>(N, 0, k0, 0, 0, k1, w, A, L.linv + bo, Uin, none);
+        k_panel_gemm<<<gr, 256, 0, h->stream>>>(ld, 0, k0, 0, 0, k1, w, A, L.linv + bo, Uin, none);
         WB_CU(cudaGetLastError());
-        WB_CU(run_gemm(L.maps, m, w, kNB, A + (size_t)k1 * N + k1, N, h->d_err, h->stream));
+        WB_CU(run_gemm(L.maps, L.cmap, k1, k1, m, w, kNB, h->d_err, h->stream));
         h->launches += 2;
       }
       WB_CU(cudaGetLastError());
@@ -902,19 +965,19 @@ int factor_mixed(wbem_context* h) {
       const size_t bo = (size_t)k * kNB * kNB;
       if (k0 > p0) {
         dim3 gu((n + 63) / 64, 2);
-        k_rowpanel_update<<<gu, 256, 0, h->stream>>>(N, k0 - p0, A + (size_t)k0 * N + p0,
-                                                     A + (size_t)p0 * N + p1,
-                                                     A + (size_t)k0 * N + p1, n);
+        k_rowpanel_update<<<gu, 256, 0, h->stream>>>(ld, k0 - p0, A + (size_t)k0 * ld + p0,
+                                                     A + (size_t)p0 * ld + p1,
+                                                     A + (size_t)k0 * ld + p1, n);
         h->launches++;
       }
       const SplitOut U12{b2 + 2 * rows * kNB2, b2 + 3 * rows * kNB2, p1, kNB2, k0 - p0};
       dim3 gr((n + 63) / 64, 2);
-      k_panel_gemm<<<gr, 256, 0, h->stream>>>(N, 0, k0, 0, 0, p1, n, A, L.linv + bo, U12, none);
+      k_panel_gemm<<<gr, 256, 0, h->stream>>>(ld, 0, k0, 0, 0, p1, n, A, L.linv + bo, U12, none);
       h->launches++;
       WB_CU(cudaGetLastError());
     }
     // ---- trailing update A22 -= L21 U12 on the tensor cores (K = 512)
-    WB_CU(run_gemm(L.maps2, n, n, p1 - p0, A + (size_t)p1 * N + p1, N, h->d_err, h->stream));
+    WB_CU(run_gemm(L.maps2, L.cmap, p1, p1, n, n, p1 - p0, h->d_err, h->stream));
     h->launches++;
   }
   WB_CHK(check_device_error(h, "LU factorisation"));
@@ -977,17 +1040,31 @@ extern "C" int wbem_test_gemm_bf16x3(int M, int Nc, int K, const float* dA, cons
   if (!encode_map(&mp.Ahi, Ahi, rA, K, GM) || !encode_map(&mp.Alo, Alo, rA, K, GM) ||
       !encode_map(&mp.Bhi, Bhi, rB, K, GN) || !encode_map(&mp.Blo, Blo, rB, K, GN))
     st = WBEM_ERR_CUDA;
+  // C through a padded copy (TMA needs 16-byte aligned row strides)
+  const int ldc = (Nc + 31) / 32 * 32;
+  float* Cp = nullptr;
+  if (st == WBEM_OK && cudaMalloc(&Cp, sizeof(float) * (size_t)M * ldc) != cudaSuccess) st = WBEM_ERR_NOMEM;
+  CUtensorMap cmap;
+  if (st == WBEM_OK) {
+    cudaMemcpy2D(Cp, sizeof(float) * ldc, dC, sizeof(float) * Nc, sizeof(float) * Nc, M,
+                 cudaMemcpyDeviceToDevice);
+    if (!encode_cmap(&cmap, Cp, M, Nc, ldc)) st = WBEM_ERR_CUDA;
+  }
   DevErr* err = nullptr;
   if (st == WBEM_OK && cudaMalloc(&err, sizeof(DevErr)) != cudaSuccess) st = WBEM_ERR_NOMEM;
   if (st == WBEM_OK) {
     cudaMemset(err, 0, sizeof(DevErr));
-    if (run_gemm(mp, M, Nc, K, dC, Nc, err, 0) != cudaSuccess) st = WBEM_ERR_CUDA;
+    if (run_gemm(mp, cmap, 0, 0, M, Nc, K, err, 0) != cudaSuccess) st = WBEM_ERR_CUDA;
     if (cudaDeviceSynchronize() != cudaSuccess) st = WBEM_ERR_CUDA;
     DevErr de{};
     cudaMemcpy(&de, err, sizeof de, cudaMemcpyDeviceToHost);
     if (st == WBEM_OK && de.code) st = de.code;
+    if (st == WBEM_OK)
+      cudaMemcpy2D(dC, sizeof(float) * Nc, Cp, sizeof(float) * ldc, sizeof(float) * Nc, M,
+                   cudaMemcpyDeviceToDevice);
   }
   if (err) cudaFree(err);
+  if (Cp) cudaFree(Cp);
   cudaFree(buf);
   return st;
 }

@@ -281,43 +281,55 @@ __global__ void __launch_bounds__(kRowsPerTile)
       gR.hi = -gR.hi;
       gR.lo = -gR.lo;
       // ---- per-point differences in FP32
+      // with num = rc^2 - rq^2 = -(2 R_c.delta + |delta|^2):
+      //   rc - rq = num / (rc + rq),  1/rq - 1/rc = (rc - rq) / (rq rc),
+      //   (R.n)(-1/r^3) - (R_c.nu)(-1/rc^3)
+      //     = rq^-3 [ (rc - rq)(rc^2 + rc rq + rq^2) (-(R_c.nu) / rc^3) - (R_c.(n - nu) + delta.n) ]
       const float Rcx = R[0].hi, Rcy = R[1].hi, Rcz = R[2].hi;
       const float rcinv = rinv.hi;
-      const float rc = r2.hi * rcinv;
       const float rc2 = r2.hi;
-      const float rcinv3 = ri3.hi;
-      const float Rnf = Rn.hi;
+      const float rc = rc2 * rcinv;
+      const float K1 = -Rn.hi * ri3.hi;
       float ls0 = 0.f, ls1 = 0.f, ls2 = 0.f, ls3 = 0.f, ln0 = 0.f, ln1 = 0.f, ln2 = 0.f, ln3 = 0.f;
-      float fnsum = 0.f;
-#pragma unroll 4
-      for (int q = 0; q < NQ; ++q) {
-        const float4 A = qa[q];
-        const float4 B = qb[q];
-        const float J = qj[q];
-        const float Rx = Rcx + A.x, Ry = Rcy + A.y, Rz = Rcz + A.z;
-        const float rq2 = __fmaf_rn(Rx, Rx, __fmaf_rn(Ry, Ry, Rz * Rz));
-        const float rqinv = rsqrtf(rq2);
-        const float rq = rq2 * rqinv;
-        const float Rd = __fmaf_rn(Rcx, A.x, __fmaf_rn(Rcy, A.y, Rcz * A.z));
-        const float num = -__fmaf_rn(2.f, Rd, A.w);
-        const float dr = __fdividef(num, rc + rq);
-        const float ds = dr * rqinv * rcinv;
-        const float rqinv3 = rqinv * rqinv * rqinv;
-        const float tsum = __fmaf_rn(rc, rq, rc2) + rq2;
-        const float dg = -(dr * tsum) * rqinv3 * rcinv3;
-        const float t2 = __fmaf_rn(Rcx, B.x, __fmaf_rn(Rcy, B.y, __fmaf_rn(Rcz, B.z, B.w)));
-        const float ddn = __fmaf_rn(Rnf, dg, -t2 * rqinv3);
-        const float fs = ds * J, fn = ddn * J;
-        fnsum += fn;
-        ls0 = __fmaf_rn(fs, c_qm.phif[q][0], ls0);
-        ls1 = __fmaf_rn(fs, c_qm.phif[q][1], ls1);
-        ls2 = __fmaf_rn(fs, c_qm.phif[q][2], ls2);
-        ls3 = __fmaf_rn(fs, c_qm.phif[q][3], ls3);
-        ln0 = __fmaf_rn(fn, c_qm.phif[q][0], ln0);
-        ln1 = __fmaf_rn(fn, c_qm.phif[q][1], ln1);
-        ln2 = __fmaf_rn(fn, c_qm.phif[q][2], ln2);
-        ln3 = __fmaf_rn(fn, c_qm.phif[q][3], ln3);
+#pragma unroll
+      for (int bq = 0; bq < Q1; ++bq) {
+        // tensor-product accumulation: row sums over xi, then the two eta weights
+        float st = 0.f, s1 = 0.f, nt = 0.f, n1 = 0.f;
+#pragma unroll
+        for (int aq = 0; aq < Q1; ++aq) {
+          const int q = aq + Q1 * bq;
+          const float4 A = qa[q];
+          const float4 B = qb[q];
+          const float J = qj[q];
+          const float Rd = __fmaf_rn(Rcx, A.x, __fmaf_rn(Rcy, A.y, Rcz * A.z));
+          const float num = -__fmaf_rn(2.f, Rd, A.w);
+          const float rq2 = rc2 - num;
+          const float rqinv = rsqrtf(rq2);
+          const float rq = rq2 * rqinv;
+          const float dr = __fdividef(num, rc + rq);
+          const float fs = dr * (rqinv * rcinv) * J;
+          const float rqinv3 = rqinv * rqinv * rqinv;
+          const float tsum = __fmaf_rn(rc, rq, rc2) + rq2;
+          const float t2 = __fmaf_rn(Rcx, B.x, __fmaf_rn(Rcy, B.y, __fmaf_rn(Rcz, B.z, B.w)));
+          const float fn = rqinv3 * __fmaf_rn(dr * tsum, K1, -t2) * J;
+          const float xa = c_qm.gpf[q][0];
+          st += fs;
+          s1 = __fmaf_rn(fs, xa, s1);
+          nt += fn;
+          n1 = __fmaf_rn(fn, xa, n1);
+        }
+        const float eb = c_qm.gpf[Q1 * bq][1];
+        const float s0 = st - s1, n0 = nt - n1;
+        ls0 = __fmaf_rn(s0, 1.f - eb, ls0);
+        ls1 = __fmaf_rn(s1, 1.f - eb, ls1);
+        ls2 = __fmaf_rn(s0, eb, ls2);
+        ls3 = __fmaf_rn(s1, eb, ls3);
+        ln0 = __fmaf_rn(n0, 1.f - eb, ln0);
+        ln1 = __fmaf_rn(n1, 1.f - eb, ln1);
+        ln2 = __fmaf_rn(n0, eb, ln2);
+        ln3 = __fmaf_rn(n1, eb, ln3);
       }
+      const float fnsum = (ln0 + ln1) + (ln2 + ln3);
       const float lsv[4] = {ls0, ls1, ls2, ls3}, lnv[4] = {ln0, ln1, ln2, ln3};
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
