@@ -150,8 +150,10 @@ __global__ void __launch_bounds__(kDiagThreads, 1)
         const float piv = __shfl_sync(0xffffffffu, col[k], k);
         okp = okp && (fabsf(piv) > 0.f) && isfinite(piv);
         const float ip = 1.0f / piv;
+        // constant trip count, so both loops unroll and col[] stays in registers
 #pragma unroll
-        for (int r = k + 1; r < 32; ++r) {
+        for (int r = 1; r < 32; ++r) {
+          if (r <= k) continue;
           const float l = __shfl_sync(0xffffffffu, col[r], k) * ip;
           if (lane == k) col[r] = l;
           else if (lane > k) col[r] = __fmaf_rn(-l, col[k], col[r]);
@@ -446,7 +448,7 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int 
 __global__ void __launch_bounds__(128, 1)
     k_gemm_bf16x3(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
                   const __grid_constant__ CUtensorMap mBhi, const __grid_constant__ CUtensorMap mBlo,
-                  const __grid_constant__ CUtensorMap mC, int crow0, int ccol0, int K,
+                  const __grid_constant__ CUtensorMap mC, int crow0, int ccol0, int brow0, int K,
                   DevErr* err) {
   extern __shared__ __align__(1024) uint8_t gsm[];
   const uint32_t base_s = smem_u32(gsm);
@@ -500,8 +502,8 @@ __global__ void __launch_bounds__(128, 1)
       mbar_arrive_expect_tx(&full[s], kStageBytes);
       tma_load_2d(st, &mAhi, c * GK, m0, &full[s]);
       tma_load_2d(st + GM * GK * 2, &mAlo, c * GK, m0, &full[s]);
-      tma_load_2d(st + 2 * GM * GK * 2, &mBhi, c * GK, n0, &full[s]);
-      tma_load_2d(st + 2 * GM * GK * 2 + GN * GK * 2, &mBlo, c * GK, n0, &full[s]);
+      tma_load_2d(st + 2 * GM * GK * 2, &mBhi, c * GK, brow0 + n0, &full[s]);
+      tma_load_2d(st + 2 * GM * GK * 2 + GN * GK * 2, &mBlo, c * GK, brow0 + n0, &full[s]);
     };
     bool ok = true;
     load(0);
@@ -644,12 +646,13 @@ static bool encode_cmap(CUtensorMap* map, const float* base, int rows, int cols,
 }
 
 // C[crow0 + (0..M), ccol0 + (0..Nc)] -= A B^T, with A rows in (Ahi, Alo)
-// [rowsA x K] and B rows in (Bhi, Blo) [rowsB x K], both K-major BF16. C is
+// [rowsA x K] and B rows in (Bhi, Blo) [rowsB x K], both K-major BF16; C
+// column ccol0 + j pairs with B row brow0 + j. C is
 // addressed through its tensor map; rows and columns past the map's extent are
 // neither read (zero fill) nor written (clipped), so tiles may overhang M / Nc
 // only where the region ends at the matrix edge.
-static cudaError_t run_gemm(const GemmMaps& mp, const CUtensorMap& cmap, int crow0, int ccol0, int M,
-                            int Nc, int K, DevErr* err, cudaStream_t s) {
+static cudaError_t run_gemm(const GemmMaps& mp, const CUtensorMap& cmap, int crow0, int ccol0,
+                            int brow0, int M, int Nc, int K, DevErr* err, cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(k_gemm_bf16x3, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -659,7 +662,7 @@ static cudaError_t run_gemm(const GemmMaps& mp, const CUtensorMap& cmap, int cro
   }
   dim3 grid((M + GM - 1) / GM, (Nc + GN - 1) / GN);
   k_gemm_bf16x3<<<grid, 128, gemm_smem(), s>>>(mp.Ahi, mp.Alo, mp.Bhi, mp.Blo, cmap, crow0, ccol0,
-                                               K, err);
+                                               brow0, K, err);
   return cudaGetLastError();
 }
 
@@ -809,8 +812,16 @@ struct LuState {
   float* linvT = nullptr;  // column-major copies
   float* uinvT = nullptr;
   uint16_t* split = nullptr;  // inner (K = 128) Lhi, Llo, Uhi, Ulo: each (N + GN) x kNB
-  uint16_t* split2 = nullptr; // outer (K = kNB2) L21hi, L21lo, U12Thi, U12Tlo
-  GemmMaps maps2;
+  // outer (K = kNB2) L21hi, L21lo, U12Thi, U12Tlo, two sets: the trailing
+  // update of outer panel P reads set P % 2 while panel P + 1 writes the other
+  uint16_t* split2[2] = {nullptr, nullptr};
+  GemmMaps maps2[2];
+  // look-ahead: panel work and the next panel's columns of the trailing update
+  // on a high-priority stream, the rest of the trailing update on a
+  // low-priority one
+  cudaStream_t s_panel = nullptr;
+  cudaStream_t s_trail = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_row = nullptr, ev_trail = nullptr, ev_join = nullptr;
   float* w = nullptr;         // 2 x N ping-pong vectors
   unsigned* flags = nullptr;  // 4 x nblk publication flags
   unsigned epoch = 0;
@@ -833,7 +844,12 @@ void free_lu(wbem_context* h) {
   if (L.linvT) cudaFree(L.linvT);
   if (L.uinvT) cudaFree(L.uinvT);
   if (L.split) cudaFree(L.split);
-  if (L.split2) cudaFree(L.split2);
+  for (int b = 0; b < 2; ++b)
+    if (L.split2[b]) cudaFree(L.split2[b]);
+  if (L.s_panel) cudaStreamDestroy(L.s_panel);
+  if (L.s_trail) cudaStreamDestroy(L.s_trail);
+  for (cudaEvent_t e : {L.ev_fork, L.ev_row, L.ev_trail, L.ev_join})
+    if (e) cudaEventDestroy(e);
   if (L.w) cudaFree(L.w);
   if (L.flags) cudaFree(L.flags);
   delete &L;
@@ -890,27 +906,37 @@ int factor_mixed(wbem_context* h) {
     WB_CHK(dev_alloc(h, &L.linvT, (size_t)nblk * kNB * kNB));
     WB_CHK(dev_alloc(h, &L.uinvT, (size_t)nblk * kNB * kNB));
     WB_CHK(dev_alloc(h, &L.split, (size_t)4 * rows * kNB));
-    WB_CHK(dev_alloc(h, &L.split2, (size_t)4 * rows * kNB2));
+    WB_CHK(dev_alloc(h, &L.split2[0], (size_t)4 * rows * kNB2));
+    WB_CHK(dev_alloc(h, &L.split2[1], (size_t)4 * rows * kNB2));
     WB_CHK(dev_alloc(h, &L.w, (size_t)2 * N));
     WB_CHK(dev_alloc(h, &L.flags, (size_t)4 * nblk));
     WB_CU(cudaMemsetAsync(L.flags, 0, sizeof(unsigned) * 4 * nblk, h->stream));
     WB_CU(cudaMemsetAsync(L.split, 0, sizeof(uint16_t) * 4 * rows * kNB, h->stream));
-    WB_CU(cudaMemsetAsync(L.split2, 0, sizeof(uint16_t) * 4 * rows * kNB2, h->stream));
     L.epoch = 0;
     uint16_t* b1 = L.split;
-    uint16_t* b2 = L.split2;
     if (!encode_map(&L.maps.Ahi, b1, (int)rows, kNB, GM) ||
         !encode_map(&L.maps.Alo, b1 + rows * kNB, (int)rows, kNB, GM) ||
         !encode_map(&L.maps.Bhi, b1 + 2 * rows * kNB, (int)rows, kNB, GN) ||
-        !encode_map(&L.maps.Blo, b1 + 3 * rows * kNB, (int)rows, kNB, GN) ||
-        !encode_map(&L.maps2.Ahi, b2, (int)rows, kNB2, GM) ||
-        !encode_map(&L.maps2.Alo, b2 + rows * kNB2, (int)rows, kNB2, GM) ||
-        !encode_map(&L.maps2.Bhi, b2 + 2 * rows * kNB2, (int)rows, kNB2, GN) ||
-        !encode_map(&L.maps2.Blo, b2 + 3 * rows * kNB2, (int)rows, kNB2, GN))
+        !encode_map(&L.maps.Blo, b1 + 3 * rows * kNB, (int)rows, kNB, GN))
       return fail(h, WBEM_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+    for (int b = 0; b < 2; ++b) {
+      uint16_t* b2 = L.split2[b];
+      WB_CU(cudaMemsetAsync(b2, 0, sizeof(uint16_t) * 4 * rows * kNB2, h->stream));
+      GemmMaps& m2 = L.maps2[b];
+      if (!encode_map(&m2.Ahi, b2, (int)rows, kNB2, GM) ||
+          !encode_map(&m2.Alo, b2 + rows * kNB2, (int)rows, kNB2, GM) ||
+          !encode_map(&m2.Bhi, b2 + 2 * rows * kNB2, (int)rows, kNB2, GN) ||
+          !encode_map(&m2.Blo, b2 + 3 * rows * kNB2, (int)rows, kNB2, GN))
+        return fail(h, WBEM_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+    }
+    int lo = 0, hi = 0;
+    WB_CU(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    WB_CU(cudaStreamCreateWithPriority(&L.s_panel, cudaStreamNonBlocking, hi));
+    WB_CU(cudaStreamCreateWithPriority(&L.s_trail, cudaStreamNonBlocking, lo));
+    for (cudaEvent_t* e : {&L.ev_fork, &L.ev_row, &L.ev_trail, &L.ev_join})
+      WB_CU(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
   }
   uint16_t* b1 = L.split;
-  uint16_t* b2 = L.split2;
   EvTimer tm(h->stream);
   {
     dim3 g(std::min(64, (N + 255) / 256), N);
@@ -928,14 +954,29 @@ int factor_mixed(wbem_context* h) {
   const SplitOut none{nullptr, nullptr, 0, 0, 0};
   const size_t kDiagSmem = (size_t)3 * kNB * kDLD * sizeof(float);
   WB_CU(cudaFuncSetAttribute(k_diag_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDiagSmem));
+  // Right-looking LU over outer panels P = [p0, p1) of kNB2 columns, with
+  // look-ahead. On s_panel: the column work of P (diagonal blocks, column
+  // panels, inner updates; it touches columns [p0, p1) only), then U12 of P
+  // (rows [p0, p1), columns [p1, N)), then the trailing update of P's
+  // successor's columns [p1, p2). On s_trail: the trailing update of the
+  // remaining columns [p2, N), which overlaps the column work of P + 1.
+  // Ordering: U12 of P waits for the trailing update of P - 1 (same rows);
+  // the trailing update of P on s_trail waits for U12 of P.
+  cudaStream_t sp = L.s_panel, st = L.s_trail;
+  WB_CU(cudaEventRecord(L.ev_fork, h->stream));
+  WB_CU(cudaStreamWaitEvent(sp, L.ev_fork, 0));
+  WB_CU(cudaStreamWaitEvent(st, L.ev_fork, 0));
+  bool trail_pending = false;  // a trailing update was queued on s_trail
   for (int p0 = 0; p0 < N; p0 += kNB2) {
     const int p1 = std::min(N, p0 + kNB2);
-    // ---- factor the panel columns [p0, p1): 128-wide blocks, right-looking
+    const int buf = (p0 / kNB2) & 1;
+    uint16_t* b2 = L.split2[buf];
+    // ---- column work of the panel: 128-wide blocks, right-looking
     for (int k0 = p0; k0 < p1; k0 += kNB) {
       const int k = k0 / kNB, nb = std::min(kNB, N - k0), k1 = k0 + nb;
       const size_t bo = (size_t)k * kNB * kNB;
-      k_diag_block<<<1, kDiagThreads, kDiagSmem, h->stream>>>(ld, k0, nb, A, L.linv + bo, L.uinv + bo,
-                                                      L.linvT + bo, L.uinvT + bo, h->d_err);
+      k_diag_block<<<1, kDiagThreads, kDiagSmem, sp>>>(ld, k0, nb, A, L.linv + bo, L.uinv + bo,
+                                                       L.linvT + bo, L.uinvT + bo, h->d_err);
       h->launches++;
       if (k1 >= N) break;
       const int m = N - k1;
@@ -944,42 +985,58 @@ int factor_mixed(wbem_context* h) {
       const SplitOut L21{b2, b2 + rows * kNB2, p1, kNB2, k0 - p0};
       // column panel (full height), inner split + outer L21 split
       dim3 gc(2, (m + 63) / 64);
-      k_panel_gemm<<<gc, 256, 0, h->stream>>>(ld, 1, k0, k1, m, 0, 0, A, L.uinv + bo, Lin,
-                                              p1 < N ? L21 : none);
+      k_panel_gemm<<<gc, 256, 0, sp>>>(ld, 1, k0, k1, m, 0, 0, A, L.uinv + bo, Lin,
+                                       p1 < N ? L21 : none);
       h->launches++;
       if (k1 < p1) {
         const int w = p1 - k1;
         dim3 gr((w + 63) / 64, 2);
-        k_panel_gemm<<<gr, 256, 0, h->stream>>>(ld, 0, k0, 0, 0, k1, w, A, L.linv + bo, Uin, none);
+        k_panel_gemm<<<gr, 256, 0, sp>>>(ld, 0, k0, 0, 0, k1, w, A, L.linv + bo, Uin, none);
         WB_CU(cudaGetLastError());
-        WB_CU(run_gemm(L.maps, L.cmap, k1, k1, m, w, kNB, h->d_err, h->stream));
+        WB_CU(run_gemm(L.maps, L.cmap, k1, k1, 0, m, w, kNB, h->d_err, sp));
         h->launches += 2;
       }
       WB_CU(cudaGetLastError());
     }
     if (p1 >= N) break;
-    // ---- row panel U12 = inv(L11) A12, one 128-block row at a time
+    // ---- row panel U12 = inv(L11) A12, one 128-block row at a time, after
+    // the previous trailing update has finished with these rows
+    if (trail_pending) WB_CU(cudaStreamWaitEvent(sp, L.ev_trail, 0));
     const int n = N - p1;
     for (int k0 = p0; k0 < p1; k0 += kNB) {
       const int k = k0 / kNB;
       const size_t bo = (size_t)k * kNB * kNB;
       if (k0 > p0) {
         dim3 gu((n + 63) / 64, 2);
-        k_rowpanel_update<<<gu, 256, 0, h->stream>>>(ld, k0 - p0, A + (size_t)k0 * ld + p0,
-                                                     A + (size_t)p0 * ld + p1,
-                                                     A + (size_t)k0 * ld + p1, n);
+        k_rowpanel_update<<<gu, 256, 0, sp>>>(ld, k0 - p0, A + (size_t)k0 * ld + p0,
+                                              A + (size_t)p0 * ld + p1, A + (size_t)k0 * ld + p1, n);
         h->launches++;
       }
       const SplitOut U12{b2 + 2 * rows * kNB2, b2 + 3 * rows * kNB2, p1, kNB2, k0 - p0};
       dim3 gr((n + 63) / 64, 2);
-      k_panel_gemm<<<gr, 256, 0, h->stream>>>(ld, 0, k0, 0, 0, p1, n, A, L.linv + bo, U12, none);
+      k_panel_gemm<<<gr, 256, 0, sp>>>(ld, 0, k0, 0, 0, p1, n, A, L.linv + bo, U12, none);
       h->launches++;
       WB_CU(cudaGetLastError());
     }
-    // ---- trailing update A22 -= L21 U12 on the tensor cores (K = 512)
-    WB_CU(run_gemm(L.maps2, L.cmap, p1, p1, n, n, p1 - p0, h->d_err, h->stream));
+    // ---- trailing update A22 -= L21 U12 on the tensor cores (K = kNB2):
+    // the next panel's columns on s_panel, the rest on s_trail
+    const int p2 = std::min(N, p1 + kNB2);
+    WB_CU(run_gemm(L.maps2[buf], L.cmap, p1, p1, 0, n, p2 - p1, p1 - p0, h->d_err, sp));
     h->launches++;
+    if (p2 < N) {
+      WB_CU(cudaEventRecord(L.ev_row, sp));
+      WB_CU(cudaStreamWaitEvent(st, L.ev_row, 0));
+      WB_CU(run_gemm(L.maps2[buf], L.cmap, p1, p2, p2 - p1, n, N - p2, p1 - p0, h->d_err, st));
+      WB_CU(cudaEventRecord(L.ev_trail, st));
+      trail_pending = true;
+      h->launches++;
+    }
   }
+  // join both streams back into the handle's stream
+  WB_CU(cudaEventRecord(L.ev_join, sp));
+  WB_CU(cudaStreamWaitEvent(h->stream, L.ev_join, 0));
+  WB_CU(cudaEventRecord(L.ev_join, st));
+  WB_CU(cudaStreamWaitEvent(h->stream, L.ev_join, 0));
   WB_CHK(check_device_error(h, "LU factorisation"));
   h->stats.t_factor_ms = tm.ms();
   return WBEM_OK;
@@ -1054,7 +1111,7 @@ extern "C" int wbem_test_gemm_bf16x3(int M, int Nc, int K, const float* dA, cons
   if (st == WBEM_OK && cudaMalloc(&err, sizeof(DevErr)) != cudaSuccess) st = WBEM_ERR_NOMEM;
   if (st == WBEM_OK) {
     cudaMemset(err, 0, sizeof(DevErr));
-    if (run_gemm(mp, cmap, 0, 0, M, Nc, K, err, 0) != cudaSuccess) st = WBEM_ERR_CUDA;
+    if (run_gemm(mp, cmap, 0, 0, 0, M, Nc, K, err, 0) != cudaSuccess) st = WBEM_ERR_CUDA;
     if (cudaDeviceSynchronize() != cudaSuccess) st = WBEM_ERR_CUDA;
     DevErr de{};
     cudaMemcpy(&de, err, sizeof de, cudaMemcpyDeviceToHost);

@@ -36,7 +36,8 @@ from .bem_problem import PREC_FP64, PREC_MIXED, BEMProblem
 
 
 class FreeSurfaceStandIn:
-    def __init__(self, n=12000, precision=PREC_MIXED, U=1.0, g=None, Fr=0.316, seed=4):
+    def __init__(self, n=12000, precision=PREC_MIXED, U=1.0, g=None, Fr=0.316, seed=4,
+                 amplitude=1e-3):
         self.m = M.wigley_mesh(n)
         m = self.m
         self.ptr, self.idx = M.double_nodes(m.X, m.cells)
@@ -53,7 +54,7 @@ class FreeSurfaceStandIn:
             for j in self.idx[self.ptr[i]:self.ptr[i + 1]]:
                 self.owner.setdefault(int(j), int(i))
         self.owner_of_moving = np.array([self.owner[int(j)] for j in self.moving])
-        self.b0 = M.wigley_bc(m, seed=seed)                 # Neumann data elsewhere
+        self.b0 = amplitude * M.wigley_bc(m, seed=seed)     # Neumann data elsewhere
         self.hull = np.nonzero(m.face == M.HULL)[0].astype(np.int32)
         # free surface patch is the first patch: (nx+1) x (ny+1) nodes, x fastest
         nxl, nxh, nxr, ny, nzh, nzb = m.info["resolution"]
@@ -130,6 +131,7 @@ class FreeSurfaceStandIn:
         y = np.zeros(2 * nF)
         hist = [y.copy()]
         step_times = []
+        newton_res = []
         t_start = time.perf_counter()
         for n in range(steps):
             ts = time.perf_counter()
@@ -140,10 +142,11 @@ class FreeSurfaceStandIn:
                 base = (4.0 * hist[-1] - hist[-2]) / 3.0
                 pred = 2.0 * hist[-1] - hist[-2]
             z = pred.copy()
-            for it in range(max_newton):
+            for it in range(max_newton + 1):
                 G = z - base - a0 * dt * self.rhs(z, assemble=True)
                 gn = np.linalg.norm(G)
-                if gn <= newton_tol * max(1.0, np.linalg.norm(z)):
+                if gn <= newton_tol * max(1.0, np.linalg.norm(z)) or it == max_newton:
+                    newton_res.append(gn / max(1.0, np.linalg.norm(z)))
                     break
                 op = LinearOperator((2 * nF, 2 * nF), matvec=lambda v: v - a0 * dt * self.jac_vec(v),
                                     dtype=np.float64)
@@ -163,7 +166,8 @@ class FreeSurfaceStandIn:
                 "per_step_s": total / steps, "step_s_median": float(np.median(step_times)),
                 "bem_fraction": self.t_bem / total, "assemblies": self.n_assemble,
                 "solves": self.n_solve, "final_Fx": F,
-                "max_eta": float(np.abs(y[:nF]).max())}
+                "max_eta": float(np.abs(y[:nF]).max()),
+                "newton_residual_max": float(max(newton_res)), "final_state": y}
 
 
 def main():
@@ -175,6 +179,8 @@ def main():
     out = {}
     for name, prec in (("mixed", PREC_MIXED), ("fp64", PREC_FP64)):
         out[name] = FreeSurfaceStandIn(args.n, precision=prec).run(args.steps, args.dt)
+    ym, y64 = out["mixed"].pop("final_state"), out["fp64"].pop("final_state")
+    out["final_state_drift_mixed_vs_fp64"] = float(np.linalg.norm(ym - y64) / np.linalg.norm(y64))
     out["final_Fx_drift_mixed_vs_fp64"] = abs(out["mixed"]["final_Fx"] - out["fp64"]["final_Fx"]) / max(
         abs(out["fp64"]["final_Fx"]), 1e-300)
     print(json.dumps(out))
