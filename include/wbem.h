@@ -46,13 +46,20 @@ extern "C" {
 /* precision forms */
 #define WBEM_PREC_FP64 0  /* plain: FP64 everywhere */
 #define WBEM_PREC_MIXED 1 /* FP32 far field (double-float panel base + FP32 quadrature deltas),
-                             FP64 singular/near field and alpha, FP32 LU with BF16x3
-                             tensor-core updates, FP64 GMRES iterative refinement */
+                             FP64 singular/near field and alpha; (hi, lo) FP32 storage;
+                             FP32 LU (BF16x3 tensor-core updates) or FP32 inner GMRES,
+                             refined to full accuracy in FP64 */
 
 /* linear solvers */
-#define WBEM_SOLVER_AUTO 0  /* FP64 -> GMRES; MIXED -> LU + GMRES-IR */
-#define WBEM_SOLVER_GMRES 1 /* FP64 GMRES(restart), block-Jacobi preconditioner */
-#define WBEM_SOLVER_LU 2    /* dense LU (FP64 or mixed) refined by FP64 GMRES */
+#define WBEM_SOLVER_AUTO 0     /* FP64 -> GMRES; MIXED -> LU */
+#define WBEM_SOLVER_GMRES 1    /* FP64 GMRES(restart) on the assembled operator, block-Jacobi
+                                  preconditioner (either precision) */
+#define WBEM_SOLVER_LU 2       /* MIXED only: FP32 dense LU (BF16x3 tensor-core updates) as the
+                                  preconditioner of FP64 GMRES; the factors are reused by every
+                                  solve until the next assembly */
+#define WBEM_SOLVER_GMRES_IR 3 /* MIXED only: FP64 iterative refinement; each correction is an
+                                  inner block-Jacobi GMRES on the FP32 system matrix, run to a
+                                  relative residual of 10^-inner_digits */
 
 typedef struct wbem_context* wbem_handle;
 
@@ -66,7 +73,8 @@ typedef struct {
   double tolerance;              /* SolverControl "Tolerance" (absolute, on the residual) */
   double near_field_ratio;       /* MIXED: a panel is near when |x_i - centre| < ratio * diameter */
   int keep_matrices;             /* keep FP64 N (dG/dn) and D (G) for wbem_get_matrices */
-  int reserved[7];
+  int inner_digits;              /* GMRES_IR: inner relative tolerance 10^-inner_digits, 0 -> 4 */
+  int reserved[6];
 } wbem_options;
 
 typedef struct {
@@ -76,7 +84,8 @@ typedef struct {
   double residual;          /* final residual norm of the last solve */
   int kernel_launches;      /* kernels launched by the last assemble+solve */
   int n_dofs, n_cells;
-  int reserved[8];
+  int outer_iterations;     /* GMRES_IR: refinement steps of the last solve */
+  int reserved[7];
 } wbem_stats;
 
 /* Defaults of prm-files/default.prm:217-230 plus library choices. */

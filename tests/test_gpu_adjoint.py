@@ -10,7 +10,7 @@ import pytest
 
 from helpers import rel2
 from wavebem_gb300 import meshes as M
-from wavebem_gb300.bem_problem import PREC_FP64, PREC_MIXED, BEMProblem
+from wavebem_gb300.bem_problem import PREC_FP64, PREC_MIXED, SOLVER_GMRES_IR, SOLVER_LU, BEMProblem
 
 pytestmark = pytest.mark.gpu
 
@@ -71,13 +71,14 @@ def test_adjoint_componentwise_few_nodes_fp64():
             assert abs(gX[node, c] - fd) <= 1e-6 * scale, (node, c, gX[node, c], fd)
 
 
-def test_adjoint_mixed_matches_fp64():
+@pytest.mark.parametrize("solver", [SOLVER_GMRES_IR, SOLVER_LU])
+def test_adjoint_mixed_matches_fp64(solver):
     m, ptr, idx, hull = _setup(2000, None)
     b = M.wigley_bc(m, seed=3)
     g64 = BEMProblem(m.X, m.cells, m.dirichlet, ptr, idx, precision=PREC_FP64, tolerance=1e-14)
     _force(g64, m, b, hull)
     gX64, gb64 = g64.force_adjoint(hull, b)
-    gm = BEMProblem(m.X, m.cells, m.dirichlet, ptr, idx, precision=PREC_MIXED)
+    gm = BEMProblem(m.X, m.cells, m.dirichlet, ptr, idx, precision=PREC_MIXED, solver=solver)
     _force(gm, m, b, hull)
     gXm, gbm = gm.force_adjoint(hull, b)
     assert rel2(gXm, gX64) <= 1e-6

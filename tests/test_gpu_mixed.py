@@ -3,15 +3,19 @@
 Entries: double-float panel base + FP32 point differences; tolerance 2e-8
 relative to the largest entry (measured 1e-9 on the Wigley tank, 1.05e-8 on
 the coarse 866-node sphere whose strongly curved panels make the point
-differences larger). Solution: FP32 LU (BF16x3
-trailing updates) + FP64 GMRES refinement; tolerance 1e-8 relative 2-norm
-(the spec bar)."""
+differences larger). Solution, for each solver of the mixed form (FP64
+refinement over inner block-Jacobi GMRES on the FP32 system; FP32 LU with
+BF16x3 tensor-core updates preconditioning FP64 GMRES; plain block-Jacobi
+GMRES on the mixed storage): tolerance 1e-8 relative 2-norm."""
 import numpy as np
 import pytest
 
 from helpers import oracle_problem, rel2, relmax
 from wavebem_gb300 import meshes as M
-from wavebem_gb300.bem_problem import PREC_MIXED, BEMProblem
+from wavebem_gb300.bem_problem import (PREC_MIXED, SOLVER_GMRES, SOLVER_GMRES_IR, SOLVER_LU,
+                                       BEMProblem)
+
+SOLVERS = [SOLVER_GMRES_IR, SOLVER_LU, SOLVER_GMRES]
 
 pytestmark = pytest.mark.gpu
 
@@ -28,17 +32,22 @@ def test_mixed_matrices_alpha(kind, n):
     assert relmax(a, P.alpha) <= 2e-8
 
 
+@pytest.mark.parametrize("solver", SOLVERS)
 @pytest.mark.parametrize("kind,n", [("wigley", 2000), ("sphere", 12)])
-def test_mixed_solve_within_1e8(kind, n):
+def test_mixed_solve_within_1e8(kind, n, solver):
     P, m, b = oracle_problem(kind, n)
     phi_o, dphi_o, _ = P.solve_system(b)
-    g = BEMProblem(m.X, m.cells, m.dirichlet, P.dn_ptr, P.dn_idx, precision=PREC_MIXED)
+    g = BEMProblem(m.X, m.cells, m.dirichlet, P.dn_ptr, P.dn_idx, precision=PREC_MIXED,
+                   solver=solver)
     phi, dphi = b.copy(), b.copy()
     g.solve(phi, dphi, b)
     st = g.stats()
     assert rel2(phi, phi_o) <= 1e-8
     assert rel2(dphi, dphi_o) <= 1e-8
-    assert st["iterations"] <= 20
+    if solver == SOLVER_LU:
+        assert st["iterations"] <= 20
+    if solver == SOLVER_GMRES_IR:
+        assert 1 <= st["outer_iterations"] <= 10
 
 
 def test_mixed_hull_force_within_1e8():
@@ -53,13 +62,17 @@ def test_mixed_hull_force_within_1e8():
     assert abs(F - F_o) <= 1e-8 * abs(F_o)
 
 
-def test_mixed_solve_system_reuses_factors():
+@pytest.mark.parametrize("solver", [SOLVER_GMRES_IR, SOLVER_LU])
+def test_mixed_solve_system_reuses_factors(solver):
     P, m, b = oracle_problem("wigley", 2000)
-    g = BEMProblem(m.X, m.cells, m.dirichlet, P.dn_ptr, P.dn_idx, precision=PREC_MIXED)
+    g = BEMProblem(m.X, m.cells, m.dirichlet, P.dn_ptr, P.dn_idx, precision=PREC_MIXED,
+                   solver=solver)
     g.assemble_system()
-    for seed in (1, 2):
+    for k, seed in enumerate((1, 2)):
         b2 = M.wigley_bc(m, seed=seed)
         phi_o, dphi_o, _ = P.solve_system(b2)
         phi, dphi = b2.copy(), b2.copy()
         g.solve_system(phi, dphi, b2)
         assert rel2(phi, phi_o) <= 1e-8 and rel2(dphi, dphi_o) <= 1e-8
+        if k == 1:  # the second solve prepares nothing
+            assert g.stats()["t_factor_ms"] == 0.0

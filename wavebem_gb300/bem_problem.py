@@ -25,7 +25,7 @@ WBEM_OK = 0
 STATUS = {1: "ERR_ARG", 2: "ERR_STATE", 3: "ERR_CUDA", 4: "ERR_NOMEM", 5: "ERR_SINGULAR",
           6: "ERR_NOCONV", 7: "ERR_NONFINITE", 8: "ERR_TIMEOUT"}
 PREC_FP64, PREC_MIXED = 0, 1
-SOLVER_AUTO, SOLVER_GMRES, SOLVER_LU = 0, 1, 2
+SOLVER_AUTO, SOLVER_GMRES, SOLVER_LU, SOLVER_GMRES_IR = 0, 1, 2, 3
 
 # every entry point declared in include/wbem.h
 EXPORTS = ["wbem_default_options", "wbem_create", "wbem_destroy", "wbem_last_error",
@@ -50,7 +50,7 @@ class Options(C.Structure):
                 ("singular_quadrature_order", C.c_int), ("gmres_restart", C.c_int),
                 ("max_steps", C.c_int), ("tolerance", C.c_double),
                 ("near_field_ratio", C.c_double), ("keep_matrices", C.c_int),
-                ("reserved", C.c_int * 7)]
+                ("inner_digits", C.c_int), ("reserved", C.c_int * 6)]
 
 
 class Stats(C.Structure):
@@ -60,7 +60,7 @@ class Stats(C.Structure):
                 ("t_solve_ms", C.c_double), ("t_adjoint_ms", C.c_double),
                 ("iterations", C.c_int), ("residual", C.c_double),
                 ("kernel_launches", C.c_int), ("n_dofs", C.c_int), ("n_cells", C.c_int),
-                ("reserved", C.c_int * 8)]
+                ("outer_iterations", C.c_int), ("reserved", C.c_int * 7)]
 
 
 _lib = None

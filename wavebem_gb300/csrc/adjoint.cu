@@ -32,8 +32,7 @@ cudaError_t upload_quadrature_adjoint(const QuadTables& t) {
   return upload_quadrature_force(t);
 }
 int ensure_vectors(wbem_context* h, int restart);
-int solve_mixed(wbem_context* h, const double* d_rhs, double* d_x, int transpose);
-int gmres_fp64(wbem_context* h, const double* rhs, double* x, int transpose);
+int solve_assembled(wbem_context* h, const double* rhs, double* x, int transpose);
 
 constexpr double kI4P = 0.07957747154594766788;
 
@@ -486,7 +485,7 @@ int adjoint_force(wbem_context* h, const int* hull_cells, int n_hull, const doub
     k_gx<<<nb, bs, 0, h->stream>>>(N, h->d_mask, nph, npn, gx);
     WB_CU(cudaGetLastError());
     // transposed solve A^T lambda = g_x (constrained operator)
-    st = mixed ? solve_mixed(h, gx, lam, 1) : gmres_fp64(h, gx, lam, 1);
+    st = solve_assembled(h, gx, lam, 1);
     if (st != WBEM_OK) break;
     // lam_u: constrained rows take no part in dG/dX; keep lam for the b-terms
     double* lamu = h->d_vec[2];

@@ -7,6 +7,8 @@
 #include "../../include/wbem.h"
 #include "kernels.h"
 
+constexpr int kNumVec = 10;
+
 struct wbem_context {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -59,7 +61,8 @@ struct wbem_context {
   int near_cap = 0;
   size_t mat_elems = 0;       // allocated N*N (fp64 or float2)
   int assembled_prec = -1;    // precision of the current assembly, -1 = none
-  bool factors_valid = false;
+  bool factors_valid = false;  // preconditioner of factors_kind ready for this assembly
+  int factors_kind = 0;        // WBEM_SOLVER_* it was prepared for
 
   // ---- constraints (internal order)
   int n_crows = 0;
@@ -81,7 +84,7 @@ struct wbem_context {
   double* d_binv = nullptr;
   double* d_V = nullptr;   // (restart + 1) x N Krylov basis
   int V_cap = 0;
-  double* d_vec[8] = {};   // N-vectors
+  double* d_vec[kNumVec] = {};  // N-vectors: [0..2] GMRES, [7] transposed operator, [8..9] refinement
   double* d_part = nullptr;
   double* d_small = nullptr;
   float* d_lu = nullptr;   // mixed LU factors

@@ -101,6 +101,10 @@ cudaError_t launch_set_rows(int nrows, const int* crow, const double* val, doubl
                             cudaStream_t s);
 
 // block-Jacobi (FP64)
+cudaError_t launch_matvec_s32(int N, int ld, const float* S, const double* x, double* y,
+                              cudaStream_t s);
+cudaError_t launch_matvec_s32_t(int N, int ld, const float* S, const double* x, double* y,
+                                double* part, cudaStream_t s);
 cudaError_t launch_bj_build(int N, const double* Nm, const double* Dm, const float2* N2,
                             const float2* D2, const uint8_t* mask, const double* alpha,
                             const uint8_t* cflag, const int* cptr_full, const int* ccol_full,

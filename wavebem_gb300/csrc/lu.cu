@@ -884,18 +884,47 @@ static int tri_sweep(wbem_context* h, LuState& L, int mode, const float* in, flo
   return WBEM_OK;
 }
 
+// The constrained system operator as one FP32 matrix in the LU buffer
+// (row-major, leading dimension rounded up to 32 floats): the input of the
+// LU, and the inner operator of the refinement solver.
+int system_ld(int N) { return (N + 31) / 32 * 32; }
+
+int form_system_f32(wbem_context* h) {
+  const int N = h->N;
+  const int ld = system_ld(N);
+  const size_t nn = (size_t)N * ld;
+  if (!h->d_lu || h->lu_elems != nn) {
+    if (h->d_lu) {
+      cudaFree(h->d_lu);
+      h->d_lu = nullptr;
+    }
+    WB_CHK(dev_alloc(h, &h->d_lu, nn));
+    h->lu_elems = nn;
+  }
+  EvTimer tm(h->stream);
+  dim3 g(std::min(64, (N + 255) / 256), N);
+  k_form_lu<<<g, 256, 0, h->stream>>>(N, ld, h->d_N2, h->d_D2, h->d_mask, h->d_alpha, h->d_cflag,
+                                      h->d_cptr_full, h->d_ccol_full, h->d_cval_full, h->d_lu);
+  WB_CU(cudaGetLastError());
+  h->launches++;
+  if (h->n_crows > 0) {
+    k_lu_constraint_entries<<<(h->n_crows + 127) / 128, 128, 0, h->stream>>>(
+        h->n_crows, h->d_crow, h->d_cptr, h->d_ccol, h->d_cval, ld, h->d_lu);
+    WB_CU(cudaGetLastError());
+    h->launches++;
+  }
+  h->stats.t_system_ms = tm.ms();
+  return WBEM_OK;
+}
+
 int factor_mixed(wbem_context* h) {
   const int N = h->N;
-  const int ld = (N + 31) / 32 * 32;
-  const size_t nn = (size_t)N * ld;
+  const int ld = system_ld(N);
   if (h->lu_state && lu_state(h).N != N) free_lu(h);
   LuState& L = lu_state(h);
   L.N = N;
   L.ld = ld;
-  if (!h->d_lu || h->lu_elems != nn) {
-    WB_CHK(dev_alloc(h, &h->d_lu, nn));
-    h->lu_elems = nn;
-  }
+  WB_CHK(form_system_f32(h));
   if (!encode_cmap(&L.cmap, h->d_lu, N, N, ld))
     return fail(h, WBEM_ERR_CUDA, "cuTensorMapEncodeTiled (LU buffer) failed");
   const int nblk = (N + kNB - 1) / kNB;
@@ -938,18 +967,6 @@ int factor_mixed(wbem_context* h) {
   }
   uint16_t* b1 = L.split;
   EvTimer tm(h->stream);
-  {
-    dim3 g(std::min(64, (N + 255) / 256), N);
-    k_form_lu<<<g, 256, 0, h->stream>>>(N, ld, h->d_N2, h->d_D2, h->d_mask, h->d_alpha, h->d_cflag,
-                                        h->d_cptr_full, h->d_ccol_full, h->d_cval_full, h->d_lu);
-    WB_CU(cudaGetLastError());
-    if (h->n_crows > 0) {
-      k_lu_constraint_entries<<<(h->n_crows + 127) / 128, 128, 0, h->stream>>>(
-          h->n_crows, h->d_crow, h->d_cptr, h->d_ccol, h->d_cval, ld, h->d_lu);
-      WB_CU(cudaGetLastError());
-    }
-  }
-  h->stats.t_system_ms = tm.ms();
   float* A = h->d_lu;
   const SplitOut none{nullptr, nullptr, 0, 0, 0};
   const size_t kDiagSmem = (size_t)3 * kNB * kDLD * sizeof(float);

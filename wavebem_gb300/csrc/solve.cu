@@ -135,6 +135,54 @@ cudaError_t launch_matvec_mixed(int N, int mode, const float2* N2, const float2*
   return cudaGetLastError();
 }
 
+// y = S x for the FP32 system matrix S (row-major, leading dimension ld, the
+// constrained operator with alpha on its diagonal): the inner operator of the
+// refinement solver. One warp per row, each lane streams float4 quads of the
+// row; products and sums in FP32 with the lane sums moved into FP64 after
+// every chunk of kMvChunk columns (64 terms per FP32 partial sum), so the
+// operator is S to about 1e-6 relative, at 4 bytes of HBM traffic per entry.
+__global__ void __launch_bounds__(kMvWarps * 32)
+    k_matvec_s32(int N, int ld, const float* __restrict__ S, const double* __restrict__ x,
+                 double* __restrict__ y) {
+  __shared__ __align__(16) float xs[kMvChunk];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int row = blockIdx.x * kMvWarps + warp;
+  const bool active = row < N;
+  const float* sr = S + (size_t)(active ? row : 0) * ld;
+  double acc = 0.0;
+  for (int c0 = 0; c0 < N; c0 += kMvChunk) {
+    const int cn = min(kMvChunk, N - c0);
+    __syncthreads();
+    for (int k = threadIdx.x; k < kMvChunk; k += blockDim.x)
+      xs[k] = (k < cn) ? (float)x[c0 + k] : 0.f;
+    __syncthreads();
+    if (active) {
+      float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+      const int cq = cn & ~3;  // whole quads (row starts are 16-byte aligned)
+#pragma unroll 4
+      for (int k = 4 * lane; k < cq; k += 128) {
+        const float4 v = __ldcs(reinterpret_cast<const float4*>(sr + c0 + k));
+        const float4 xv = *reinterpret_cast<const float4*>(xs + k);
+        a0 = __fmaf_rn(v.x, xv.x, a0);
+        a1 = __fmaf_rn(v.y, xv.y, a1);
+        a2 = __fmaf_rn(v.z, xv.z, a2);
+        a3 = __fmaf_rn(v.w, xv.w, a3);
+      }
+      for (int k = cq + lane; k < cn; k += 32) a0 = __fmaf_rn(sr[c0 + k], xs[k], a0);
+      acc += ((double)a0 + (double)a1) + ((double)a2 + (double)a3);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (active && lane == 0) y[row] = acc;
+}
+
+cudaError_t launch_matvec_s32(int N, int ld, const float* S, const double* x, double* y,
+                              cudaStream_t s) {
+  k_matvec_s32<<<(N + kMvWarps - 1) / kMvWarps, kMvWarps * 32, 0, s>>>(N, ld, S, x, y);
+  return cudaGetLastError();
+}
+
 // Transposed system operator y_j = sum_i sel(i,j) x_i + (1 - mask_j) alpha_j x_j.
 // Blocks own column strips of 256 columns and a slice of rows; partial sums
 // go to part[slice][N] and are added in a fixed order (deterministic).
@@ -195,6 +243,34 @@ cudaError_t launch_matvec_t_mixed(int N, const float2* N2, const float2* D2, con
   dim3 g((N + kMvtCols - 1) / kMvtCols, kMvtSlices);
   k_matvec_t<float2><<<g, kMvtCols, 0, s>>>(N, N2, D2, mask, x, part);
   k_matvec_t_finish<<<(N + 255) / 256, 256, 0, s>>>(N, mask, alpha, x, part, y);
+  return cudaGetLastError();
+}
+
+// y = S^T x for the FP32 system matrix: threads own columns, blocks own a
+// column strip and a slice of rows; FP32 partial sums over 64 rows at a time,
+// moved into FP64, then the slices are added in a fixed order.
+__global__ void k_matvec_s32_t(int N, int ld, const float* __restrict__ S,
+                               const double* __restrict__ x, double* __restrict__ part) {
+  const int col = blockIdx.x * kMvtCols + threadIdx.x;
+  const int slice = blockIdx.y;
+  const int rows_per = (N + kMvtSlices - 1) / kMvtSlices;
+  const int r0 = slice * rows_per, r1 = min(N, r0 + rows_per);
+  if (col >= N) return;
+  double acc = 0.0;
+  for (int i0 = r0; i0 < r1; i0 += 64) {
+    const int i1 = min(r1, i0 + 64);
+    float a = 0.f;
+    for (int i = i0; i < i1; ++i) a = __fmaf_rn(__ldcs(S + (size_t)i * ld + col), (float)x[i], a);
+    acc += (double)a;
+  }
+  part[(size_t)slice * N + col] = acc;
+}
+
+cudaError_t launch_matvec_s32_t(int N, int ld, const float* S, const double* x, double* y,
+                                double* part, cudaStream_t s) {
+  dim3 g((N + kMvtCols - 1) / kMvtCols, kMvtSlices);
+  k_matvec_s32_t<<<g, kMvtCols, 0, s>>>(N, ld, S, x, part);
+  k_matvec_t_finish<<<(N + 255) / 256, 256, 0, s>>>(N, nullptr, nullptr, x, part, y);
   return cudaGetLastError();
 }
 
