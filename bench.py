@@ -198,20 +198,65 @@ def run_reference(args, rank, world):
 
 
 # ------------------------------------------------------------------ GPU side
+# DRAM traffic per unit of work of the roofline kernels, from one ncu capture
+# each (dram__bytes_read.sum + dram__bytes_write.sum); the capture and the
+# command that made it are in the named profile summary.
+NCU_TRAFFIC = {}
+
+
+class KernelProfile:
+    """wbem_kernel_profile (include/wbem_kernels.h)."""
+
+    @staticmethod
+    def struct():
+        import ctypes as C
+
+        class P(C.Structure):
+            _fields_ = [("gemm_ms", C.c_double), ("gemm_flop", C.c_double), ("gemm_launches", C.c_int),
+                        ("diag_ms", C.c_double), ("diag_launches", C.c_int),
+                        ("panel_ms", C.c_double), ("panel_launches", C.c_int),
+                        ("matvec_ms", C.c_double), ("matvec_bytes", C.c_double),
+                        ("matvec_launches", C.c_int),
+                        ("trsv_ms", C.c_double), ("trsv_bytes", C.c_double), ("trsv_launches", C.c_int),
+                        ("reserved", C.c_int * 8)]
+        return P
+
+
+def timed(stream, fn, reps):
+    import torch
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        t0.record(stream)
+        for _ in range(reps):
+            fn()
+        t1.record(stream)
+    torch.cuda.synchronize()
+    return t0.elapsed_time(t1) / reps / 1e3
+
+
 def run_gpu(args, rank, world, local):
     import ctypes
     import torch
-    from wavebem_gb300.bem_problem import PREC_FP64, PREC_MIXED, BEMProblem, load_library
+    from wavebem_gb300 import meshes as M
+    from wavebem_gb300.bem_problem import (PREC_FP64, PREC_MIXED, SOLVER_GMRES_IR, SOLVER_LU,
+                                           BEMProblem, load_library)
 
     torch.cuda.set_device(local)
     L = load_library()
     L.wbem_set_stream.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    L.wbem_set_profiling.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    Prof = KernelProfile.struct()
+    L.wbem_get_kernel_profile.argtypes = [ctypes.c_void_p, ctypes.POINTER(Prof)]
     m, ptr, idx, b, hull = workload(args.n)
     N = m.n_dofs
     stream = torch.cuda.Stream()
 
-    def problem(prec):
-        g = BEMProblem(m.X, m.cells, m.dirichlet, ptr, idx, device=local, precision=prec)
+    def problem(prec, mesh=None, p=None, i=None):
+        mesh = m if mesh is None else mesh
+        g = BEMProblem(mesh.X, mesh.cells, mesh.dirichlet, ptr if p is None else p,
+                       idx if i is None else i, device=local, precision=prec)
         assert L.wbem_set_stream(g.h, ctypes.c_void_p(stream.cuda_stream)) == 0
         return g
 
@@ -260,26 +305,58 @@ def run_gpu(args, rank, world, local):
     torch.cuda.synchronize()
     e2e = allmax(world, (time.perf_counter() - t0) / args.steps)
     per_phase = {k: v / args.steps for k, v in phase.items()}
+
+    # adjoint of the hull force on the same assembly (LU factors reused)
+    g.solve(phi, dphi, b)
+    adj_s = timed(stream, lambda: g.force_adjoint(hull, b), 2)
+    adjoint = {"s": adj_s, "n_dofs": N, "over_forward": adj_s / (ms_step / 1e3),
+               "what": "dF_x/dX (all nodes) and dF_x/dtmp_rhs after one mixed assemble+solve"}
+
+    # instrumented pass: kernel classes bracketed by events (serialised factor)
+    L.wbem_set_profiling(g.h, 1)
+    g.solve(phi, dphi, b)
+    pr = Prof()
+    assert L.wbem_get_kernel_profile(g.h, ctypes.byref(pr)) == 0
+    L.wbem_set_profiling(g.h, 0)
+    st_prof = g.stats()
+    kprof = {k: getattr(pr, k) for k, _ in Prof._fields_ if k != "reserved"}
+    kprof["tile_ms"] = st_prof["t_assemble_ms"]
+    kprof["factor_ms_serialised"] = st_prof["t_factor_ms"]
+
+    # the refinement solver variant on the same workload
+    variants = {}
+    ir_s = timed(stream, lambda: g.solve(phi, dphi, b, solver=SOLVER_GMRES_IR), 2)
+    st_ir = g.stats()
+    phi_ir, dphi_ir = phi.copy(), dphi.copy()
+    variants["gmres_ir"] = {"s": ir_s, "iterations": st_ir["iterations"],
+                            "outer_iterations": st_ir["outer_iterations"],
+                            "what": "FP64 refinement over inner block-Jacobi GMRES on the FP32 "
+                                    "system matrix (no LU)"}
     g.close()
     del g
+
+    # configs[3]-style adjoint workload: N = 8,192 with shape parameters
+    rng = np.random.default_rng(7)
+    m8 = M.wigley_mesh(8192, a=rng.normal(0.0, 1e-3, 8))
+    p8, i8 = M.double_nodes(m8.X, m8.cells)
+    b8 = M.wigley_bc(m8, seed=3)
+    h8 = np.nonzero(m8.face == M.HULL)[0].astype(np.int32)
+    g8 = problem(PREC_MIXED, m8, p8, i8)
+    ph8, dp8 = b8.copy(), b8.copy()
+    g8.solve(ph8, dp8, b8)
+    f8 = timed(stream, lambda: g8.solve(ph8, dp8, b8), 2)
+    a8 = timed(stream, lambda: g8.force_adjoint(h8, b8), 2)
+    adjoint["n8192"] = {"forward_s": f8, "adjoint_s": a8, "over_forward": a8 / f8}
+    g8.close()
+    del g8
 
     extra = {}
     if not args.no_fp64:
         g64 = problem(PREC_FP64)
         p64, d64 = b.copy(), b.copy()
         g64.solve(p64, d64, b)  # warm-up
-        torch.cuda.synchronize()
-        t0 = torch.cuda.Event(enable_timing=True)
-        t1 = torch.cuda.Event(enable_timing=True)
-        reps = 2
-        with torch.cuda.stream(stream):
-            t0.record(stream)
-            for _ in range(reps):
-                g64.solve(p64, d64, b)
-            t1.record(stream)
-        torch.cuda.synchronize()
+        fp64_s = timed(stream, lambda: g64.solve(p64, d64, b), 2)
         st64 = g64.stats()
-        fp64_s = t0.elapsed_time(t1) / reps / 1e3
         F64 = g64.hull_force(hull, p64, d64)
         nrm = lambda a, r: float(np.linalg.norm(a - r) / np.linalg.norm(r))
         extra = {"fp64_gpu_s": fp64_s, "speedup_vs_fp64_gpu": fp64_s / (ms_step / 1e3),
@@ -287,6 +364,7 @@ def run_gpu(args, rank, world, local):
                  "rel_err_vs_fp64": {"phi": nrm(phi_mx, p64), "dphi_dn": nrm(dphi_mx, d64),
                                      "hull_force": abs(F_mx - F64) / abs(F64)},
                  "fp64_phases_ms": {k: st64[k] for k in phase}}
+        variants["gmres_ir"]["rel_err_vs_fp64"] = {"phi": nrm(phi_ir, p64), "dphi_dn": nrm(dphi_ir, d64)}
         g64.close()
         del g64
 
@@ -297,36 +375,62 @@ def run_gpu(args, rank, world, local):
         if not args.no_cpu:
             v, desc, ta, ts = cpu_sample(m, ptr, idx, 1, budget_rows=16)
             cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "sample": desc}
-        asm_ms = per_phase["t_assemble_ms"]
-        fac_ms = per_phase["t_factor_ms"]
-        # roofline of the dominant kernel
-        nblk = (N + 127) // 128
-        gemm_flop = sum(3 * 2.0 * (N - (k + 1) * 128) ** 2 * 128 for k in range(nblk) if N - (k + 1) * 128 > 0)
-        if fac_ms >= asm_ms:
-            achieved = gemm_flop / (fac_ms / 1e3) / 1e12
-            roof = {"bound": "tensor", "kernel": "LU (BF16x3 tcgen05 trailing updates + panels)",
-                    "achieved": achieved, "peak": peaks.get("bf16_tflops"), "unit": "TFLOP/s",
-                    "frac": achieved / peaks.get("bf16_tflops"), "traffic": None,
-                    "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst) — of measured"}
-        else:
-            bytes_ = 2 * N * N * 8.0  # N and D as (hi, lo) float pairs
-            achieved = bytes_ / (asm_ms / 1e3) / 1e9
-            roof = {"bound": "hbm", "kernel": "k_tile_mixed (assembly)", "achieved": achieved,
-                    "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
-                    "frac": achieved / peaks.get("hbm_gbs"), "traffic": None,
-                    "peak_source": "MEASURED_PEAKS.json hbm_gbs — of measured; the kernel is FP32-ALU bound"}
+        hbm = peaks.get("hbm_gbs")
+        tc = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops"))
+        src = "of fallback" if peaks.get("fallback") else "of measured"
+        # every kernel class with its own bound; the dominant one is the roofline
+        kernels = []
+        if kprof["gemm_ms"] > 0:
+            a = kprof["gemm_flop"] / (kprof["gemm_ms"] / 1e3) / 1e12
+            kernels.append({"kernel": "k_gemm_bf16x3", "bound": "tensor", "ms": kprof["gemm_ms"],
+                            "launches": kprof["gemm_launches"], "achieved": a, "peak": tc,
+                            "unit": "TFLOP/s", "frac": a / tc,
+                            "work": "3 x 2 M N K per launch (BF16x3 products of the trailing updates)",
+                            "peak_source": f"MEASURED_PEAKS.json bf16_tflops_sustained ({src})"})
+        tile_bytes = 2.0 * N * N * 8.0
+        a = tile_bytes / (kprof["tile_ms"] / 1e3) / 1e9
+        kernels.append({"kernel": "k_tile_mixed", "bound": "hbm", "ms": kprof["tile_ms"], "launches": 1,
+                        "achieved": a, "peak": hbm, "unit": "GB/s", "frac": a / hbm,
+                        "work": "N and D written as (hi, lo) float pairs: 16 N^2 bytes",
+                        "note": "FP32/MUFU-issue bound (quadrature of every pair), not HBM",
+                        "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({src})"})
+        if kprof["matvec_ms"] > 0:
+            a = kprof["matvec_bytes"] / (kprof["matvec_ms"] / 1e3) / 1e9
+            kernels.append({"kernel": "k_matvec_mixed", "bound": "hbm", "ms": kprof["matvec_ms"],
+                            "launches": kprof["matvec_launches"], "achieved": a, "peak": hbm,
+                            "unit": "GB/s", "frac": a / hbm, "work": "8 N^2 bytes per launch",
+                            "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({src})"})
+        if kprof["trsv_ms"] > 0:
+            a = kprof["trsv_bytes"] / (kprof["trsv_ms"] / 1e3) / 1e9
+            kernels.append({"kernel": "k_trsv_wave", "bound": "hbm", "ms": kprof["trsv_ms"],
+                            "launches": kprof["trsv_launches"], "achieved": a, "peak": hbm,
+                            "unit": "GB/s", "frac": a / hbm, "work": "2 N^2 bytes per sweep",
+                            "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({src})"})
+        kernels.append({"kernel": "k_diag_block", "ms": kprof["diag_ms"], "launches": kprof["diag_launches"]})
+        kernels.append({"kernel": "k_panel_gemm+k_rowpanel_update", "ms": kprof["panel_ms"],
+                        "launches": kprof["panel_launches"]})
+        dom = max((k for k in kernels if "bound" in k), key=lambda k: k["ms"])
+        per_launch = dom["ms"] / max(1, dom["launches"])
+        roof = {"bound": dom["bound"], "kernel": dom["kernel"], "achieved": dom["achieved"],
+                "peak": dom["peak"], "unit": dom["unit"], "frac": dom["frac"],
+                "traffic": NCU_TRAFFIC.get(dom["kernel"]), "ms_per_launch": per_launch,
+                "peak_source": dom["peak_source"],
+                "timing": "CUDA events around each launch on its own stream, in an instrumented "
+                          "pass after the timed region (factorisation serialised on one stream)"}
         out = {"metric": METRIC, "value": ms_step / 1e3, "unit": UNIT, "n_gpus": world,
                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
                "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
                "dtype": "f32+f64 (mixed)", "data": "synthetic Wigley towing-tank mesh (seeded)",
                "config": {"workload": f"Wigley tank N={N} mixed-precision assemble+solve",
                           "n_dofs": N, "n_cells": m.n_cells, "parallelism": "replicas",
+                          "solver": "FP32 LU (BF16x3 tcgen05 trailing updates) + FP64 GMRES refinement",
                           "l2": "inputs (N, D: 17 GB) larger than L2"},
                "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(N * 3 * 8 + N * 8),
                        "d2h_bytes_per_step": int(N * 8)},
                "gpu_launches": int(launches),
                "phases_ms": per_phase, "gmres_iterations": iters,
-               "roofline": roof, "cpu_baseline": cpu, "clocks": clk}
+               "roofline": roof, "kernels": kernels, "adjoint": adjoint, "variants": variants,
+               "cpu_baseline": cpu, "clocks": clk}
         out.update(extra)
         print(json.dumps(out), flush=True)
     return out

@@ -19,10 +19,52 @@ extern "C" {
  * synchronizes. Returns a wbem.h status. */
 int wbem_test_gemm_bf16x3(int M, int Nc, int K, const float* dA, const float* dB, float* dC);
 
+/* The mixed-precision system matrix and its LU factors, for factor tests.
+ * After wbem_assemble (WBEM_PREC_MIXED) and wbem_set_bc: forms the FP32
+ * system matrix S (the constrained operator with alpha on its diagonal, rows
+ * and columns in the library's internal dof order) and copies it to A_host
+ * (n_dofs x n_dofs, row-major), factors it and copies the packed factors
+ * (unit-lower L below the diagonal, U on and above it) to LU_host; perm_host
+ * receives the internal order (perm_host[k] = caller dof of internal dof k).
+ * Any of the three pointers may be NULL. The factors then serve the next
+ * wbem_solve_system with WBEM_SOLVER_LU. Returns a wbem.h status. */
+struct wbem_context;
+int wbem_test_lu_factors(struct wbem_context* h, float* A_host, float* LU_host, int* perm_host);
+
+/* z = M^{-1} v (transpose: M^{-T}) with the current LU factors M = L U, host
+ * vectors of n_dofs doubles in the internal dof order (the order of
+ * wbem_test_lu_factors). Call after wbem_test_lu_factors or a solve with
+ * WBEM_SOLVER_LU. Returns a wbem.h status. */
+int wbem_test_lu_apply(struct wbem_context* h, const double* v, double* z, int transpose);
+
+/* Kernel profiling. With profiling on, the LU factorisation runs on the
+ * handle's stream alone (no look-ahead overlap) and every launch of the
+ * kernel classes below is bracketed by CUDA events on that stream, so the
+ * sums are the kernels' own device times. Meant for a separate, instrumented
+ * pass next to the timed one. The profile covers the last factorisation and
+ * the solves since then (reset by each factorisation). */
+typedef struct {
+  double gemm_ms;       /* k_gemm_bf16x3: tensor-core trailing updates */
+  double gemm_flop;     /*   their work: 3 x 2 M N K per launch (three BF16 products) */
+  int gemm_launches;
+  double diag_ms;       /* k_diag_block: 128 x 128 diagonal LU + triangle inverses */
+  int diag_launches;
+  double panel_ms;      /* k_panel_gemm + k_rowpanel_update (FP32 SIMT panels) */
+  int panel_launches;
+  double matvec_ms;     /* system mat-vecs of the refinement (k_matvec_mixed) */
+  double matvec_bytes;  /*   matrix bytes they stream: 8 N^2 per launch */
+  int matvec_launches;
+  double trsv_ms;       /* k_trsv_wave: block triangular sweeps */
+  double trsv_bytes;    /*   factor bytes they stream: 2 N^2 per sweep */
+  int trsv_launches;
+  int reserved[8];
+} wbem_kernel_profile;
+int wbem_set_profiling(struct wbem_context* h, int on);
+int wbem_get_kernel_profile(struct wbem_context* h, wbem_kernel_profile* p);
+
 /* Run all later work of the handle on the given cudaStream_t (NULL: back to
  * a private non-blocking stream). Lets a caller order the library's kernels
  * with its own work and time them with events on that stream. */
-struct wbem_context;
 int wbem_set_stream(struct wbem_context* h, void* cuda_stream);
 
 /* Hull force from device-resident fields without touching the allocator.

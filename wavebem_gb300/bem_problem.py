@@ -96,6 +96,8 @@ def load_library(path: str = LIB_PATH):
     L.wbem_hull_force.argtypes = [H, ip, C.c_int, dp, C.c_int, dp, dp, C.POINTER(C.c_double)]
     L.wbem_force_adjoint.argtypes = [H, ip, C.c_int, dp, C.c_int, dp, dp, dp]
     L.wbem_get_stats.argtypes = [H, C.POINTER(Stats)]
+    L.wbem_test_lu_factors.argtypes = [H, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.wbem_test_lu_apply.argtypes = [H, dp, dp, C.c_int]
     _lib = L
     return L
 
@@ -235,6 +237,25 @@ class BEMProblem:
         self._check(self.L.wbem_force_adjoint(self.h, hc, hc.size, _f64(U), int(direction),
                                               _f64(tmp_rhs), gX, gb))
         return gX.reshape(-1, 3), gb
+
+    def lu_factors(self):
+        """(S, LU, perm) of the current mixed assembly: the FP32 system matrix and
+        its packed FP32 factors in the internal dof order, perm[k] = caller dof
+        of internal dof k (factor tests)."""
+        N = self.n_dofs
+        S = np.zeros((N, N), np.float32)
+        LU = np.zeros((N, N), np.float32)
+        perm = np.zeros(N, np.int32)
+        self._check(self.L.wbem_test_lu_factors(self.h, S.ctypes.data_as(C.c_void_p),
+                                                LU.ctypes.data_as(C.c_void_p),
+                                                perm.ctypes.data_as(C.c_void_p)))
+        return S, LU, perm
+
+    def lu_apply(self, v, transpose=False):
+        """M^{-1} v with the current FP32 LU factors (internal dof order)."""
+        z = np.zeros(self.n_dofs)
+        self._check(self.L.wbem_test_lu_apply(self.h, _f64(v), z, int(bool(transpose))))
+        return z
 
     def stats(self) -> dict:
         s = Stats()

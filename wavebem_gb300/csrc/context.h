@@ -9,6 +9,47 @@
 
 constexpr int kNumVec = 10;
 
+// Event-bracketed intervals of one kernel class on one stream (kernel
+// profiling mode): begin/end around each launch, summed after the work.
+struct ProfTimer {
+  std::vector<cudaEvent_t> a, b;
+  size_t used = 0;
+  double work = 0.0;  // flops or bytes of the bracketed launches
+  void reset() {
+    used = 0;
+    work = 0.0;
+  }
+  void begin(cudaStream_t s) {
+    if (used == a.size()) {
+      cudaEvent_t x, y;
+      cudaEventCreate(&x);
+      cudaEventCreate(&y);
+      a.push_back(x);
+      b.push_back(y);
+    }
+    cudaEventRecord(a[used], s);
+  }
+  void end(cudaStream_t s, double w) {
+    cudaEventRecord(b[used], s);
+    ++used;
+    work += w;
+  }
+  double total_ms() {
+    double t = 0.0;
+    for (size_t i = 0; i < used; ++i) {
+      float ms = 0.f;
+      cudaEventSynchronize(b[i]);
+      cudaEventElapsedTime(&ms, a[i], b[i]);
+      t += ms;
+    }
+    return t;
+  }
+  ~ProfTimer() {
+    for (cudaEvent_t e : a) cudaEventDestroy(e);
+    for (cudaEvent_t e : b) cudaEventDestroy(e);
+  }
+};
+
 struct wbem_context {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -61,6 +102,10 @@ struct wbem_context {
   int near_cap = 0;
   size_t mat_elems = 0;       // allocated N*N (fp64 or float2)
   int assembled_prec = -1;    // precision of the current assembly, -1 = none
+  // kernel profiling mode: the factorisation runs on one stream and the
+  // launches of each kernel class are bracketed by events
+  bool profiling = false;
+  ProfTimer prof_gemm, prof_diag, prof_panel, prof_matvec, prof_trsv;
   bool factors_valid = false;  // preconditioner of factors_kind ready for this assembly
   int factors_kind = 0;        // WBEM_SOLVER_* it was prepared for
 

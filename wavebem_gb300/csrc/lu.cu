@@ -14,11 +14,17 @@
 // Step k (block size kNB = 128):
 //   1. k_diag_block: LU of A_kk in shared memory, plus the inverses of its
 //      unit-lower and upper factors;
-//   2. k_panel_gemm: U_kj = inv(L_kk) A_kj and L_ik = A_ik inv(U_kk) (FP32 SIMT),
+//   2. k_panel_sgemm: U_kj = inv(L_kk) A_kj and L_ik = A_ik inv(U_kk) (FP32 SIMT),
 //      also writing the BF16 hi/lo splits of both panels (K-major);
 //   3. k_gemm_bf16x3: A_ij -= L_ik U_kj as Lhi Uhi + Lhi Ulo + Llo Uhi with
-//      FP32 accumulation in TMEM (128 x 256 tile per CTA, K = 128 in two
-//      64-wide TMA stages with 128B swizzle).
+//      FP32 accumulation in TMEM (128 x 128 tile per CTA, K in 64-wide TMA
+//      stages with 128B swizzle, C staged through shared memory by TMA).
+// The steps are grouped in outer panels of kNB2 = 512 columns: inside a
+// panel the trailing updates cover the panel's own columns only (K = 128);
+// the rest of the matrix gets one K = 512 update per outer panel, split
+// between the next panel's columns (high-priority stream) and the remainder
+// (low-priority stream), so the next panel's factorisation overlaps the bulk
+// of the update (look-ahead).
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -149,7 +155,7 @@ __global__ void __launch_bounds__(kDiagThreads, 1)
       for (int k = 0; k < 32; ++k) {
         const float piv = __shfl_sync(0xffffffffu, col[k], k);
         okp = okp && (fabsf(piv) > 0.f) && isfinite(piv);
-        const float ip = 1.0f / piv;
+        const float ip = __frcp_rn(piv);
         // constant trip count, so both loops unroll and col[] stays in registers
 #pragma unroll
         for (int r = 1; r < 32; ++r) {
@@ -162,8 +168,15 @@ __global__ void __launch_bounds__(kDiagThreads, 1)
 #pragma unroll
       for (int r = 0; r < 32; ++r) sA[(o + r) * kDLD + o + lane] = col[r];
       if (!okp && lane == 0) bad = 1;
-      __syncwarp();
-      // ---- inverses of the two triangles of the 32-block, lane = column
+    }
+    __syncthreads();
+    if (bad) {
+      if (tid == 0) dev_fail(err, WBEM_ERR_SINGULAR, 51, k0, o);
+      return;  // uniform
+    }
+    // ---- inverses of the two triangles of the 32-block (warp 0: L, warp 1:
+    // U), lane = column
+    if (warp == 0) {
       float x[32];
 #pragma unroll
       for (int r = 0; r < 32; ++r) {
@@ -174,23 +187,23 @@ __global__ void __launch_bounds__(kDiagThreads, 1)
       }
 #pragma unroll
       for (int r = 0; r < 32; ++r) sLi[(o + r) * kDLD + o + lane] = x[r];
+    } else if (warp == 1) {
+      // reciprocals of the 32 pivots, one per lane, broadcast in the sweep
+      const float rd = __frcp_rn(sA[(o + lane) * kDLD + o + lane]);
+      float x[32];
 #pragma unroll
       for (int rr = 0; rr < 32; ++rr) {
         const int r = 31 - rr;
         float sum = 0.f;
 #pragma unroll
         for (int t = r + 1; t < 32; ++t) sum = __fmaf_rn(sA[(o + r) * kDLD + o + t], x[t], sum);
-        const float d = sA[(o + r) * kDLD + o + r];
-        x[r] = (r == lane) ? 1.f / d : (r < lane ? -sum / d : 0.f);
+        const float di = __shfl_sync(0xffffffffu, rd, r);
+        x[r] = (r == lane) ? di : (r < lane ? -sum * di : 0.f);
       }
 #pragma unroll
       for (int r = 0; r < 32; ++r) sUi[(o + r) * kDLD + o + lane] = x[r];
     }
     __syncthreads();
-    if (bad) {
-      if (tid == 0) dev_fail(err, WBEM_ERR_SINGULAR, 51, k0, o);
-      return;  // uniform
-    }
     // ---- panels: U_st = inv(L_ss) A_st (warps 0..), L_ts = A_ts inv(U_ss) (warps 3..)
     const int np = 3 - s;
     if (warp < np) {
@@ -244,12 +257,7 @@ __global__ void __launch_bounds__(kDiagThreads, 1)
 }
 
 // ------------------------------------------------------------- panel GEMM
-// out = Left (rows x 128) * Right (128 x cols), FP32 SIMT, 64 x 64 tiles,
-// 256 threads (4 x 4 outputs each).
-//   mode 0 (row panel):  Left = inv(L_kk), Right = A[k0:k0+128, c0:], out -> A same place,
-//                        BF16 splits of out^T -> Uhi/Ulo[(c - c0)][k] (K-major)
-//   mode 1 (col panel):  Left = A[r0:, k0:k0+128], Right = inv(U_kk), out -> A same place,
-//                        BF16 splits -> Lhi/Llo[(r - r0)][k]
+// BF16 hi/lo split of an FP32 value: hi = bf16(v), lo = bf16(v - hi).
 __device__ __forceinline__ void split_bf16(float v, uint16_t* hi, uint16_t* lo) {
   const __nv_bfloat16 h = __float2bfloat16_rn(v);
   const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
@@ -265,135 +273,154 @@ struct SplitOut {
   int coloff;     // column offset inside a row
 };
 
-//   mode 0 (row panel):  out[128 x ncols] = inv(L_kk) * A[k0:k0+128, cbeg:cbeg+ncols]
-//                        -> A, and split rows (cbeg + c - row0), columns (coloff + r)
-//   mode 1 (col panel):  out[nrows x 128] = A[rbeg:rbeg+nrows, k0:k0+128] * inv(U_kk)
-//                        -> A, and split rows (rbeg + r - row0) (rows >= row0 only),
-//                           columns (coloff + c)
-__global__ void __launch_bounds__(256)
-    k_panel_gemm(int N, int mode, int k0, int rbeg, int nrows, int cbeg, int ncols,
-                 float* __restrict__ A, const float* __restrict__ inv, SplitOut s1, SplitOut s2) {
-  __shared__ float sL[64][33];
-  __shared__ float sR[32][65];
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const int r0 = blockIdx.y * 64, c0 = blockIdx.x * 64;
-  float acc[4][4] = {};
-  for (int kk = 0; kk < kNB; kk += 32) {
-    for (int t = threadIdx.x; t < 64 * 32; t += 256) {
-      const int rr = t / 32, cc = t % 32;
-      float v = 0.f;
-      if (mode == 0) {
-        v = (r0 + rr < kNB) ? inv[(r0 + rr) * kNB + kk + cc] : 0.f;
-      } else if (r0 + rr < nrows) {
-        v = A[(size_t)(rbeg + r0 + rr) * N + k0 + kk + cc];
-      }
-      sL[rr][cc] = v;
-    }
-    for (int t = threadIdx.x; t < 32 * 64; t += 256) {
-      const int rr = t / 64, cc = t % 64;
-      float v = 0.f;
-      if (mode == 0) {
-        if (c0 + cc < ncols) v = A[(size_t)(k0 + kk + rr) * N + cbeg + c0 + cc];
-      } else if (c0 + cc < kNB) {
-        v = inv[(kk + rr) * kNB + c0 + cc];
-      }
-      sR[rr][cc] = v;
-    }
-    __syncthreads();
-#pragma unroll 8
-    for (int k = 0; k < 32; ++k) {
-      float a[4], b[4];
+// FP32 SIMT product of the panel work: out = Lft (rows x K) * Rgt (K x cols),
+// K a multiple of 8, written (SET) or subtracted (SUB), optionally with BF16
+// hi/lo splits of the result. 128 x 128 output tile per CTA, 256 threads with
+// 8 x 8 outputs each (two 4-wide halves 64 apart, so the shared-memory
+// fragments are read conflict-free as float4), K in steps of 8 through
+// double-buffered shared memory. In-place use (out == Lft with cols == K, or
+// out == Rgt with rows == K) is safe: a CTA reads all it needs before it
+// writes, and no other CTA reads its rows (columns).
+//   split rows: col_split == 0 -> split row = out row (column panel, L K-major)
+//               col_split == 1 -> split row = out column (row panel, U^T K-major)
+struct PanelArgs {
+  const float* L;  // Lft(i, k) = L[i * ldl + k]
+  int ldl;
+  const float* R;  // Rgt(k, j) = R[k * ldr + j]
+  int ldr;
+  float* O;        // out(i, j) = O[i * ldo + j]
+  int ldo;
+  int rows, cols, K;
+  int abs_row0, abs_col0;  // absolute matrix index of out row 0 / column 0 (splits)
+  int sub;                 // 1: out -= product, 0: out = product
+  int col_split;
+};
+
+constexpr int kPT = 128;  // panel tile
+constexpr int kPK = 8;    // K step
+constexpr int kPAS = kPT + 4;  // padded row of the transposed Lft tile
+
+__global__ void __launch_bounds__(256, 2)
+    k_panel_sgemm(PanelArgs pa, SplitOut s1, SplitOut s2) {
+  __shared__ __align__(16) float As[2][kPK][kPAS];
+  __shared__ __align__(16) float Bs[2][kPK][kPT];
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int i0 = blockIdx.x * kPT, j0 = blockIdx.y * kPT;
+  // global -> register staging of one K step
+  const int lr = tid >> 1, lk = (tid & 1) * 4;   // Lft: row lr, k lk..lk+3
+  const int rk = tid >> 5, rj = (tid & 31) * 4;  // Rgt: k rk, columns rj..rj+3
+  const bool lrow_ok = i0 + lr < pa.rows;
+  const float* lp = pa.L + (size_t)(i0 + lr) * pa.ldl + lk;
+  const int gj = j0 + rj;
+  const bool rvec = gj + 3 < pa.cols;
+  auto load_l = [&](int kk) -> float4 {
+    return lrow_ok ? __ldcg(reinterpret_cast<const float4*>(lp + kk)) : make_float4(0.f, 0.f, 0.f, 0.f);
+  };
+  auto load_r = [&](int kk) -> float4 {
+    const float* rp = pa.R + (size_t)(kk + rk) * pa.ldr + gj;
+    if (rvec) return __ldcg(reinterpret_cast<const float4*>(rp));
+    float4 v;
+    v.x = gj < pa.cols ? rp[0] : 0.f;
+    v.y = gj + 1 < pa.cols ? rp[1] : 0.f;
+    v.z = gj + 2 < pa.cols ? rp[2] : 0.f;
+    v.w = gj + 3 < pa.cols ? rp[3] : 0.f;
+    return v;
+  };
+  auto stage = [&](int buf, float4 a, float4 b) {
+    As[buf][lk + 0][lr] = a.x;
+    As[buf][lk + 1][lr] = a.y;
+    As[buf][lk + 2][lr] = a.z;
+    As[buf][lk + 3][lr] = a.w;
+    *reinterpret_cast<float4*>(&Bs[buf][rk][rj]) = b;
+  };
+  float acc[8][8];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        a[u] = sL[ty * 4 + u][k];
-        b[u] = sR[k][tx * 4 + u];
-      }
+  for (int u = 0; u < 8; ++u)
 #pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int v = 0; v < 4; ++v) acc[u][v] = __fmaf_rn(a[u], b[v], acc[u][v]);
+    for (int v = 0; v < 8; ++v) acc[u][v] = 0.f;
+  stage(0, load_l(0), load_r(0));
+  __syncthreads();
+  const int nk = pa.K / kPK;
+  for (int kt = 0; kt < nk; ++kt) {
+    const int cur = kt & 1;
+    float4 na = make_float4(0.f, 0.f, 0.f, 0.f), nb = na;
+    if (kt + 1 < nk) {
+      na = load_l((kt + 1) * kPK);
+      nb = load_r((kt + 1) * kPK);
     }
+#pragma unroll
+    for (int k = 0; k < kPK; ++k) {
+      const float4 a0 = *reinterpret_cast<const float4*>(&As[cur][k][ty * 4]);
+      const float4 a1 = *reinterpret_cast<const float4*>(&As[cur][k][64 + ty * 4]);
+      const float4 b0 = *reinterpret_cast<const float4*>(&Bs[cur][k][tx * 4]);
+      const float4 b1 = *reinterpret_cast<const float4*>(&Bs[cur][k][64 + tx * 4]);
+      const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+#pragma unroll
+        for (int v = 0; v < 8; ++v) acc[u][v] = __fmaf_rn(a[u], b[v], acc[u][v]);
+    }
+    if (kt + 1 < nk) stage(cur ^ 1, na, nb);
     __syncthreads();
   }
+  // epilogue: rows {ty*4 + u, 64 + ty*4 + u}, columns {tx*4 + v, 64 + tx*4 + v}
 #pragma unroll
-  for (int u = 0; u < 4; ++u)
+  for (int hu = 0; hu < 2; ++hu)
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      const int rr = r0 + ty * 4 + u, cc = c0 + tx * 4 + v;
-      const float val = acc[u][v];
-      if (mode == 0) {
-        if (rr < kNB && cc < ncols) {
-          const int col = cbeg + cc;
-          A[(size_t)(k0 + rr) * N + col] = val;
-          if (s1.hi) {
-            const size_t o = (size_t)(col - s1.row0) * s1.ld + s1.coloff + rr;
-            split_bf16(val, &s1.hi[o], &s1.lo[o]);
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + hu * 64 + ty * 4 + u;
+      if (i >= pa.rows) continue;
+#pragma unroll
+      for (int hv = 0; hv < 2; ++hv) {
+        const int j = j0 + hv * 64 + tx * 4;
+        if (j >= pa.cols) continue;
+        float* op = pa.O + (size_t)i * pa.ldo + j;
+        float r[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) r[v] = acc[hu * 4 + u][hv * 4 + v];
+        const int nv = min(4, pa.cols - j);
+        if (nv == 4) {
+          float4 o4 = make_float4(r[0], r[1], r[2], r[3]);
+          if (pa.sub) {
+            const float4 c = *reinterpret_cast<const float4*>(op);
+            o4 = make_float4(c.x - r[0], c.y - r[1], c.z - r[2], c.w - r[3]);
           }
-          if (s2.hi) {
-            const size_t o = (size_t)(col - s2.row0) * s2.ld + s2.coloff + rr;
-            split_bf16(val, &s2.hi[o], &s2.lo[o]);
+          *reinterpret_cast<float4*>(op) = o4;
+          r[0] = o4.x; r[1] = o4.y; r[2] = o4.z; r[3] = o4.w;
+        } else {
+          for (int v = 0; v < nv; ++v) {
+            r[v] = pa.sub ? op[v] - r[v] : r[v];
+            op[v] = r[v];
           }
         }
-      } else {
-        if (rr < nrows && cc < kNB) {
-          const int row = rbeg + rr;
-          A[(size_t)row * N + k0 + cc] = val;
-          if (s1.hi) {
-            const size_t o = (size_t)(row - s1.row0) * s1.ld + s1.coloff + cc;
-            split_bf16(val, &s1.hi[o], &s1.lo[o]);
-          }
-          if (s2.hi && row >= s2.row0) {
-            const size_t o = (size_t)(row - s2.row0) * s2.ld + s2.coloff + cc;
-            split_bf16(val, &s2.hi[o], &s2.lo[o]);
+        // BF16 splits of the values just written
+        for (int w = 0; w < 2; ++w) {
+          const SplitOut& so = w == 0 ? s1 : s2;
+          if (!so.hi) continue;
+          for (int v = 0; v < nv; ++v) {
+            const int ai = pa.abs_row0 + i, aj = pa.abs_col0 + j + v;
+            size_t o;
+            if (pa.col_split) {
+              if (aj < so.row0) continue;
+              o = (size_t)(aj - so.row0) * so.ld + so.coloff + (i);
+            } else {
+              if (ai < so.row0) continue;
+              o = (size_t)(ai - so.row0) * so.ld + so.coloff + (j + v);
+            }
+            split_bf16(r[v], &so.hi[o], &so.lo[o]);
           }
         }
       }
     }
 }
 
-// C[128 x n] -= Lrow[128 x K] * U[K x n] (FP32 SIMT, all operands inside the
-// LU buffer, ld N): the contributions of the earlier 128-blocks of an outer
-// panel to the row panel of a later block.
-__global__ void __launch_bounds__(256)
-    k_rowpanel_update(int N, int K, const float* __restrict__ Lrow, const float* __restrict__ U,
-                      float* __restrict__ Cm, int n) {
-  __shared__ float sL[64][33];
-  __shared__ float sR[32][65];
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const int r0 = blockIdx.y * 64, c0 = blockIdx.x * 64;
-  float acc[4][4] = {};
-  for (int kk = 0; kk < K; kk += 32) {
-    for (int t = threadIdx.x; t < 64 * 32; t += 256) {
-      const int rr = t / 32, cc = t % 32;
-      sL[rr][cc] = Lrow[(size_t)(r0 + rr) * N + kk + cc];
-    }
-    for (int t = threadIdx.x; t < 32 * 64; t += 256) {
-      const int rr = t / 64, cc = t % 64;
-      sR[rr][cc] = (c0 + cc < n) ? U[(size_t)(kk + rr) * N + c0 + cc] : 0.f;
-    }
-    __syncthreads();
-#pragma unroll 8
-    for (int k = 0; k < 32; ++k) {
-      float a[4], b[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        a[u] = sL[ty * 4 + u][k];
-        b[u] = sR[k][tx * 4 + u];
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int v = 0; v < 4; ++v) acc[u][v] = __fmaf_rn(a[u], b[v], acc[u][v]);
-    }
-    __syncthreads();
-  }
-#pragma unroll
-  for (int u = 0; u < 4; ++u)
-#pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      const int rr = r0 + ty * 4 + u, cc = c0 + tx * 4 + v;
-      if (cc < n) Cm[(size_t)rr * N + cc] -= acc[u][v];
-    }
+static cudaError_t run_panel(const PanelArgs& pa, const SplitOut& s1, const SplitOut& s2,
+                             cudaStream_t s) {
+  dim3 g((pa.rows + kPT - 1) / kPT, (pa.cols + kPT - 1) / kPT);
+  k_panel_sgemm<<<g, 256, 0, s>>>(pa, s1, s2);
+  return cudaGetLastError();
 }
 
 // ------------------------------------------------------- tcgen05 BF16x3 GEMM
@@ -879,8 +906,10 @@ static int tri_sweep(wbem_context* h, LuState& L, int mode, const float* in, flo
   const int ld = L.ld;
   void* args[] = {(void*)&N, (void*)&ld, (void*)&nblk, (void*)&mode, (void*)&LU, (void*)&dinv,
                   (void*)&in, (void*)&out, (void*)&flags, (void*)&epoch, (void*)&err};
+  if (h->profiling) h->prof_trsv.begin(h->stream);
   WB_CU(cudaLaunchCooperativeKernel((const void*)k_trsv_wave, dim3(nblk), dim3(kTriThreads), args,
                                     smem, h->stream));
+  if (h->profiling) h->prof_trsv.end(h->stream, 2.0 * (double)N * N);
   return WBEM_OK;
 }
 
@@ -889,7 +918,11 @@ static int tri_sweep(wbem_context* h, LuState& L, int mode, const float* in, flo
 // LU, and the inner operator of the refinement solver.
 int system_ld(int N) { return (N + 31) / 32 * 32; }
 
+int build_constraint_structure(wbem_context* h);
+
 int form_system_f32(wbem_context* h) {
+  if (!h->d_cflag || !h->d_cptr_full || !h->d_N2 || !h->d_D2 || !h->d_mask || !h->d_alpha)
+    return fail(h, WBEM_ERR_STATE, "system matrix: assembly, mask or constraints missing");
   const int N = h->N;
   const int ld = system_ld(N);
   const size_t nn = (size_t)N * ld;
@@ -979,7 +1012,23 @@ int factor_mixed(wbem_context* h) {
   // remaining columns [p2, N), which overlaps the column work of P + 1.
   // Ordering: U12 of P waits for the trailing update of P - 1 (same rows);
   // the trailing update of P on s_trail waits for U12 of P.
-  cudaStream_t sp = L.s_panel, st = L.s_trail;
+  // profiling: one stream, each launch bracketed by events
+  const bool prof = h->profiling;
+  cudaStream_t sp = prof ? h->stream : L.s_panel, st = prof ? h->stream : L.s_trail;
+  if (prof) {
+    h->prof_gemm.reset();
+    h->prof_diag.reset();
+    h->prof_panel.reset();
+    h->prof_matvec.reset();
+    h->prof_trsv.reset();
+  }
+  auto pb = [&](ProfTimer& t, cudaStream_t s) {
+    if (prof) t.begin(s);
+  };
+  auto pe = [&](ProfTimer& t, cudaStream_t s, double w) {
+    if (prof) t.end(s, w);
+  };
+  auto gemm_flop = [](int M, int Nc, int K) { return 3.0 * 2.0 * M * (double)Nc * K; };
   WB_CU(cudaEventRecord(L.ev_fork, h->stream));
   WB_CU(cudaStreamWaitEvent(sp, L.ev_fork, 0));
   WB_CU(cudaStreamWaitEvent(st, L.ev_fork, 0));
@@ -992,8 +1041,10 @@ int factor_mixed(wbem_context* h) {
     for (int k0 = p0; k0 < p1; k0 += kNB) {
       const int k = k0 / kNB, nb = std::min(kNB, N - k0), k1 = k0 + nb;
       const size_t bo = (size_t)k * kNB * kNB;
+      pb(h->prof_diag, sp);
       k_diag_block<<<1, kDiagThreads, kDiagSmem, sp>>>(ld, k0, nb, A, L.linv + bo, L.uinv + bo,
                                                        L.linvT + bo, L.uinvT + bo, h->d_err);
+      pe(h->prof_diag, sp, 0.0);
       h->launches++;
       if (k1 >= N) break;
       const int m = N - k1;
@@ -1001,16 +1052,24 @@ int factor_mixed(wbem_context* h) {
       const SplitOut Uin{b1 + 2 * rows * kNB, b1 + 3 * rows * kNB, k1, kNB, 0};
       const SplitOut L21{b2, b2 + rows * kNB2, p1, kNB2, k0 - p0};
       // column panel (full height), inner split + outer L21 split
-      dim3 gc(2, (m + 63) / 64);
-      k_panel_gemm<<<gc, 256, 0, sp>>>(ld, 1, k0, k1, m, 0, 0, A, L.uinv + bo, Lin,
-                                       p1 < N ? L21 : none);
+      // L_ik = A_ik inv(U_kk) for rows k1.., in place
+      const PanelArgs pc{A + (size_t)k1 * ld + k0, ld, L.uinv + bo, kNB, A + (size_t)k1 * ld + k0,
+                         ld, m, kNB, kNB, k1, k0, 0, 0};
+      pb(h->prof_panel, sp);
+      WB_CU(run_panel(pc, Lin, p1 < N ? L21 : none, sp));
+      pe(h->prof_panel, sp, 0.0);
       h->launches++;
       if (k1 < p1) {
         const int w = p1 - k1;
-        dim3 gr((w + 63) / 64, 2);
-        k_panel_gemm<<<gr, 256, 0, sp>>>(ld, 0, k0, 0, 0, k1, w, A, L.linv + bo, Uin, none);
-        WB_CU(cudaGetLastError());
+        // U_kj = inv(L_kk) A_kj for the panel's remaining columns, in place
+        const PanelArgs pr{L.linv + bo, kNB, A + (size_t)k0 * ld + k1, ld, A + (size_t)k0 * ld + k1,
+                           ld, kNB, w, kNB, k0, k1, 0, 1};
+        pb(h->prof_panel, sp);
+        WB_CU(run_panel(pr, Uin, none, sp));
+        pe(h->prof_panel, sp, 0.0);
+        pb(h->prof_gemm, sp);
         WB_CU(run_gemm(L.maps, L.cmap, k1, k1, 0, m, w, kNB, h->d_err, sp));
+        pe(h->prof_gemm, sp, gemm_flop(m, w, kNB));
         h->launches += 2;
       }
       WB_CU(cudaGetLastError());
@@ -1023,27 +1082,35 @@ int factor_mixed(wbem_context* h) {
     for (int k0 = p0; k0 < p1; k0 += kNB) {
       const int k = k0 / kNB;
       const size_t bo = (size_t)k * kNB * kNB;
+      pb(h->prof_panel, sp);
       if (k0 > p0) {
-        dim3 gu((n + 63) / 64, 2);
-        k_rowpanel_update<<<gu, 256, 0, sp>>>(ld, k0 - p0, A + (size_t)k0 * ld + p0,
-                                              A + (size_t)p0 * ld + p1, A + (size_t)k0 * ld + p1, n);
+        // A_kj -= L_k,[p0,k0) U_[p0,k0),j for the columns right of the panel
+        const PanelArgs pu{A + (size_t)k0 * ld + p0, ld, A + (size_t)p0 * ld + p1, ld,
+                           A + (size_t)k0 * ld + p1, ld, kNB, n, k0 - p0, k0, p1, 1, 0};
+        WB_CU(run_panel(pu, none, none, sp));
         h->launches++;
       }
       const SplitOut U12{b2 + 2 * rows * kNB2, b2 + 3 * rows * kNB2, p1, kNB2, k0 - p0};
-      dim3 gr((n + 63) / 64, 2);
-      k_panel_gemm<<<gr, 256, 0, sp>>>(ld, 0, k0, 0, 0, p1, n, A, L.linv + bo, U12, none);
+      const PanelArgs pr{L.linv + bo, kNB, A + (size_t)k0 * ld + p1, ld, A + (size_t)k0 * ld + p1, ld,
+                         kNB, n, kNB, k0, p1, 0, 1};
+      WB_CU(run_panel(pr, U12, none, sp));
+      pe(h->prof_panel, sp, 0.0);
       h->launches++;
       WB_CU(cudaGetLastError());
     }
     // ---- trailing update A22 -= L21 U12 on the tensor cores (K = kNB2):
     // the next panel's columns on s_panel, the rest on s_trail
     const int p2 = std::min(N, p1 + kNB2);
+    pb(h->prof_gemm, sp);
     WB_CU(run_gemm(L.maps2[buf], L.cmap, p1, p1, 0, n, p2 - p1, p1 - p0, h->d_err, sp));
+    pe(h->prof_gemm, sp, gemm_flop(n, p2 - p1, p1 - p0));
     h->launches++;
     if (p2 < N) {
       WB_CU(cudaEventRecord(L.ev_row, sp));
       WB_CU(cudaStreamWaitEvent(st, L.ev_row, 0));
+      pb(h->prof_gemm, st);
       WB_CU(run_gemm(L.maps2[buf], L.cmap, p1, p2, p2 - p1, n, N - p2, p1 - p0, h->d_err, st));
+      pe(h->prof_gemm, st, gemm_flop(n, N - p2, p1 - p0));
       WB_CU(cudaEventRecord(L.ev_trail, st));
       trail_pending = true;
       h->launches++;
@@ -1140,5 +1207,60 @@ extern "C" int wbem_test_gemm_bf16x3(int M, int Nc, int K, const float* dA, cons
   if (err) cudaFree(err);
   if (Cp) cudaFree(Cp);
   cudaFree(buf);
+  return st;
+}
+
+extern "C" int wbem_test_lu_factors(wbem_context* h, float* A_host, float* LU_host,
+                                    int* perm_host) {
+  using namespace wbem;
+  if (!h) return WBEM_ERR_ARG;
+  if (h->assembled_prec != WBEM_PREC_MIXED)
+    return fail(h, WBEM_ERR_STATE, "wbem_test_lu_factors: assemble in mixed precision first");
+  if (!h->have_mask) return fail(h, WBEM_ERR_STATE, "wbem_test_lu_factors: set the boundary conditions first");
+  if (cudaSetDevice(h->device) != cudaSuccess)
+    return fail(h, WBEM_ERR_CUDA, "wbem_test_lu_factors: cannot select the handle's device");
+  const int N = h->N;
+  const size_t ld = (size_t)system_ld(N);
+  WB_CHK(build_constraint_structure(h));
+  if (A_host) {
+    WB_CHK(form_system_f32(h));
+    WB_CU(cudaMemcpy2DAsync(A_host, sizeof(float) * N, h->d_lu, sizeof(float) * ld,
+                            sizeof(float) * N, N, cudaMemcpyDeviceToHost, h->stream));
+    WB_CU(cudaStreamSynchronize(h->stream));
+  }
+  WB_CHK(factor_mixed(h));
+  h->factors_valid = true;
+  h->factors_kind = WBEM_SOLVER_LU;
+  if (LU_host) {
+    WB_CU(cudaMemcpy2DAsync(LU_host, sizeof(float) * N, h->d_lu, sizeof(float) * ld,
+                            sizeof(float) * N, N, cudaMemcpyDeviceToHost, h->stream));
+    WB_CU(cudaStreamSynchronize(h->stream));
+  }
+  if (perm_host)
+    for (int k = 0; k < N; ++k) perm_host[k] = h->perm[k];
+  return WBEM_OK;
+}
+
+extern "C" int wbem_test_lu_apply(wbem_context* h, const double* v, double* z, int transpose) {
+  using namespace wbem;
+  if (!h || !v || !z) return WBEM_ERR_ARG;
+  if (!h->factors_valid || h->factors_kind != WBEM_SOLVER_LU || !h->lu_state)
+    return fail(h, WBEM_ERR_STATE, "wbem_test_lu_apply: no LU factors");
+  if (cudaSetDevice(h->device) != cudaSuccess)
+    return fail(h, WBEM_ERR_CUDA, "wbem_test_lu_apply: cannot select the handle's device");
+  const int N = h->N;
+  double* dv = nullptr;
+  WB_CU(cudaMalloc(&dv, sizeof(double) * 2 * N));
+  double* dz = dv + N;
+  int st = WBEM_OK;
+  if (cudaMemcpyAsync(dv, v, sizeof(double) * N, cudaMemcpyHostToDevice, h->stream) != cudaSuccess)
+    st = WBEM_ERR_CUDA;
+  if (st == WBEM_OK) st = lu_apply(h, dv, dz, transpose);
+  if (st == WBEM_OK &&
+      cudaMemcpyAsync(z, dz, sizeof(double) * N, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
+    st = WBEM_ERR_CUDA;
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess) st = WBEM_ERR_CUDA;
+  cudaFree(dv);
+  if (st == WBEM_OK) st = check_device_error(h, "wbem_test_lu_apply");
   return st;
 }

@@ -15,6 +15,7 @@
 #include <vector>
 #include "context.h"
 #include "host_util.h"
+#include "../../include/wbem_kernels.h"
 
 using namespace wbem;
 
@@ -643,8 +644,11 @@ int ensure_vectors(wbem_context* h, int restart) {
 int apply_system(wbem_context* h, const double* x, double* y) {
   if (h->assembled_prec == WBEM_PREC_FP64)
     CU(launch_matvec_fp64(h->N, 0, h->d_N, h->d_D, h->d_mask, h->d_alpha, x, y, h->stream));
-  else
+  else {
+    if (h->profiling) h->prof_matvec.begin(h->stream);
     CU(launch_matvec_mixed(h->N, 0, h->d_N2, h->d_D2, h->d_mask, h->d_alpha, x, y, h->stream));
+    if (h->profiling) h->prof_matvec.end(h->stream, 8.0 * (double)h->N * h->N);
+  }
   CU(launch_constraint_rows(h->n_crows, h->d_crow, h->d_cptr, h->d_ccol, h->d_cval, x, y, h->stream));
   h->launches += 2;
   return WBEM_OK;
@@ -898,6 +902,14 @@ int gmres_ir(wbem_context* h, const double* rhs, double* x, int transpose) {
   h->stats.residual = rnorm;
   h->stats.outer_iterations = outer;
   return WBEM_OK;
+}
+
+// Constraint rows and entries for the current mask and geometry (the
+// inhomogeneities, which depend on tmp_rhs, are left at zero): what the FP32
+// system matrix needs when no solve has run yet.
+int build_constraint_structure(wbem_context* h) {
+  std::vector<double> zero(h->N, 0.0);
+  return build_constraints(h, zero.data());
 }
 
 // The solver an assembly uses (the AUTO choice resolved), or -1 if the
@@ -1357,6 +1369,31 @@ int wbem_force_adjoint(wbem_handle h, const int* hull_cells, int n_hull, const d
   if (!h->have_solution) return fail(h, WBEM_ERR_STATE, "wbem_force_adjoint: solve first");
   cudaSetDevice(h->device);
   return adjoint_force(h, hull_cells, n_hull, U, dir, tmp_rhs, dF_dX, dF_drhs);
+}
+
+int wbem_set_profiling(wbem_handle h, int on) {
+  if (!h) return WBEM_ERR_ARG;
+  h->profiling = on != 0;
+  return WBEM_OK;
+}
+
+int wbem_get_kernel_profile(wbem_handle h, wbem_kernel_profile* p) {
+  if (!h || !p) return WBEM_ERR_ARG;
+  std::memset(p, 0, sizeof *p);
+  p->gemm_ms = h->prof_gemm.total_ms();
+  p->gemm_flop = h->prof_gemm.work;
+  p->gemm_launches = (int)h->prof_gemm.used;
+  p->diag_ms = h->prof_diag.total_ms();
+  p->diag_launches = (int)h->prof_diag.used;
+  p->panel_ms = h->prof_panel.total_ms();
+  p->panel_launches = (int)h->prof_panel.used;
+  p->matvec_ms = h->prof_matvec.total_ms();
+  p->matvec_bytes = h->prof_matvec.work;
+  p->matvec_launches = (int)h->prof_matvec.used;
+  p->trsv_ms = h->prof_trsv.total_ms();
+  p->trsv_bytes = h->prof_trsv.work;
+  p->trsv_launches = (int)h->prof_trsv.used;
+  return WBEM_OK;
 }
 
 int wbem_set_stream(wbem_handle h, void* cuda_stream) {
