@@ -15,7 +15,7 @@ extern "C" {
  * row-major), all FP32 device pointers. A and B are split into BF16 hi/lo
  * parts and multiplied as Ahi Bhi + Ahi Blo + Alo Bhi on the tcgen05 tensor
  * cores with FP32 accumulation in TMEM (the trailing update of the LU).
- * K must be a positive multiple of 64. Runs on the legacy default stream and
+ * K must be a positive multiple of 32. Runs on the legacy default stream and
  * synchronizes. Returns a wbem.h status. */
 int wbem_test_gemm_bf16x3(int M, int Nc, int K, const float* dA, const float* dB, float* dC);
 

@@ -1,5 +1,6 @@
 """Kernel-level GPU tests: the tcgen05 BF16x3 GEMM against a PyTorch FP32
-reference of the same operation (and its exact BF16-split emulation)."""
+reference of the same operation (and its exact BF16-split emulation), from
+one tile to more tiles than SMs (persistent CTAs, both TMEM accumulators)."""
 import ctypes
 
 import numpy as np
@@ -15,7 +16,8 @@ def _lib():
     return L
 
 
-@pytest.mark.parametrize("M,Nc,K", [(128, 256, 64), (300, 520, 128), (1000, 777, 128), (256, 512, 256)])
+@pytest.mark.parametrize("M,Nc,K", [(128, 256, 64), (300, 520, 128), (1000, 777, 128), (256, 512, 256),
+                                    (64, 40, 32), (2048, 1000, 512), (4096, 4096, 128)])
 def test_gemm_bf16x3_matches_torch(M, Nc, K):
     torch = pytest.importorskip("torch")
     g = torch.Generator(device="cpu").manual_seed(M + Nc + K)

@@ -274,12 +274,9 @@ struct SplitOut {
 };
 
 // FP32 SIMT product of the panel work: out = Lft (rows x K) * Rgt (K x cols),
-// K a multiple of 8, written (SET) or subtracted (SUB), optionally with BF16
-// hi/lo splits of the result. 128 x 128 output tile per CTA, 256 threads with
-// 8 x 8 outputs each (two 4-wide halves 64 apart, so the shared-memory
-// fragments are read conflict-free as float4), K in steps of 8 through
-// double-buffered shared memory. In-place use (out == Lft with cols == K, or
-// out == Rgt with rows == K) is safe: a CTA reads all it needs before it
+// K a multiple of 128, written (SET) or subtracted (SUB), optionally with
+// BF16 hi/lo splits of the result. In-place use (out == Lft with cols == K,
+// or out == Rgt with rows == K) is safe: a CTA reads all it needs before it
 // writes, and no other CTA reads its rows (columns).
 //   split rows: col_split == 0 -> split row = out row (column panel, L K-major)
 //               col_split == 1 -> split row = out column (row panel, U^T K-major)
@@ -296,130 +293,185 @@ struct PanelArgs {
   int col_split;
 };
 
-constexpr int kPT = 128;  // panel tile
-constexpr int kPK = 8;    // K step
-constexpr int kPAS = kPT + 4;  // padded row of the transposed Lft tile
+// Panel products with the whole K chunk resident in shared memory: the CTA
+// copies its Lft rows (TM x 128) and the Rgt block (128 x TN) with cp.async in
+// one go, waits once, and runs 128 FMA steps from shared memory (no per-step
+// global latency). Larger K (the row-panel update) loops over 128-chunks.
+//   TM x TN = 64 x 128 (column panels: tall, full width) or 128 x 64 (row
+//   panels and their updates: full height, column strips); 256 threads, 32
+//   outputs each; 96 KB of shared memory, two CTAs per SM.
+//   ATRANS: Lft is given transposed (LT(k, i) = L[k * ldl + i], e.g. the
+//   column-major copy of inv(L_kk)), so its fragments are float4 reads.
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, int src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src),
+               "r"(src_bytes)
+               : "memory");
+}
 
-__global__ void __launch_bounds__(256, 2)
-    k_panel_sgemm(PanelArgs pa, SplitOut s1, SplitOut s2) {
-  __shared__ __align__(16) float As[2][kPK][kPAS];
-  __shared__ __align__(16) float Bs[2][kPK][kPT];
+template <int TM, int TN, bool ATRANS>
+__global__ void __launch_bounds__(256, 2) k_panel_tile(PanelArgs pa, SplitOut s1, SplitOut s2) {
+  constexpr int KC = 128;
+  constexpr int ALD = ATRANS ? TM + 4 : KC + 4;  // padded smem rows
+  constexpr int BLD = TN + 4;
+  extern __shared__ __align__(16) float psm[];
+  float* As = psm;                        // ATRANS: [KC][ALD] else [TM][ALD]
+  float* Bs = psm + (ATRANS ? KC : TM) * ALD;  // [KC][BLD]
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;
-  const int i0 = blockIdx.x * kPT, j0 = blockIdx.y * kPT;
-  // global -> register staging of one K step
-  const int lr = tid >> 1, lk = (tid & 1) * 4;   // Lft: row lr, k lk..lk+3
-  const int rk = tid >> 5, rj = (tid & 31) * 4;  // Rgt: k rk, columns rj..rj+3
-  const bool lrow_ok = i0 + lr < pa.rows;
-  const float* lp = pa.L + (size_t)(i0 + lr) * pa.ldl + lk;
-  const int gj = j0 + rj;
-  const bool rvec = gj + 3 < pa.cols;
-  auto load_l = [&](int kk) -> float4 {
-    return lrow_ok ? __ldcg(reinterpret_cast<const float4*>(lp + kk)) : make_float4(0.f, 0.f, 0.f, 0.f);
-  };
-  auto load_r = [&](int kk) -> float4 {
-    const float* rp = pa.R + (size_t)(kk + rk) * pa.ldr + gj;
-    if (rvec) return __ldcg(reinterpret_cast<const float4*>(rp));
-    float4 v;
-    v.x = gj < pa.cols ? rp[0] : 0.f;
-    v.y = gj + 1 < pa.cols ? rp[1] : 0.f;
-    v.z = gj + 2 < pa.cols ? rp[2] : 0.f;
-    v.w = gj + 3 < pa.cols ? rp[3] : 0.f;
-    return v;
-  };
-  auto stage = [&](int buf, float4 a, float4 b) {
-    As[buf][lk + 0][lr] = a.x;
-    As[buf][lk + 1][lr] = a.y;
-    As[buf][lk + 2][lr] = a.z;
-    As[buf][lk + 3][lr] = a.w;
-    *reinterpret_cast<float4*>(&Bs[buf][rk][rj]) = b;
-  };
-  float acc[8][8];
+  const int i0 = blockIdx.x * TM, j0 = blockIdx.y * TN;
+  // thread outputs: TM x TN = 64 x 128 -> rows ty*4+u, cols {tx*4+v, 64+tx*4+v}
+  //                 128 x 64          -> rows {ty*4+u, 64+ty*4+u}, cols tx*4+v
+  constexpr int RH = TM / 64, CH = TN / 64;  // row / column halves per thread
+  float acc[4 * RH][4 * CH];
 #pragma unroll
-  for (int u = 0; u < 8; ++u)
+  for (int u = 0; u < 4 * RH; ++u)
 #pragma unroll
-    for (int v = 0; v < 8; ++v) acc[u][v] = 0.f;
-  stage(0, load_l(0), load_r(0));
-  __syncthreads();
-  const int nk = pa.K / kPK;
-  for (int kt = 0; kt < nk; ++kt) {
-    const int cur = kt & 1;
-    float4 na = make_float4(0.f, 0.f, 0.f, 0.f), nb = na;
-    if (kt + 1 < nk) {
-      na = load_l((kt + 1) * kPK);
-      nb = load_r((kt + 1) * kPK);
+    for (int v = 0; v < 4 * CH; ++v) acc[u][v] = 0.f;
+  for (int kc = 0; kc < pa.K; kc += KC) {
+    if (kc > 0) __syncthreads();  // previous chunk consumed
+    // ---- stage Lft
+    if (ATRANS) {
+      for (int q = tid; q < KC * (TM / 4); q += 256) {
+        const int k = q / (TM / 4), c = (q % (TM / 4)) * 4;
+        const int gi = i0 + c;
+        const int nbytes = gi + 4 <= pa.rows ? 16 : (gi < pa.rows ? 4 * (pa.rows - gi) : 0);
+        const float* src = pa.L + (size_t)(kc + k) * pa.ldl + (nbytes ? gi : 0);
+        cp_async16(As + k * ALD + c, src, nbytes);
+      }
+    } else {
+      for (int q = tid; q < TM * (KC / 4); q += 256) {
+        const int i = q / (KC / 4), c = (q % (KC / 4)) * 4;
+        const bool ok = i0 + i < pa.rows;
+        const float* src = pa.L + (size_t)(ok ? i0 + i : 0) * pa.ldl + kc + c;
+        cp_async16(As + i * ALD + c, src, ok ? 16 : 0);
+      }
     }
-#pragma unroll
-    for (int k = 0; k < kPK; ++k) {
-      const float4 a0 = *reinterpret_cast<const float4*>(&As[cur][k][ty * 4]);
-      const float4 a1 = *reinterpret_cast<const float4*>(&As[cur][k][64 + ty * 4]);
-      const float4 b0 = *reinterpret_cast<const float4*>(&Bs[cur][k][tx * 4]);
-      const float4 b1 = *reinterpret_cast<const float4*>(&Bs[cur][k][64 + tx * 4]);
-      const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-      const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
-#pragma unroll
-      for (int u = 0; u < 8; ++u)
-#pragma unroll
-        for (int v = 0; v < 8; ++v) acc[u][v] = __fmaf_rn(a[u], b[v], acc[u][v]);
+    // ---- stage Rgt
+    for (int q = tid; q < KC * (TN / 4); q += 256) {
+      const int k = q / (TN / 4), c = (q % (TN / 4)) * 4;
+      const int gj = j0 + c;
+      const int nbytes = gj + 4 <= pa.cols ? 16 : (gj < pa.cols ? 4 * (pa.cols - gj) : 0);
+      const float* src = pa.R + (size_t)(kc + k) * pa.ldr + (nbytes ? gj : 0);
+      cp_async16(Bs + k * BLD + c, src, nbytes);
     }
-    if (kt + 1 < nk) stage(cur ^ 1, na, nb);
+    asm volatile("cp.async.commit_group;\n cp.async.wait_group 0;" ::: "memory");
     __syncthreads();
+#pragma unroll 4
+    for (int k = 0; k < KC; ++k) {
+      float a[4 * RH], b[4 * CH];
+#pragma unroll
+      for (int h = 0; h < RH; ++h) {
+        if (ATRANS) {
+          const float4 t = *reinterpret_cast<const float4*>(As + k * ALD + h * 64 + ty * 4);
+          a[4 * h] = t.x; a[4 * h + 1] = t.y; a[4 * h + 2] = t.z; a[4 * h + 3] = t.w;
+        } else {
+#pragma unroll
+          for (int u = 0; u < 4; ++u) a[4 * h + u] = As[(h * 64 + ty * 4 + u) * ALD + k];
+        }
+      }
+#pragma unroll
+      for (int h = 0; h < CH; ++h) {
+        const float4 t = *reinterpret_cast<const float4*>(Bs + k * BLD + h * 64 + tx * 4);
+        b[4 * h] = t.x; b[4 * h + 1] = t.y; b[4 * h + 2] = t.z; b[4 * h + 3] = t.w;
+      }
+#pragma unroll
+      for (int u = 0; u < 4 * RH; ++u)
+#pragma unroll
+        for (int v = 0; v < 4 * CH; ++v) acc[u][v] = __fmaf_rn(a[u], b[v], acc[u][v]);
+    }
   }
-  // epilogue: rows {ty*4 + u, 64 + ty*4 + u}, columns {tx*4 + v, 64 + tx*4 + v}
+  // ---- epilogue: 4 x 4 blocks of (row quad, column quad)
 #pragma unroll
-  for (int hu = 0; hu < 2; ++hu)
+  for (int hu = 0; hu < RH; ++hu)
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int i = i0 + hu * 64 + ty * 4 + u;
-      if (i >= pa.rows) continue;
+    for (int hv = 0; hv < CH; ++hv) {
+      const int ib = i0 + hu * 64 + ty * 4;  // first row of the quad
+      const int jb = j0 + hv * 64 + tx * 4;  // first column of the quad
+      if (ib >= pa.rows || jb >= pa.cols) continue;
+      const int nu = min(4, pa.rows - ib), nv = min(4, pa.cols - jb);
+      float r[4][4];
 #pragma unroll
-      for (int hv = 0; hv < 2; ++hv) {
-        const int j = j0 + hv * 64 + tx * 4;
-        if (j >= pa.cols) continue;
-        float* op = pa.O + (size_t)i * pa.ldo + j;
-        float r[4];
+      for (int u = 0; u < 4; ++u)
 #pragma unroll
-        for (int v = 0; v < 4; ++v) r[v] = acc[hu * 4 + u][hv * 4 + v];
-        const int nv = min(4, pa.cols - j);
+        for (int v = 0; v < 4; ++v) r[u][v] = acc[hu * 4 + u][hv * 4 + v];
+      for (int u = 0; u < nu; ++u) {
+        float* op = pa.O + (size_t)(ib + u) * pa.ldo + jb;
         if (nv == 4) {
-          float4 o4 = make_float4(r[0], r[1], r[2], r[3]);
+          float4 o4 = make_float4(r[u][0], r[u][1], r[u][2], r[u][3]);
           if (pa.sub) {
             const float4 c = *reinterpret_cast<const float4*>(op);
-            o4 = make_float4(c.x - r[0], c.y - r[1], c.z - r[2], c.w - r[3]);
+            o4 = make_float4(c.x - o4.x, c.y - o4.y, c.z - o4.z, c.w - o4.w);
           }
           *reinterpret_cast<float4*>(op) = o4;
-          r[0] = o4.x; r[1] = o4.y; r[2] = o4.z; r[3] = o4.w;
+          r[u][0] = o4.x; r[u][1] = o4.y; r[u][2] = o4.z; r[u][3] = o4.w;
         } else {
           for (int v = 0; v < nv; ++v) {
-            r[v] = pa.sub ? op[v] - r[v] : r[v];
-            op[v] = r[v];
+            r[u][v] = pa.sub ? op[v] - r[u][v] : r[u][v];
+            op[v] = r[u][v];
           }
         }
-        // BF16 splits of the values just written
-        for (int w = 0; w < 2; ++w) {
-          const SplitOut& so = w == 0 ? s1 : s2;
-          if (!so.hi) continue;
+      }
+      // BF16 splits, 4 consecutive K entries packed into one 8-byte store
+      for (int w = 0; w < 2; ++w) {
+        const SplitOut& so = w == 0 ? s1 : s2;
+        if (!so.hi) continue;
+        if (pa.col_split) {
+          // split row = absolute column, K index = row (4 rows contiguous)
           for (int v = 0; v < nv; ++v) {
-            const int ai = pa.abs_row0 + i, aj = pa.abs_col0 + j + v;
-            size_t o;
-            if (pa.col_split) {
-              if (aj < so.row0) continue;
-              o = (size_t)(aj - so.row0) * so.ld + so.coloff + (i);
+            const int aj = pa.abs_col0 + jb + v;
+            if (aj < so.row0) continue;
+            const size_t o = (size_t)(aj - so.row0) * so.ld + so.coloff + ib;
+            uint16_t hh[4], ll[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) split_bf16(u < nu ? r[u][v] : 0.f, &hh[u], &ll[u]);
+            if (nu == 4) {
+              *reinterpret_cast<uint2*>(so.hi + o) = *reinterpret_cast<const uint2*>(hh);
+              *reinterpret_cast<uint2*>(so.lo + o) = *reinterpret_cast<const uint2*>(ll);
             } else {
-              if (ai < so.row0) continue;
-              o = (size_t)(ai - so.row0) * so.ld + so.coloff + (j + v);
+              for (int u = 0; u < nu; ++u) {
+                so.hi[o + u] = hh[u];
+                so.lo[o + u] = ll[u];
+              }
             }
-            split_bf16(r[v], &so.hi[o], &so.lo[o]);
+          }
+        } else {
+          // split row = absolute row, K index = column (4 columns contiguous)
+          for (int u = 0; u < nu; ++u) {
+            const int ai = pa.abs_row0 + ib + u;
+            if (ai < so.row0) continue;
+            const size_t o = (size_t)(ai - so.row0) * so.ld + so.coloff + jb;
+            uint16_t hh[4], ll[4];
+#pragma unroll
+            for (int v = 0; v < 4; ++v) split_bf16(v < nv ? r[u][v] : 0.f, &hh[v], &ll[v]);
+            if (nv == 4) {
+              *reinterpret_cast<uint2*>(so.hi + o) = *reinterpret_cast<const uint2*>(hh);
+              *reinterpret_cast<uint2*>(so.lo + o) = *reinterpret_cast<const uint2*>(ll);
+            } else {
+              for (int v = 0; v < nv; ++v) {
+                so.hi[o + v] = hh[v];
+                so.lo[o + v] = ll[v];
+              }
+            }
           }
         }
       }
     }
 }
 
-static cudaError_t run_panel(const PanelArgs& pa, const SplitOut& s1, const SplitOut& s2,
-                             cudaStream_t s) {
-  dim3 g((pa.rows + kPT - 1) / kPT, (pa.cols + kPT - 1) / kPT);
-  k_panel_sgemm<<<g, 256, 0, s>>>(pa, s1, s2);
+template <int TM, int TN, bool ATRANS>
+static cudaError_t run_panel_tile(const PanelArgs& pa, const SplitOut& s1, const SplitOut& s2,
+                                  cudaStream_t s) {
+  constexpr int ALD = ATRANS ? TM + 4 : 128 + 4;
+  const size_t smem = sizeof(float) * ((size_t)(ATRANS ? 128 : TM) * ALD + (size_t)128 * (TN + 4));
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_panel_tile<TM, TN, ATRANS>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  dim3 g((pa.rows + TM - 1) / TM, (pa.cols + TN - 1) / TN);
+  k_panel_tile<TM, TN, ATRANS><<<g, 256, smem, s>>>(pa, s1, s2);
   return cudaGetLastError();
 }
 
@@ -621,6 +673,280 @@ __global__ void __launch_bounds__(128, 1)
                  : "memory");
 }
 
+// ------------------------------------------------- persistent tcgen05 GEMM
+// C[crow0 + m, ccol0 + n] -= sum_k A[m, k] B[brow0 + n, k], BF16x3, for the
+// large trailing updates. Persistent CTAs (one per SM) walk 128 x 256 output
+// tiles (M fastest, so the CTAs in flight share B tiles and stream A); warp
+// roles:
+//   warp 0     TMA producer: A hi/lo (128 x 32) and B hi/lo (256 x 32) per
+//              K step into a 4-stage ring of 48 KB (64-byte swizzle);
+//   warp 1     TMEM owner and MMA issuer: 6 tcgen05.mma (M 128, N 256, K 16)
+//              per K step into one of two 256-column FP32 accumulators;
+//   warps 2-5  epilogue: per 32-column chunk, the C chunk arrives by TMA into
+//              one of two 16 KB buffers (128-byte swizzle), each thread
+//              subtracts its TMEM row (tcgen05.ld 32x32b.x32), one thread
+//              stores the chunk back by TMA and refills the buffer two
+//              chunks ahead.
+// The epilogue of tile i overlaps the MMAs of tile i + 1 (the other
+// accumulator). Columns at or beyond Nc are neither read nor written (chunk
+// granularity: Nc is a multiple of 32 or reaches the matrix edge); rows past
+// the matrix edge are clipped by the tensor map.
+constexpr int G3M = 128, G3N = 256, G3K = 32, G3S = 4;
+constexpr uint32_t kA3 = G3M * G3K * 2;                  // 8 KB
+constexpr uint32_t kB3 = G3N * G3K * 2;                  // 16 KB
+constexpr uint32_t kStage3 = 2 * kA3 + 2 * kB3;          // 48 KB
+constexpr uint32_t kC3 = 128 * 32 * 4;                   // 16 KB C chunk
+constexpr int kG3Threads = 192;
+
+__device__ __forceinline__ uint64_t smem_desc_sw64(uint32_t saddr) {
+  // K-major operand tile, 64-byte swizzle: rows of 64 B, 8-row atoms of
+  // 512 B (stride byte offset), descriptor version 1 (tcgen05)
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(512 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)4 << 61);
+}
+
+__device__ __forceinline__ void named_bar_epi() {
+  asm volatile("bar.sync 1, 128;" ::: "memory");
+}
+// Barrier of the 128 epilogue threads that also ORs a flag across them, so
+// every thread takes the same branch after it.
+__device__ __forceinline__ bool named_bar_epi_or(bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.or.pred q, 1, 128, p;\n selp.u32 %0, 1, "
+      "0, q;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)v)
+      : "memory");
+  return r != 0;
+}
+
+__global__ void __launch_bounds__(kG3Threads, 1)
+    k_gemm3(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
+            const __grid_constant__ CUtensorMap mBhi, const __grid_constant__ CUtensorMap mBlo,
+            const __grid_constant__ CUtensorMap mC, int crow0, int ccol0, int brow0, int M, int Nc,
+            int K, DevErr* err) {
+  extern __shared__ __align__(1024) uint8_t g3sm[];
+  const uint32_t base_s = smem_u32(g3sm);
+  const uint32_t pad = (1024 - (base_s & 1023)) & 1023;
+  uint8_t* sm = g3sm + pad;                    // [G3S stages][Ahi Alo Bhi Blo]
+  uint8_t* csm = sm + G3S * kStage3;           // 2 C chunk buffers, 1024-aligned
+  uint64_t* full = reinterpret_cast<uint64_t*>(csm + 2 * kC3);
+  uint64_t* empty = full + G3S;
+  uint64_t* tfull = empty + G3S;
+  uint64_t* tempty = tfull + 2;
+  uint64_t* cfull = tempty + 2;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(cfull + 2);
+  int* abort_flag = reinterpret_cast<int*>(tslot + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tiles_m = (M + G3M - 1) / G3M, tiles_n = (Nc + G3N - 1) / G3N;
+  const int ntiles = tiles_m * tiles_n;
+  const int nk = K / G3K;
+
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tslot)),
+                 "r"(512)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int i = 0; i < G3S; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&tfull[i], 1);
+      mbar_init(&tempty[i], 4);  // one arrival per epilogue warp
+      mbar_init(&cfull[i], 1);
+    }
+    *abort_flag = 0;
+    fence_mbar_init();
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+  volatile int* vabort = abort_flag;
+
+  if (warp == 0) {
+    // ------------------------------------------------ TMA producer
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      for (int t = blockIdx.x; t < ntiles && !*vabort; t += gridDim.x) {
+        const int m0 = (t % tiles_m) * G3M, n0 = (t / tiles_m) * G3N;
+        for (int kb = 0; kb < nk; ++kb) {
+          if (!mbar_wait_bounded(&empty[stage], phase ^ 1u)) {
+            *vabort = 1;
+            dev_fail(err, WBEM_ERR_TIMEOUT, 81, blockIdx.x, t);
+            break;
+          }
+          const uint32_t st = smem_u32(sm + (size_t)stage * kStage3);
+          mbar_arrive_expect_tx(&full[stage], kStage3);
+          tma_load_2d(st, &mAhi, kb * G3K, m0, &full[stage]);
+          tma_load_2d(st + kA3, &mAlo, kb * G3K, m0, &full[stage]);
+          tma_load_2d(st + 2 * kA3, &mBhi, kb * G3K, brow0 + n0, &full[stage]);
+          tma_load_2d(st + 2 * kA3 + kB3, &mBlo, kb * G3K, brow0 + n0, &full[stage]);
+          if (++stage == G3S) {
+            stage = 0;
+            phase ^= 1u;
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      // D f32, A/B bf16, K-major both, N = 256, M = 128
+      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(G3N >> 3) << 17) |
+                             ((uint32_t)(G3M >> 4) << 24);
+      int stage = 0;
+      uint32_t phase = 0;
+      int acc = 0;
+      uint32_t aphase = 0;
+      for (int t = blockIdx.x; t < ntiles && !*vabort; t += gridDim.x) {
+        if (!mbar_wait_bounded(&tempty[acc], aphase ^ 1u)) {
+          *vabort = 1;
+          dev_fail(err, WBEM_ERR_TIMEOUT, 82, blockIdx.x, t);
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t d = tmem + (uint32_t)(acc * G3N);
+        bool ok = true;
+        for (int kb = 0; kb < nk; ++kb) {
+          if (!mbar_wait_bounded(&full[stage], phase)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t st = smem_u32(sm + (size_t)stage * kStage3);
+          const uint64_t dAh = smem_desc_sw64(st);
+          const uint64_t dAl = smem_desc_sw64(st + kA3);
+          const uint64_t dBh = smem_desc_sw64(st + 2 * kA3);
+          const uint64_t dBl = smem_desc_sw64(st + 2 * kA3 + kB3);
+#pragma unroll
+          for (int kk = 0; kk < G3K / 16; ++kk) {
+            const uint64_t adv = (uint64_t)(kk * 2);  // 32 bytes along K, in 16-byte units
+            umma_bf16(d, dAh + adv, dBh + adv, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+            umma_bf16(d, dAh + adv, dBl + adv, idesc, 1u);
+            umma_bf16(d, dAl + adv, dBh + adv, idesc, 1u);
+          }
+          umma_commit(&empty[stage]);
+          if (++stage == G3S) {
+            stage = 0;
+            phase ^= 1u;
+          }
+        }
+        if (!ok) {
+          *vabort = 1;
+          dev_fail(err, WBEM_ERR_TIMEOUT, 83, blockIdx.x, t);
+          break;
+        }
+        umma_commit(&tfull[acc]);  // arrives once the tile's MMAs have completed
+        if (++acc == 2) {
+          acc = 0;
+          aphase ^= 1u;
+        }
+      }
+    }
+  } else {
+    // ------------------------------------------------ epilogue (warps 2..5)
+    const int etid = tid - 64;          // 0..127
+    const int q = warp & 3;             // TMEM lane quarter this warp may access
+    const int r = q * 32 + lane;        // tile row = TMEM lane
+    const uint32_t rsw = (uint32_t)(r & 7);
+    int acc = 0;
+    uint32_t aphase = 0;
+    uint32_t cph[2] = {0u, 0u};
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+      const int m0 = (t % tiles_m) * G3M, n0 = (t / tiles_m) * G3N;
+      const int nch = min(G3N / 32, (Nc - n0 + 31) / 32);
+      if (etid == 0) {
+        for (int j = 0; j < 2 && j < nch; ++j) {
+          mbar_arrive_expect_tx(&cfull[j], kC3);
+          tma_load_2d(smem_u32(csm + j * kC3), &mC, ccol0 + n0 + 32 * j, crow0 + m0, &cfull[j]);
+        }
+      }
+      if (!mbar_wait_bounded(&tfull[acc], aphase)) {
+        *vabort = 1;
+        dev_fail(err, WBEM_ERR_TIMEOUT, 84, blockIdx.x, t);
+      }
+      if (named_bar_epi_or(*vabort != 0)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      bool stop = false;
+      for (int j = 0; j < nch; ++j) {
+        const int b = j & 1;
+        if (!mbar_wait_bounded(&cfull[b], cph[b])) {
+          *vabort = 1;
+          dev_fail(err, WBEM_ERR_TIMEOUT, 85, blockIdx.x, t);
+        }
+        cph[b] ^= 1u;
+        if (named_bar_epi_or(*vabort != 0)) {
+          stop = true;
+          break;
+        }
+        uint32_t v[32];
+        const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * G3N + 32 * j);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+            "%11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, "
+            "%28, %29, %30, %31}, [%32];"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+              "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+              "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]),
+              "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),
+              "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]),
+              "=r"(v[31])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        uint8_t* row = csm + b * kC3 + (size_t)r * 128;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          float4* p4 = reinterpret_cast<float4*>(row + (((uint32_t)c ^ rsw) << 4));
+          float4 o = *p4;
+          o.x -= __uint_as_float(v[4 * c + 0]);
+          o.y -= __uint_as_float(v[4 * c + 1]);
+          o.z -= __uint_as_float(v[4 * c + 2]);
+          o.w -= __uint_as_float(v[4 * c + 3]);
+          *p4 = o;
+        }
+        fence_proxy_async_smem();
+        named_bar_epi();
+        if (etid == 0) {
+          tma_store_2d(&mC, ccol0 + n0 + 32 * j, crow0 + m0, smem_u32(csm + b * kC3));
+          asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+          // the buffer is refilled two chunks ahead once the store has read it
+          asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+          if (j + 2 < nch) {
+            mbar_arrive_expect_tx(&cfull[b], kC3);
+            tma_load_2d(smem_u32(csm + b * kC3), &mC, ccol0 + n0 + 32 * (j + 2), crow0 + m0,
+                        &cfull[b]);
+          }
+        }
+      }
+      if (stop) break;
+      // accumulator read out: release it to the MMA warp
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&tempty[acc]);
+      if (++acc == 2) {
+        acc = 0;
+        aphase ^= 1u;
+      }
+    }
+    if (etid == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (warp == 1)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512)
+                 : "memory");
+}
+
+static size_t gemm3_smem() { return (size_t)G3S * kStage3 + 2 * kC3 + 1024 + 256; }
+
 static size_t gemm_smem() { return 2 * (size_t)kStageBytes + kCBytes + 1024 + 128; }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (the
@@ -657,6 +983,30 @@ struct GemmMaps {
   CUtensorMap Ahi, Alo, Bhi, Blo;
 };
 
+// The four BF16 planes of a split buffer (A hi, A lo, B hi, B lo; each rows x
+// kdim, K-major) as operands of k_gemm3: boxes of 32 K x 128 rows (A) and
+// 32 K x 256 rows (B), 64-byte swizzle.
+static bool encode_ops3(GemmMaps* mp, const uint16_t* ahi, const uint16_t* alo, size_t rows_a,
+                        const uint16_t* bhi, const uint16_t* blo, size_t rows_b, int kdim) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
+  if (!enc) return false;
+  auto one = [&](CUtensorMap* map, const uint16_t* b, size_t rows, int box_rows) {
+    const cuuint64_t dims[2] = {(cuuint64_t)kdim, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)kdim * 2};
+    const cuuint32_t box[2] = {(cuuint32_t)G3K, (cuuint32_t)box_rows};
+    const cuuint32_t es[2] = {1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)b, dims, strides, box, es,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  };
+  return one(&mp->Ahi, ahi, rows_a, G3M) && one(&mp->Alo, alo, rows_a, G3M) &&
+         one(&mp->Bhi, bhi, rows_b, G3N) && one(&mp->Blo, blo, rows_b, G3N);
+}
+static bool encode_split3(GemmMaps* mp, const uint16_t* base, size_t rows, int kdim) {
+  const size_t plane = rows * (size_t)kdim;
+  return encode_ops3(mp, base, base + plane, rows, base + 2 * plane, base + 3 * plane, rows, kdim);
+}
+
 // FP32 matrix (rows x cols, leading dimension ld floats, ld % 4 == 0) seen by
 // TMA in 128 x 32 boxes with 128-byte swizzle.
 static bool encode_cmap(CUtensorMap* map, const float* base, int rows, int cols, int ld) {
@@ -678,6 +1028,28 @@ static bool encode_cmap(CUtensorMap* map, const float* base, int rows, int cols,
 // addressed through its tensor map; rows and columns past the map's extent are
 // neither read (zero fill) nor written (clipped), so tiles may overhang M / Nc
 // only where the region ends at the matrix edge.
+static cudaError_t run_gemm3(const GemmMaps& mp, const CUtensorMap& cmap, int crow0, int ccol0,
+                             int brow0, int M, int Nc, int K, DevErr* err, cudaStream_t s) {
+  static bool attr = false;
+  static int sms = 0;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_gemm3, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)gemm3_smem());
+    if (e != cudaSuccess) return e;
+    int dev = 0;
+    e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  const int ntiles = ((M + G3M - 1) / G3M) * ((Nc + G3N - 1) / G3N);
+  const int grid = std::min(ntiles, sms);
+  k_gemm3<<<grid, kG3Threads, gemm3_smem(), s>>>(mp.Ahi, mp.Alo, mp.Bhi, mp.Blo, cmap, crow0, ccol0,
+                                                 brow0, M, Nc, K, err);
+  return cudaGetLastError();
+}
+
 static cudaError_t run_gemm(const GemmMaps& mp, const CUtensorMap& cmap, int crow0, int ccol0,
                             int brow0, int M, int Nc, int K, DevErr* err, cudaStream_t s) {
   static bool attr = false;
@@ -976,19 +1348,13 @@ int factor_mixed(wbem_context* h) {
     WB_CU(cudaMemsetAsync(L.split, 0, sizeof(uint16_t) * 4 * rows * kNB, h->stream));
     L.epoch = 0;
     uint16_t* b1 = L.split;
-    if (!encode_map(&L.maps.Ahi, b1, (int)rows, kNB, GM) ||
-        !encode_map(&L.maps.Alo, b1 + rows * kNB, (int)rows, kNB, GM) ||
-        !encode_map(&L.maps.Bhi, b1 + 2 * rows * kNB, (int)rows, kNB, GN) ||
-        !encode_map(&L.maps.Blo, b1 + 3 * rows * kNB, (int)rows, kNB, GN))
+    if (!encode_split3(&L.maps, b1, rows, kNB))
       return fail(h, WBEM_ERR_CUDA, "cuTensorMapEncodeTiled failed");
     for (int b = 0; b < 2; ++b) {
       uint16_t* b2 = L.split2[b];
       WB_CU(cudaMemsetAsync(b2, 0, sizeof(uint16_t) * 4 * rows * kNB2, h->stream));
       GemmMaps& m2 = L.maps2[b];
-      if (!encode_map(&m2.Ahi, b2, (int)rows, kNB2, GM) ||
-          !encode_map(&m2.Alo, b2 + rows * kNB2, (int)rows, kNB2, GM) ||
-          !encode_map(&m2.Bhi, b2 + 2 * rows * kNB2, (int)rows, kNB2, GN) ||
-          !encode_map(&m2.Blo, b2 + 3 * rows * kNB2, (int)rows, kNB2, GN))
+      if (!encode_split3(&m2, b2, rows, kNB2))
         return fail(h, WBEM_ERR_CUDA, "cuTensorMapEncodeTiled failed");
     }
     int lo = 0, hi = 0;
@@ -1056,19 +1422,19 @@ int factor_mixed(wbem_context* h) {
       const PanelArgs pc{A + (size_t)k1 * ld + k0, ld, L.uinv + bo, kNB, A + (size_t)k1 * ld + k0,
                          ld, m, kNB, kNB, k1, k0, 0, 0};
       pb(h->prof_panel, sp);
-      WB_CU(run_panel(pc, Lin, p1 < N ? L21 : none, sp));
+      WB_CU((run_panel_tile<64, 128, false>(pc, Lin, p1 < N ? L21 : none, sp)));
       pe(h->prof_panel, sp, 0.0);
       h->launches++;
       if (k1 < p1) {
         const int w = p1 - k1;
         // U_kj = inv(L_kk) A_kj for the panel's remaining columns, in place
-        const PanelArgs pr{L.linv + bo, kNB, A + (size_t)k0 * ld + k1, ld, A + (size_t)k0 * ld + k1,
+        const PanelArgs pr{L.linvT + bo, kNB, A + (size_t)k0 * ld + k1, ld, A + (size_t)k0 * ld + k1,
                            ld, kNB, w, kNB, k0, k1, 0, 1};
         pb(h->prof_panel, sp);
-        WB_CU(run_panel(pr, Uin, none, sp));
+        WB_CU((run_panel_tile<128, 64, true>(pr, Uin, none, sp)));
         pe(h->prof_panel, sp, 0.0);
         pb(h->prof_gemm, sp);
-        WB_CU(run_gemm(L.maps, L.cmap, k1, k1, 0, m, w, kNB, h->d_err, sp));
+        WB_CU(run_gemm3(L.maps, L.cmap, k1, k1, 0, m, w, kNB, h->d_err, sp));
         pe(h->prof_gemm, sp, gemm_flop(m, w, kNB));
         h->launches += 2;
       }
@@ -1087,13 +1453,13 @@ int factor_mixed(wbem_context* h) {
         // A_kj -= L_k,[p0,k0) U_[p0,k0),j for the columns right of the panel
         const PanelArgs pu{A + (size_t)k0 * ld + p0, ld, A + (size_t)p0 * ld + p1, ld,
                            A + (size_t)k0 * ld + p1, ld, kNB, n, k0 - p0, k0, p1, 1, 0};
-        WB_CU(run_panel(pu, none, none, sp));
+        WB_CU((run_panel_tile<128, 64, false>(pu, none, none, sp)));
         h->launches++;
       }
       const SplitOut U12{b2 + 2 * rows * kNB2, b2 + 3 * rows * kNB2, p1, kNB2, k0 - p0};
-      const PanelArgs pr{L.linv + bo, kNB, A + (size_t)k0 * ld + p1, ld, A + (size_t)k0 * ld + p1, ld,
-                         kNB, n, kNB, k0, p1, 0, 1};
-      WB_CU(run_panel(pr, U12, none, sp));
+      const PanelArgs pr{L.linvT + bo, kNB, A + (size_t)k0 * ld + p1, ld, A + (size_t)k0 * ld + p1,
+                         ld, kNB, n, kNB, k0, p1, 0, 1};
+      WB_CU((run_panel_tile<128, 64, true>(pr, U12, none, sp)));
       pe(h->prof_panel, sp, 0.0);
       h->launches++;
       WB_CU(cudaGetLastError());
@@ -1102,14 +1468,14 @@ int factor_mixed(wbem_context* h) {
     // the next panel's columns on s_panel, the rest on s_trail
     const int p2 = std::min(N, p1 + kNB2);
     pb(h->prof_gemm, sp);
-    WB_CU(run_gemm(L.maps2[buf], L.cmap, p1, p1, 0, n, p2 - p1, p1 - p0, h->d_err, sp));
+    WB_CU(run_gemm3(L.maps2[buf], L.cmap, p1, p1, 0, n, p2 - p1, p1 - p0, h->d_err, sp));
     pe(h->prof_gemm, sp, gemm_flop(n, p2 - p1, p1 - p0));
     h->launches++;
     if (p2 < N) {
       WB_CU(cudaEventRecord(L.ev_row, sp));
       WB_CU(cudaStreamWaitEvent(st, L.ev_row, 0));
       pb(h->prof_gemm, st);
-      WB_CU(run_gemm(L.maps2[buf], L.cmap, p1, p2, p2 - p1, n, N - p2, p1 - p0, h->d_err, st));
+      WB_CU(run_gemm3(L.maps2[buf], L.cmap, p1, p2, p2 - p1, n, N - p2, p1 - p0, h->d_err, st));
       pe(h->prof_gemm, st, gemm_flop(n, N - p2, p1 - p0));
       WB_CU(cudaEventRecord(L.ev_trail, st));
       trail_pending = true;
@@ -1165,7 +1531,7 @@ __global__ void k_split_rows(int rows, int K, const float* __restrict__ X, uint1
 extern "C" int wbem_test_gemm_bf16x3(int M, int Nc, int K, const float* dA, const float* dB,
                                      float* dC) {
   using namespace wbem;
-  if (M < 1 || Nc < 1 || K < GK || K % GK) return WBEM_ERR_ARG;
+  if (M < 1 || Nc < 1 || K < G3K || K % G3K) return WBEM_ERR_ARG;
   const int rA = M + GM, rB = Nc + GN;
   uint16_t* buf = nullptr;
   if (cudaMalloc(&buf, sizeof(uint16_t) * 2 * ((size_t)rA + rB) * K) != cudaSuccess) return WBEM_ERR_NOMEM;
@@ -1178,9 +1544,7 @@ extern "C" int wbem_test_gemm_bf16x3(int M, int Nc, int K, const float* dA, cons
   k_split_rows<<<(unsigned)(((size_t)Nc * K + 255) / 256), 256>>>(Nc, K, dB, Bhi, Blo);
   GemmMaps mp;
   int st = WBEM_OK;
-  if (!encode_map(&mp.Ahi, Ahi, rA, K, GM) || !encode_map(&mp.Alo, Alo, rA, K, GM) ||
-      !encode_map(&mp.Bhi, Bhi, rB, K, GN) || !encode_map(&mp.Blo, Blo, rB, K, GN))
-    st = WBEM_ERR_CUDA;
+  if (!encode_ops3(&mp, Ahi, Alo, rA, Bhi, Blo, rB, K)) st = WBEM_ERR_CUDA;
   // C through a padded copy (TMA needs 16-byte aligned row strides)
   const int ldc = (Nc + 31) / 32 * 32;
   float* Cp = nullptr;
@@ -1195,7 +1559,7 @@ extern "C" int wbem_test_gemm_bf16x3(int M, int Nc, int K, const float* dA, cons
   if (st == WBEM_OK && cudaMalloc(&err, sizeof(DevErr)) != cudaSuccess) st = WBEM_ERR_NOMEM;
   if (st == WBEM_OK) {
     cudaMemset(err, 0, sizeof(DevErr));
-    if (run_gemm(mp, cmap, 0, 0, 0, M, Nc, K, err, 0) != cudaSuccess) st = WBEM_ERR_CUDA;
+    if (run_gemm3(mp, cmap, 0, 0, 0, M, Nc, K, err, 0) != cudaSuccess) st = WBEM_ERR_CUDA;
     if (cudaDeviceSynchronize() != cudaSuccess) st = WBEM_ERR_CUDA;
     DevErr de{};
     cudaMemcpy(&de, err, sizeof de, cudaMemcpyDeviceToHost);
