@@ -476,15 +476,8 @@ static cudaError_t run_panel_tile(const PanelArgs& pa, const SplitOut& s1, const
 }
 
 // ------------------------------------------------------- tcgen05 BF16x3 GEMM
-constexpr int GM = 128, GN = 128, GK = 64;
-constexpr uint32_t kStageBytes = (GM + GM + GN + GN) * GK * 2;  // Ahi Alo Bhi Blo: 96 KB
-
-__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
-  // K-major operand tile, 128-byte swizzle: rows of 128 B, 8-row atoms of
-  // 1024 B (stride byte offset), descriptor version 1 (tcgen05)
-  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
-         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
-}
+// rows of padding after each split buffer and each padded test operand
+constexpr int kSplitPad = 128;
 
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y,
                                             uint64_t* bar) {
@@ -511,166 +504,12 @@ __device__ __forceinline__ void umma_commit(uint64_t* bar) {
       : "memory");
 }
 
-// C tile staging: 4 sub-tiles of 128 rows x 32 FP32 columns, 128-byte
-// swizzled (16-byte chunk index XOR row % 8), loaded by TMA while the MMAs
-// run and stored back by TMA after the subtraction.
-constexpr uint32_t kCSubBytes = GM * 32 * 4;   // 16 KB
-constexpr uint32_t kCBytes = 4 * kCSubBytes;    // 64 KB (GN = 128)
 
 __device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int y, uint32_t src) {
   asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
                    map),
                "r"(x), "r"(y), "r"(src)
                : "memory");
-}
-
-__global__ void __launch_bounds__(128, 1)
-    k_gemm_bf16x3(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
-                  const __grid_constant__ CUtensorMap mBhi, const __grid_constant__ CUtensorMap mBlo,
-                  const __grid_constant__ CUtensorMap mC, int crow0, int ccol0, int brow0, int K,
-                  DevErr* err) {
-  extern __shared__ __align__(1024) uint8_t gsm[];
-  const uint32_t base_s = smem_u32(gsm);
-  const uint32_t pad = (1024 - (base_s & 1023)) & 1023;
-  uint8_t* sm = gsm + pad;                 // [2 stages][Ahi Alo Bhi Blo] then C
-  uint8_t* csm = sm + 2 * kStageBytes;     // 4 x 16 KB, 1024-aligned
-  uint64_t* full = reinterpret_cast<uint64_t*>(csm + kCBytes);
-  uint64_t* empty = full + 2;
-  uint64_t* done = full + 4;
-  uint64_t* cbar = full + 5;
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(full + 6);
-  int* fail_flag = reinterpret_cast<int*>(full + 7);
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int m0 = blockIdx.x * GM, n0 = blockIdx.y * GN;
-
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-                     smem_u32(tslot)),
-                 "r"(GN)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-  }
-  if (tid == 0) {
-    mbar_init(&full[0], 1);
-    mbar_init(&full[1], 1);
-    mbar_init(&empty[0], 1);
-    mbar_init(&empty[1], 1);
-    mbar_init(done, 1);
-    mbar_init(cbar, 1);
-    *fail_flag = 0;
-    fence_mbar_init();
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  const uint32_t tmem = *tslot;
-  const int nk = K / GK;
-  // instruction descriptor: D f32, A/B bf16, K-major both, N = GN, M = GM
-  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(GN >> 3) << 17) |
-                         ((uint32_t)(GM >> 4) << 24);
-
-  if (tid == 0) {
-    // the C tile (read-modify-write target) streams in while the MMAs run
-    mbar_arrive_expect_tx(cbar, kCBytes);
-    for (int j = 0; j < 4; ++j)
-      tma_load_2d(smem_u32(csm + j * kCSubBytes), &mC, ccol0 + n0 + 32 * j, crow0 + m0, cbar);
-    auto stage_ptr = [&](int s) { return smem_u32(sm + (size_t)s * kStageBytes); };
-    auto load = [&](int c) {
-      const int s = c & 1;
-      const uint32_t st = stage_ptr(s);
-      mbar_arrive_expect_tx(&full[s], kStageBytes);
-      tma_load_2d(st, &mAhi, c * GK, m0, &full[s]);
-      tma_load_2d(st + GM * GK * 2, &mAlo, c * GK, m0, &full[s]);
-      tma_load_2d(st + 2 * GM * GK * 2, &mBhi, c * GK, brow0 + n0, &full[s]);
-      tma_load_2d(st + 2 * GM * GK * 2 + GN * GK * 2, &mBlo, c * GK, brow0 + n0, &full[s]);
-    };
-    bool ok = true;
-    load(0);
-    if (nk > 1) load(1);
-    for (int c = 0; c < nk && ok; ++c) {
-      const int s = c & 1;
-      if (!mbar_wait_bounded(&full[s], (uint32_t)((c >> 1) & 1))) {
-        ok = false;
-        break;
-      }
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t st = stage_ptr(s);
-      const uint64_t dAh = smem_desc_sw128(st);
-      const uint64_t dAl = smem_desc_sw128(st + GM * GK * 2);
-      const uint64_t dBh = smem_desc_sw128(st + 2 * GM * GK * 2);
-      const uint64_t dBl = smem_desc_sw128(st + 2 * GM * GK * 2 + GN * GK * 2);
-#pragma unroll
-      for (int kk = 0; kk < GK / 16; ++kk) {
-        const uint64_t adv = (uint64_t)(kk * 2);  // 32 bytes along K, in 16-byte units
-        umma_bf16(tmem, dAh + adv, dBh + adv, idesc, (c > 0 || kk > 0) ? 1u : 0u);
-        umma_bf16(tmem, dAh + adv, dBl + adv, idesc, 1u);
-        umma_bf16(tmem, dAl + adv, dBh + adv, idesc, 1u);
-      }
-      umma_commit(&empty[s]);
-      if (c + 2 < nk) {
-        if (!mbar_wait_bounded(&empty[s], (uint32_t)((c >> 1) & 1))) {
-          ok = false;
-          break;
-        }
-        load(c + 2);
-      }
-    }
-    if (!ok) {
-      *fail_flag = 1;
-      dev_fail(err, WBEM_ERR_TIMEOUT, 61, blockIdx.x, blockIdx.y);
-    }
-    umma_commit(done);  // arrives once all issued MMAs have completed
-  }
-  __syncwarp();
-  const bool ok_done = mbar_wait_bounded(done, 0u);
-  const bool ok_c = mbar_wait_bounded(cbar, 0u);
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  __syncthreads();
-  const bool good = ok_done && ok_c && *fail_flag == 0;
-  if (good) {
-    const int r = warp * 32 + lane;  // tile row = TMEM lane
-    const uint32_t rsw = (uint32_t)(r & 7);
-    for (int cc = 0; cc < GN; cc += 16) {
-      uint32_t v[16];
-      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cc;
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
-          "%12, %13, %14, %15}, [%16];"
-          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-            "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
-            "=r"(v[14]), "=r"(v[15])
-          : "r"(taddr));
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      uint8_t* sub = csm + (cc >> 5) * kCSubBytes + (size_t)r * 128;
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const uint32_t chunk = (uint32_t)(((cc & 31) >> 2) + u);  // logical 16-byte chunk
-        float4* q = reinterpret_cast<float4*>(sub + ((chunk ^ rsw) << 4));
-        float4 o = *q;
-        o.x -= __uint_as_float(v[4 * u + 0]);
-        o.y -= __uint_as_float(v[4 * u + 1]);
-        o.z -= __uint_as_float(v[4 * u + 2]);
-        o.w -= __uint_as_float(v[4 * u + 3]);
-        *q = o;
-      }
-    }
-  } else if (tid == 0) {
-    dev_fail(err, WBEM_ERR_TIMEOUT, 62, blockIdx.x, blockIdx.y);
-  }
-  fence_proxy_async_smem();
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  if (tid == 0) {
-    if (good) {
-      for (int j = 0; j < 4; ++j)
-        tma_store_2d(&mC, ccol0 + n0 + 32 * j, crow0 + m0, smem_u32(csm + j * kCSubBytes));
-      asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-    }
-    asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-  }
-  if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(GN)
-                 : "memory");
 }
 
 // ------------------------------------------------- persistent tcgen05 GEMM
@@ -722,7 +561,7 @@ __device__ __forceinline__ bool named_bar_epi_or(bool v) {
 }
 
 __global__ void __launch_bounds__(kG3Threads, 1)
-    k_gemm3(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
+    k_gemm_bf16x3(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
             const __grid_constant__ CUtensorMap mBhi, const __grid_constant__ CUtensorMap mBlo,
             const __grid_constant__ CUtensorMap mC, int crow0, int ccol0, int brow0, int M, int Nc,
             int K, DevErr* err) {
@@ -945,9 +784,8 @@ __global__ void __launch_bounds__(kG3Threads, 1)
                  : "memory");
 }
 
-static size_t gemm3_smem() { return (size_t)G3S * kStage3 + 2 * kC3 + 1024 + 256; }
+static size_t gemm_smem() { return (size_t)G3S * kStage3 + 2 * kC3 + 1024 + 256; }
 
-static size_t gemm_smem() { return 2 * (size_t)kStageBytes + kCBytes + 1024 + 128; }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (the
 // library does not link libcuda directly, so it loads on hosts without a
@@ -965,26 +803,12 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-static bool encode_map(CUtensorMap* map, const uint16_t* base, int rows, int kdim, int box_rows) {
-  const cuuint64_t dims[2] = {(cuuint64_t)kdim, (cuuint64_t)rows};
-  const cuuint64_t strides[1] = {(cuuint64_t)kdim * 2};
-  const cuuint32_t box[2] = {(cuuint32_t)GK, (cuuint32_t)box_rows};
-  const cuuint32_t es[2] = {1, 1};
-  PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
-  if (!enc) return false;
-  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)base, dims,
-                                      strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                                      CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  return r == CUDA_SUCCESS;
-}
-
 struct GemmMaps {
   CUtensorMap Ahi, Alo, Bhi, Blo;
 };
 
 // The four BF16 planes of a split buffer (A hi, A lo, B hi, B lo; each rows x
-// kdim, K-major) as operands of k_gemm3: boxes of 32 K x 128 rows (A) and
+// kdim, K-major) as operands of k_gemm_bf16x3: boxes of 32 K x 128 rows (A) and
 // 32 K x 256 rows (B), 64-byte swizzle.
 static bool encode_ops3(GemmMaps* mp, const uint16_t* ahi, const uint16_t* alo, size_t rows_a,
                         const uint16_t* bhi, const uint16_t* blo, size_t rows_b, int kdim) {
@@ -1012,7 +836,7 @@ static bool encode_split3(GemmMaps* mp, const uint16_t* base, size_t rows, int k
 static bool encode_cmap(CUtensorMap* map, const float* base, int rows, int cols, int ld) {
   const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
   const cuuint64_t strides[1] = {(cuuint64_t)ld * 4};
-  const cuuint32_t box[2] = {32u, (cuuint32_t)GM};
+  const cuuint32_t box[2] = {32u, 128u};
   const cuuint32_t es[2] = {1, 1};
   PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
   if (!enc || (ld & 3)) return false;
@@ -1028,13 +852,13 @@ static bool encode_cmap(CUtensorMap* map, const float* base, int rows, int cols,
 // addressed through its tensor map; rows and columns past the map's extent are
 // neither read (zero fill) nor written (clipped), so tiles may overhang M / Nc
 // only where the region ends at the matrix edge.
-static cudaError_t run_gemm3(const GemmMaps& mp, const CUtensorMap& cmap, int crow0, int ccol0,
+static cudaError_t run_gemm(const GemmMaps& mp, const CUtensorMap& cmap, int crow0, int ccol0,
                              int brow0, int M, int Nc, int K, DevErr* err, cudaStream_t s) {
   static bool attr = false;
   static int sms = 0;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_gemm3, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)gemm3_smem());
+    cudaError_t e = cudaFuncSetAttribute(k_gemm_bf16x3, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)gemm_smem());
     if (e != cudaSuccess) return e;
     int dev = 0;
     e = cudaGetDevice(&dev);
@@ -1045,25 +869,11 @@ static cudaError_t run_gemm3(const GemmMaps& mp, const CUtensorMap& cmap, int cr
   }
   const int ntiles = ((M + G3M - 1) / G3M) * ((Nc + G3N - 1) / G3N);
   const int grid = std::min(ntiles, sms);
-  k_gemm3<<<grid, kG3Threads, gemm3_smem(), s>>>(mp.Ahi, mp.Alo, mp.Bhi, mp.Blo, cmap, crow0, ccol0,
+  k_gemm_bf16x3<<<grid, kG3Threads, gemm_smem(), s>>>(mp.Ahi, mp.Alo, mp.Bhi, mp.Blo, cmap, crow0, ccol0,
                                                  brow0, M, Nc, K, err);
   return cudaGetLastError();
 }
 
-static cudaError_t run_gemm(const GemmMaps& mp, const CUtensorMap& cmap, int crow0, int ccol0,
-                            int brow0, int M, int Nc, int K, DevErr* err, cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_gemm_bf16x3, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)gemm_smem());
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
-  dim3 grid((M + GM - 1) / GM, (Nc + GN - 1) / GN);
-  k_gemm_bf16x3<<<grid, 128, gemm_smem(), s>>>(mp.Ahi, mp.Alo, mp.Bhi, mp.Blo, cmap, crow0, ccol0,
-                                               brow0, K, err);
-  return cudaGetLastError();
-}
 
 // ------------------------------------------------------------ triangular solves
 // One cooperative launch per triangular sweep: CTA k owns block row k. It
@@ -1210,7 +1020,7 @@ struct LuState {
   float* uinv = nullptr;
   float* linvT = nullptr;  // column-major copies
   float* uinvT = nullptr;
-  uint16_t* split = nullptr;  // inner (K = 128) Lhi, Llo, Uhi, Ulo: each (N + GN) x kNB
+  uint16_t* split = nullptr;  // inner (K = 128) Lhi, Llo, Uhi, Ulo: each (N + kSplitPad) x kNB
   // outer (K = kNB2) L21hi, L21lo, U12Thi, U12Tlo, two sets: the trailing
   // update of outer panel P reads set P % 2 while panel P + 1 writes the other
   uint16_t* split2[2] = {nullptr, nullptr};
@@ -1333,7 +1143,7 @@ int factor_mixed(wbem_context* h) {
   if (!encode_cmap(&L.cmap, h->d_lu, N, N, ld))
     return fail(h, WBEM_ERR_CUDA, "cuTensorMapEncodeTiled (LU buffer) failed");
   const int nblk = (N + kNB - 1) / kNB;
-  const size_t rows = (size_t)N + GN;
+  const size_t rows = (size_t)N + kSplitPad;
   if (!L.linv) {
     WB_CHK(dev_alloc(h, &L.linv, (size_t)nblk * kNB * kNB));
     WB_CHK(dev_alloc(h, &L.uinv, (size_t)nblk * kNB * kNB));
@@ -1434,7 +1244,7 @@ int factor_mixed(wbem_context* h) {
         WB_CU((run_panel_tile<128, 64, true>(pr, Uin, none, sp)));
         pe(h->prof_panel, sp, 0.0);
         pb(h->prof_gemm, sp);
-        WB_CU(run_gemm3(L.maps, L.cmap, k1, k1, 0, m, w, kNB, h->d_err, sp));
+        WB_CU(run_gemm(L.maps, L.cmap, k1, k1, 0, m, w, kNB, h->d_err, sp));
         pe(h->prof_gemm, sp, gemm_flop(m, w, kNB));
         h->launches += 2;
       }
@@ -1468,14 +1278,14 @@ int factor_mixed(wbem_context* h) {
     // the next panel's columns on s_panel, the rest on s_trail
     const int p2 = std::min(N, p1 + kNB2);
     pb(h->prof_gemm, sp);
-    WB_CU(run_gemm3(L.maps2[buf], L.cmap, p1, p1, 0, n, p2 - p1, p1 - p0, h->d_err, sp));
+    WB_CU(run_gemm(L.maps2[buf], L.cmap, p1, p1, 0, n, p2 - p1, p1 - p0, h->d_err, sp));
     pe(h->prof_gemm, sp, gemm_flop(n, p2 - p1, p1 - p0));
     h->launches++;
     if (p2 < N) {
       WB_CU(cudaEventRecord(L.ev_row, sp));
       WB_CU(cudaStreamWaitEvent(st, L.ev_row, 0));
       pb(h->prof_gemm, st);
-      WB_CU(run_gemm3(L.maps2[buf], L.cmap, p1, p2, p2 - p1, n, N - p2, p1 - p0, h->d_err, st));
+      WB_CU(run_gemm(L.maps2[buf], L.cmap, p1, p2, p2 - p1, n, N - p2, p1 - p0, h->d_err, st));
       pe(h->prof_gemm, st, gemm_flop(n, N - p2, p1 - p0));
       WB_CU(cudaEventRecord(L.ev_trail, st));
       trail_pending = true;
@@ -1532,7 +1342,7 @@ extern "C" int wbem_test_gemm_bf16x3(int M, int Nc, int K, const float* dA, cons
                                      float* dC) {
   using namespace wbem;
   if (M < 1 || Nc < 1 || K < G3K || K % G3K) return WBEM_ERR_ARG;
-  const int rA = M + GM, rB = Nc + GN;
+  const int rA = M + kSplitPad, rB = Nc + kSplitPad;
   uint16_t* buf = nullptr;
   if (cudaMalloc(&buf, sizeof(uint16_t) * 2 * ((size_t)rA + rB) * K) != cudaSuccess) return WBEM_ERR_NOMEM;
   cudaMemset(buf, 0, sizeof(uint16_t) * 2 * ((size_t)rA + rB) * K);
@@ -1559,7 +1369,7 @@ extern "C" int wbem_test_gemm_bf16x3(int M, int Nc, int K, const float* dA, cons
   if (st == WBEM_OK && cudaMalloc(&err, sizeof(DevErr)) != cudaSuccess) st = WBEM_ERR_NOMEM;
   if (st == WBEM_OK) {
     cudaMemset(err, 0, sizeof(DevErr));
-    if (run_gemm3(mp, cmap, 0, 0, 0, M, Nc, K, err, 0) != cudaSuccess) st = WBEM_ERR_CUDA;
+    if (run_gemm(mp, cmap, 0, 0, 0, M, Nc, K, err, 0) != cudaSuccess) st = WBEM_ERR_CUDA;
     if (cudaDeviceSynchronize() != cudaSuccess) st = WBEM_ERR_CUDA;
     DevErr de{};
     cudaMemcpy(&de, err, sizeof de, cudaMemcpyDeviceToHost);
