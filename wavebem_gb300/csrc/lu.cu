@@ -43,32 +43,38 @@ constexpr int kNB2 = 512;  // outer block: K of the tensor-core trailing update
 // ------------------------------------------------------------------ input
 // LU input: hi part of the system operator, alpha on Neumann diagonals,
 // constrained rows replaced by e_i - sum_j c_ij e_j.
-__global__ void k_form_lu(int N, int ld, const float2* __restrict__ N2, const float2* __restrict__ D2,
-                          const uint8_t* __restrict__ mask, const double* __restrict__ alpha,
-                          const uint8_t* __restrict__ cflag, const int* __restrict__ cptr,
-                          const int* __restrict__ ccol, const double* __restrict__ cval,
-                          float* __restrict__ A) {
-  const int i = blockIdx.y;
+__global__ void __launch_bounds__(256)
+    k_form_lu(int N, int ld, const float2* __restrict__ N2, const float2* __restrict__ D2,
+              const uint8_t* __restrict__ mask, const double* __restrict__ alpha,
+              const uint8_t* __restrict__ cflag, const int* __restrict__ cptr,
+              const int* __restrict__ ccol, const double* __restrict__ cval,
+              float* __restrict__ A) {
+  // one CTA per row, four consecutive columns per thread and step
+  const int i = blockIdx.x;
   float* ar = A + (size_t)i * ld;
   if (cflag[i]) {
-    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < N; j += gridDim.x * blockDim.x)
-      ar[j] = (j == i) ? 1.f : 0.f;
+    for (int j = threadIdx.x; j < N; j += blockDim.x) ar[j] = (j == i) ? 1.f : 0.f;
     return;
   }
   const float2* nr = N2 + (size_t)i * N;
   const float2* dr = D2 + (size_t)i * N;
-  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < N; j += gridDim.x * blockDim.x) {
-    float v;
+  auto entry = [&](int j) -> float {
     if (mask[j]) {
-      const float2 d = dr[j];
-      v = -(float)((double)d.x + (double)d.y);
-    } else {
-      const float2 n = nr[j];
-      double s = (double)n.x + (double)n.y;
-      if (j == i) s += alpha[i];
-      v = (float)s;
+      const float2 d = __ldcs(dr + j);
+      return -(float)((double)d.x + (double)d.y);
     }
-    ar[j] = v;
+    const float2 n = __ldcs(nr + j);
+    double s = (double)n.x + (double)n.y;
+    if (j == i) s += alpha[i];
+    return (float)s;
+  };
+  for (int j = 4 * threadIdx.x; j < N; j += 4 * blockDim.x) {
+    if (j + 3 < N) {
+      const float4 v = make_float4(entry(j), entry(j + 1), entry(j + 2), entry(j + 3));
+      __stcs(reinterpret_cast<float4*>(ar + j), v);
+    } else {
+      for (int u = 0; j + u < N; ++u) ar[j + u] = entry(j + u);
+    }
   }
 }
 
@@ -518,24 +524,25 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int 
 // tiles (M fastest, so the CTAs in flight share B tiles and stream A); warp
 // roles:
 //   warp 0     TMA producer: A hi/lo (128 x 32) and B hi/lo (256 x 32) per
-//              K step into a 4-stage ring of 48 KB (64-byte swizzle);
+//              K step into a 3-stage ring of 48 KB (64-byte swizzle);
 //   warp 1     TMEM owner and MMA issuer: 6 tcgen05.mma (M 128, N 256, K 16)
 //              per K step into one of two 256-column FP32 accumulators;
-//   warps 2-5  epilogue: per 32-column chunk, the C chunk arrives by TMA into
-//              one of two 16 KB buffers (128-byte swizzle), each thread
-//              subtracts its TMEM row (tcgen05.ld 32x32b.x32), one thread
-//              stores the chunk back by TMA and refills the buffer two
-//              chunks ahead.
-// The epilogue of tile i overlaps the MMAs of tile i + 1 (the other
-// accumulator). Columns at or beyond Nc are neither read nor written (chunk
+//   warps 2-5, 6-9  two epilogue groups, one per accumulator (even / odd
+//              tiles of the CTA): per 32-column chunk, the C chunk arrives by
+//              TMA into one of the group's two 16 KB buffers (128-byte
+//              swizzle), each thread subtracts its TMEM row (tcgen05.ld
+//              32x32b.x32), one thread stores the chunk back by TMA and
+//              refills the buffer two chunks ahead.
+// Each group has two tiles' worth of MMA time for its epilogue, which is
+// bound by the latency of the C round trip. Columns at or beyond Nc are neither read nor written (chunk
 // granularity: Nc is a multiple of 32 or reaches the matrix edge); rows past
 // the matrix edge are clipped by the tensor map.
-constexpr int G3M = 128, G3N = 256, G3K = 32, G3S = 4;
+constexpr int G3M = 128, G3N = 256, G3K = 32, G3S = 3;
 constexpr uint32_t kA3 = G3M * G3K * 2;                  // 8 KB
 constexpr uint32_t kB3 = G3N * G3K * 2;                  // 16 KB
 constexpr uint32_t kStage3 = 2 * kA3 + 2 * kB3;          // 48 KB
 constexpr uint32_t kC3 = 128 * 32 * 4;                   // 16 KB C chunk
-constexpr int kG3Threads = 192;
+constexpr int kG3Threads = 320;
 
 __device__ __forceinline__ uint64_t smem_desc_sw64(uint32_t saddr) {
   // K-major operand tile, 64-byte swizzle: rows of 64 B, 8-row atoms of
@@ -544,18 +551,19 @@ __device__ __forceinline__ uint64_t smem_desc_sw64(uint32_t saddr) {
          ((uint64_t)1 << 46) | ((uint64_t)4 << 61);
 }
 
-__device__ __forceinline__ void named_bar_epi() {
-  asm volatile("bar.sync 1, 128;" ::: "memory");
+// Barrier of one epilogue group (named barrier 1 + group, 128 threads).
+__device__ __forceinline__ void named_bar_epi(int g) {
+  asm volatile("bar.sync %0, 128;" ::"r"(1 + g) : "memory");
 }
-// Barrier of the 128 epilogue threads that also ORs a flag across them, so
-// every thread takes the same branch after it.
-__device__ __forceinline__ bool named_bar_epi_or(bool v) {
+// The same barrier, also ORing a flag across the group, so every thread of
+// the group takes the same branch after it.
+__device__ __forceinline__ bool named_bar_epi_or(int g, bool v) {
   uint32_t r;
   asm volatile(
-      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.or.pred q, 1, 128, p;\n selp.u32 %0, 1, "
-      "0, q;\n}\n"
+      "{\n .reg .pred p, q;\n setp.ne.u32 p, %2, 0;\n bar.red.or.pred q, %1, 128, p;\n selp.u32 %0, "
+      "1, 0, q;\n}\n"
       : "=r"(r)
-      : "r"((uint32_t)v)
+      : "r"(1 + g), "r"((uint32_t)v)
       : "memory");
   return r != 0;
 }
@@ -569,13 +577,13 @@ __global__ void __launch_bounds__(kG3Threads, 1)
   const uint32_t base_s = smem_u32(g3sm);
   const uint32_t pad = (1024 - (base_s & 1023)) & 1023;
   uint8_t* sm = g3sm + pad;                    // [G3S stages][Ahi Alo Bhi Blo]
-  uint8_t* csm = sm + G3S * kStage3;           // 2 C chunk buffers, 1024-aligned
-  uint64_t* full = reinterpret_cast<uint64_t*>(csm + 2 * kC3);
+  uint8_t* csm = sm + G3S * kStage3;           // [2 groups][2] C chunk buffers, 1024-aligned
+  uint64_t* full = reinterpret_cast<uint64_t*>(csm + 4 * kC3);
   uint64_t* empty = full + G3S;
   uint64_t* tfull = empty + G3S;
   uint64_t* tempty = tfull + 2;
-  uint64_t* cfull = tempty + 2;
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(cfull + 2);
+  uint64_t* cfull = tempty + 2;                // [2 groups][2]
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(cfull + 4);
   int* abort_flag = reinterpret_cast<int*>(tslot + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int tiles_m = (M + G3M - 1) / G3M, tiles_n = (Nc + G3N - 1) / G3N;
@@ -596,9 +604,9 @@ __global__ void __launch_bounds__(kG3Threads, 1)
     }
     for (int i = 0; i < 2; ++i) {
       mbar_init(&tfull[i], 1);
-      mbar_init(&tempty[i], 4);  // one arrival per epilogue warp
-      mbar_init(&cfull[i], 1);
+      mbar_init(&tempty[i], 4);  // one arrival per warp of the epilogue group
     }
+    for (int i = 0; i < 4; ++i) mbar_init(&cfull[i], 1);
     *abort_flag = 0;
     fence_mbar_init();
   }
@@ -690,38 +698,41 @@ __global__ void __launch_bounds__(kG3Threads, 1)
       }
     }
   } else {
-    // ------------------------------------------------ epilogue (warps 2..5)
-    const int etid = tid - 64;          // 0..127
+    // ------------------------------------------------ epilogue (warps 2..9)
+    const int grp = (warp - 2) >> 2;    // group: accumulator and tile parity
+    const int etid = tid - 64 - 128 * grp;  // 0..127 within the group
     const int q = warp & 3;             // TMEM lane quarter this warp may access
     const int r = q * 32 + lane;        // tile row = TMEM lane
     const uint32_t rsw = (uint32_t)(r & 7);
-    int acc = 0;
+    const int acc = grp;
     uint32_t aphase = 0;
     uint32_t cph[2] = {0u, 0u};
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    uint8_t* gcsm = csm + (size_t)grp * 2 * kC3;
+    uint64_t* gcfull = cfull + 2 * grp;
+    for (int t = blockIdx.x + grp * gridDim.x; t < ntiles; t += 2 * gridDim.x) {
       const int m0 = (t % tiles_m) * G3M, n0 = (t / tiles_m) * G3N;
       const int nch = min(G3N / 32, (Nc - n0 + 31) / 32);
       if (etid == 0) {
         for (int j = 0; j < 2 && j < nch; ++j) {
-          mbar_arrive_expect_tx(&cfull[j], kC3);
-          tma_load_2d(smem_u32(csm + j * kC3), &mC, ccol0 + n0 + 32 * j, crow0 + m0, &cfull[j]);
+          mbar_arrive_expect_tx(&gcfull[j], kC3);
+          tma_load_2d(smem_u32(gcsm + j * kC3), &mC, ccol0 + n0 + 32 * j, crow0 + m0, &gcfull[j]);
         }
       }
       if (!mbar_wait_bounded(&tfull[acc], aphase)) {
         *vabort = 1;
         dev_fail(err, WBEM_ERR_TIMEOUT, 84, blockIdx.x, t);
       }
-      if (named_bar_epi_or(*vabort != 0)) break;
+      if (named_bar_epi_or(grp, *vabort != 0)) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       bool stop = false;
       for (int j = 0; j < nch; ++j) {
         const int b = j & 1;
-        if (!mbar_wait_bounded(&cfull[b], cph[b])) {
+        if (!mbar_wait_bounded(&gcfull[b], cph[b])) {
           *vabort = 1;
           dev_fail(err, WBEM_ERR_TIMEOUT, 85, blockIdx.x, t);
         }
         cph[b] ^= 1u;
-        if (named_bar_epi_or(*vabort != 0)) {
+        if (named_bar_epi_or(grp, *vabort != 0)) {
           stop = true;
           break;
         }
@@ -739,7 +750,7 @@ __global__ void __launch_bounds__(kG3Threads, 1)
               "=r"(v[31])
             : "r"(taddr));
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        uint8_t* row = csm + b * kC3 + (size_t)r * 128;
+        uint8_t* row = gcsm + b * kC3 + (size_t)r * 128;
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
           float4* p4 = reinterpret_cast<float4*>(row + (((uint32_t)c ^ rsw) << 4));
@@ -751,16 +762,16 @@ __global__ void __launch_bounds__(kG3Threads, 1)
           *p4 = o;
         }
         fence_proxy_async_smem();
-        named_bar_epi();
+        named_bar_epi(grp);
         if (etid == 0) {
-          tma_store_2d(&mC, ccol0 + n0 + 32 * j, crow0 + m0, smem_u32(csm + b * kC3));
+          tma_store_2d(&mC, ccol0 + n0 + 32 * j, crow0 + m0, smem_u32(gcsm + b * kC3));
           asm volatile("cp.async.bulk.commit_group;" ::: "memory");
           // the buffer is refilled two chunks ahead once the store has read it
           asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
           if (j + 2 < nch) {
-            mbar_arrive_expect_tx(&cfull[b], kC3);
-            tma_load_2d(smem_u32(csm + b * kC3), &mC, ccol0 + n0 + 32 * (j + 2), crow0 + m0,
-                        &cfull[b]);
+            mbar_arrive_expect_tx(&gcfull[b], kC3);
+            tma_load_2d(smem_u32(gcsm + b * kC3), &mC, ccol0 + n0 + 32 * (j + 2), crow0 + m0,
+                        &gcfull[b]);
           }
         }
       }
@@ -769,10 +780,7 @@ __global__ void __launch_bounds__(kG3Threads, 1)
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncwarp();
       if (lane == 0) mbar_arrive(&tempty[acc]);
-      if (++acc == 2) {
-        acc = 0;
-        aphase ^= 1u;
-      }
+      aphase ^= 1u;
     }
     if (etid == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
   }
@@ -784,7 +792,7 @@ __global__ void __launch_bounds__(kG3Threads, 1)
                  : "memory");
 }
 
-static size_t gemm_smem() { return (size_t)G3S * kStage3 + 2 * kC3 + 1024 + 256; }
+static size_t gemm_smem() { return (size_t)G3S * kStage3 + 4 * kC3 + 1024 + 256; }
 
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (the
@@ -1117,8 +1125,7 @@ int form_system_f32(wbem_context* h) {
     h->lu_elems = nn;
   }
   EvTimer tm(h->stream);
-  dim3 g(std::min(64, (N + 255) / 256), N);
-  k_form_lu<<<g, 256, 0, h->stream>>>(N, ld, h->d_N2, h->d_D2, h->d_mask, h->d_alpha, h->d_cflag,
+  k_form_lu<<<N, 256, 0, h->stream>>>(N, ld, h->d_N2, h->d_D2, h->d_mask, h->d_alpha, h->d_cflag,
                                       h->d_cptr_full, h->d_ccol_full, h->d_cval_full, h->d_lu);
   WB_CU(cudaGetLastError());
   h->launches++;

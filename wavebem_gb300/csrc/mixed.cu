@@ -128,14 +128,22 @@ __global__ void k_cell_records_mixed(int C, const double* __restrict__ X,
   cd[22] = 0.f;
   cd[23] = 0.f;
   for (int k = 9 * nq + 24; k < RF; ++k) r[k] = 0.f;
-  // near test: centre (float) and (ratio * largest diagonal)^2
-  double d1 = 0, d2 = 0;
+  // near test: centre (float) and (ratio * largest diagonal)^2, at least
+  // 1.01 x the farthest vertex, so that every panel with the collocation
+  // point (or a double-node partner of it) as a vertex tests near: the
+  // regular far-field kernel then needs no singular test of its own
+  double d1 = 0, d2 = 0, dv = 0;
   for (int e = 0; e < 3; ++e) {
     d1 += (P[3][e] - P[0][e]) * (P[3][e] - P[0][e]);
     d2 += (P[2][e] - P[1][e]) * (P[2][e] - P[1][e]);
   }
+  for (int k = 0; k < 4; ++k) {
+    double v = 0;
+    for (int e = 0; e < 3; ++e) v += (P[k][e] - cen[e]) * (P[k][e] - cen[e]);
+    dv = v > dv ? v : dv;
+  }
   const double diam = sqrt(d1 > d2 ? d1 : d2);
-  const double rad = (double)ratio * diam;
+  const double rad = fmax((double)ratio * diam, 1.01 * sqrt(dv));
   cellgeo[c] = make_float4((float)cen[0], (float)cen[1], (float)cen[2], (float)(rad * rad));
 }
 
@@ -166,14 +174,9 @@ __global__ void __launch_bounds__(kRowsPerTile)
   const int row = row0 + tid;
   const bool active = row < N;
   df xr[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-  int set[kMaxSet];
-#pragma unroll
-  for (int k = 0; k < kMaxSet; ++k) set[k] = -2;
   if (active) {
 #pragma unroll
     for (int d = 0; d < 3; ++d) xr[d] = df_from_double(X[3 * (size_t)row + d]);
-#pragma unroll
-    for (int k = 0; k < kMaxSet; ++k) set[k] = dnset[(size_t)row * kMaxSet + k];
   }
   const float xf = active ? __double2float_rn(X[3 * (size_t)row]) : 0.f;
   const float yf = active ? __double2float_rn(X[3 * (size_t)row + 1]) : 0.f;
@@ -244,10 +247,8 @@ __global__ void __launch_bounds__(kRowsPerTile)
       const ChunkMeta& mt = meta[(c & 1) * kChunkM + k];
       const bool owner = mt.owner != 0;
       const uint32_t slots = mt.slots;
-      const int4 dd = mt.dofs;
-      const bool sing = in_set_m(set, dd.x) || in_set_m(set, dd.y) || in_set_m(set, dd.z) ||
-                        in_set_m(set, dd.w);
-      if (!active || sing || near_test(xf, yf, zf, mt.geo)) continue;
+      // near (FP64 kernel) or singular (always near, see the cell records)
+      if (!active || near_test(xf, yf, zf, mt.geo)) continue;
       const float* r = stage + (size_t)((c & 1) * kChunkM + k) * RF;
       const float4* qa = reinterpret_cast<const float4*>(r);
       const float4* qb = reinterpret_cast<const float4*>(r + 4 * NQ);
@@ -274,9 +275,20 @@ __global__ void __launch_bounds__(kRowsPerTile)
       const float ecor = (1.0f - t.hi) - t.lo;
       const df rinv = fast_two_sum(y0, 0.5f * y0 * ecor);
       const df ri3 = df_mul(df_mul(rinv, rinv), rinv);
-      df Rn = df_mul(R[0], df{cd[6], cd[9]});
-      Rn = df_add(Rn, df_mul(R[1], df{cd[7], cd[10]}));
-      Rn = df_add(Rn, df_mul(R[2], df{cd[8], cd[11]}));
+      // R . nu in double-float: exact hi products, cross terms into the lo part
+      df Rn;
+      {
+        const df p0 = two_prod(R[0].hi, cd[6]);
+        const df p1 = two_prod(R[1].hi, cd[7]);
+        const df p2 = two_prod(R[2].hi, cd[8]);
+        df s01 = two_sum(p0.hi, p1.hi);
+        df s = two_sum(s01.hi, p2.hi);
+        float lo = s01.lo + s.lo + (p0.lo + p1.lo + p2.lo);
+        lo = __fmaf_rn(R[0].hi, cd[9], __fmaf_rn(R[0].lo, cd[6], lo));
+        lo = __fmaf_rn(R[1].hi, cd[10], __fmaf_rn(R[1].lo, cd[7], lo));
+        lo = __fmaf_rn(R[2].hi, cd[11], __fmaf_rn(R[2].lo, cd[8], lo));
+        Rn = fast_two_sum(s.hi, lo);
+      }
       df gR = df_mul(Rn, ri3);
       gR.hi = -gR.hi;
       gR.lo = -gR.lo;
@@ -307,11 +319,11 @@ __global__ void __launch_bounds__(kRowsPerTile)
           const float rqinv = rsqrtf(rq2);
           const float rq = rq2 * rqinv;
           const float dr = __fdividef(num, rc + rq);
-          const float fs = dr * (rqinv * rcinv) * J;
-          const float rqinv3 = rqinv * rqinv * rqinv;
+          const float u = rqinv * J;
+          const float fs = dr * u;  // times 1/rc after the point sums
           const float tsum = __fmaf_rn(rc, rq, rc2) + rq2;
           const float t2 = __fmaf_rn(Rcx, B.x, __fmaf_rn(Rcy, B.y, __fmaf_rn(Rcz, B.z, B.w)));
-          const float fn = rqinv3 * __fmaf_rn(dr * tsum, K1, -t2) * J;
+          const float fn = (rqinv * rqinv) * u * __fmaf_rn(dr * tsum, K1, -t2);
           const float xa = c_qm.gpf[q][0];
           st += fs;
           s1 = __fmaf_rn(fs, xa, s1);
@@ -330,21 +342,32 @@ __global__ void __launch_bounds__(kRowsPerTile)
         ln3 = __fmaf_rn(n1, eb, ln3);
       }
       const float fnsum = (ln0 + ln1) + (ln2 + ln3);
-      const float lsv[4] = {ls0, ls1, ls2, ls3}, lnv[4] = {ln0, ln1, ln2, ln3};
+      const float lsv[4] = {ls0 * rcinv, ls1 * rcinv, ls2 * rcinv, ls3 * rcinv};
+      const float lnv[4] = {ln0, ln1, ln2, ln3};
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const uint32_t sl = (slots >> (8 * j)) & 255u;
         if (sl != 255u) {
-          const df Mj = {cd[12 + j], cd[16 + j]};
-          const df vs = df_add_f(df_mul(rinv, Mj), lsv[j]);
-          const df vn = df_add_f(df_mul(gR, Mj), lnv[j]);
+          // acc += k(c) M_j + (FP32 point sum): exact hi product, one
+          // two_sum into the accumulator, everything else into its lo part
+          const float Mh = cd[12 + j], Ml = cd[16 + j];
           const int o = sl * LDA + tid;
-          df a = df_add_fast(df{aNh[o], aNl[o]}, vn);
-          aNh[o] = a.hi;
-          aNl[o] = a.lo;
-          a = df_add_fast(df{aDh[o], aDl[o]}, vs);
-          aDh[o] = a.hi;
-          aDl[o] = a.lo;
+          {
+            const df p = two_prod(gR.hi, Mh);
+            const float pl = __fmaf_rn(gR.hi, Ml, __fmaf_rn(gR.lo, Mh, p.lo));
+            const df s2 = two_sum(aNh[o], p.hi);
+            const df a = fast_two_sum(s2.hi, s2.lo + (aNl[o] + (pl + lnv[j])));
+            aNh[o] = a.hi;
+            aNl[o] = a.lo;
+          }
+          {
+            const df p = two_prod(rinv.hi, Mh);
+            const float pl = __fmaf_rn(rinv.hi, Ml, __fmaf_rn(rinv.lo, Mh, p.lo));
+            const df s2 = two_sum(aDh[o], p.hi);
+            const df a = fast_two_sum(s2.hi, s2.lo + (aDl[o] + (pl + lsv[j])));
+            aDh[o] = a.hi;
+            aDl[o] = a.lo;
+          }
         }
       }
       if (owner) alpha_acc = df_add(alpha_acc, df_add_f(df_mul(gR, df{cd[20], cd[21]}), fnsum));
