@@ -116,6 +116,47 @@ __device__ __forceinline__ void w_gemm_col(float* C, const float* A, const float
     C[r * kDLD + lane] = acc ? __fmaf_rn(sign, sum, C[r * kDLD + lane]) : sign * sum;
   }
 }
+// Row-split products: several warps share one 32 x 32 output block. A warp
+// holds one column (lane = column) or one row (lane = row) of an operand in
+// registers and produces a range of output rows (columns). Loads and stores
+// are separated by a CTA barrier where the product is in place.
+__device__ __forceinline__ void load_col32(float v[32], const float* B) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 0; k < 32; ++k) v[k] = B[k * kDLD + lane];
+}
+__device__ __forceinline__ void load_row32(float v[32], const float* A) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 0; k < 32; ++k) v[k] = A[lane * kDLD + k];
+}
+// rows [r0, r0 + nr) of C = sign * A * col (+ C if acc), lane = column
+__device__ __forceinline__ void rows_prod(float* C, const float* A, const float col[32], float sign,
+                                          bool acc, int r0, int nr) {
+  const int lane = threadIdx.x & 31;
+  for (int r = r0; r < r0 + nr; ++r) {
+    float sum = 0.f;
+#pragma unroll
+    for (int k = 0; k < 32; ++k) sum = __fmaf_rn(A[r * kDLD + k], col[k], sum);
+    C[r * kDLD + lane] = acc ? __fmaf_rn(sign, sum, C[r * kDLD + lane]) : sign * sum;
+  }
+}
+// columns [c0, c0 + nc) of C = row * B, lane = row
+__device__ __forceinline__ void cols_prod(float* C, const float row[32], const float* B, int c0,
+                                          int nc) {
+  const int lane = threadIdx.x & 31;
+  for (int c = c0; c < c0 + nc; ++c) {
+    float sum = 0.f;
+#pragma unroll
+    for (int k = 0; k < 32; ++k) sum = __fmaf_rn(row[k], B[k * kDLD + c], sum);
+    C[lane * kDLD + c] = sum;
+  }
+}
+// warps per task when 16 warps share ntask 32 x 32 tasks (a power of two)
+__device__ __forceinline__ int warps_per_task(int ntask) {
+  return ntask <= 1 ? 16 : ntask <= 2 ? 8 : ntask <= 4 ? 4 : ntask <= 8 ? 2 : 1;
+}
+
 // C[32x32] = A[32x32] * B[32x32] with lane = row (A read by rows, in place on A allowed).
 __device__ __forceinline__ void w_gemm_row(float* C, const float* A, const float* B) {
   const int lane = threadIdx.x & 31;
@@ -210,45 +251,73 @@ __global__ void __launch_bounds__(kDiagThreads, 1)
       for (int r = 0; r < 32; ++r) sUi[(o + r) * kDLD + o + lane] = x[r];
     }
     __syncthreads();
-    // ---- panels: U_st = inv(L_ss) A_st (warps 0..), L_ts = A_ts inv(U_ss) (warps 3..)
     const int np = 3 - s;
-    if (warp < np) {
-      const int t = s + 1 + warp;
-      w_gemm_col(sA + o * kDLD + 32 * t, sLi + o * kDLD + o, sA + o * kDLD + 32 * t, 1.f, false);
-    } else if (warp >= 3 && warp < 3 + np) {
-      const int t = s + 1 + (warp - 3);
-      w_gemm_row(sA + 32 * t * kDLD + o, sA + 32 * t * kDLD + o, sUi + o * kDLD + o);
+    if (np == 0) break;
+    // ---- panels (in place): U_st = inv(L_ss) A_st (tasks 0..np-1, lane =
+    // column) and L_ts = A_ts inv(U_ss) (tasks np..2np-1, lane = row)
+    {
+      const int ntask = 2 * np, wpt = warps_per_task(ntask), part = 32 / wpt;
+      const int task = warp / wpt, sub = warp % wpt;
+      const bool act = task < ntask;
+      const bool upanel = task < np;
+      const int t = s + 1 + (upanel ? task : task - np);
+      float v[32];
+      if (act) {
+        if (upanel) load_col32(v, sA + o * kDLD + 32 * t);
+        else load_row32(v, sA + 32 * t * kDLD + o);
+      }
+      __syncthreads();
+      if (act) {
+        if (upanel) rows_prod(sA + o * kDLD + 32 * t, sLi + o * kDLD + o, v, 1.f, false, sub * part, part);
+        else cols_prod(sA + 32 * t * kDLD + o, v, sUi + o * kDLD + o, sub * part, part);
+      }
+      __syncthreads();
     }
-    __syncthreads();
-    // ---- trailing: A_tu -= L_ts U_su
-    if (warp < np * np) {
-      const int t = s + 1 + warp / np, u = s + 1 + warp % np;
-      w_gemm_col(sA + 32 * t * kDLD + 32 * u, sA + 32 * t * kDLD + o, sA + o * kDLD + 32 * u, -1.f,
-                 true);
+    // ---- trailing: A_tu -= L_ts U_su (np * np tasks, lane = column)
+    {
+      const int ntask = np * np, wpt = warps_per_task(ntask), part = 32 / wpt;
+      const int task = warp / wpt, sub = warp % wpt;
+      if (task < ntask) {
+        const int t = s + 1 + task / np, u = s + 1 + task % np;
+        float v[32];
+        load_col32(v, sA + o * kDLD + 32 * u);
+        rows_prod(sA + 32 * t * kDLD + 32 * u, sA + 32 * t * kDLD + o, v, -1.f, true, sub * part, part);
+      }
+      __syncthreads();
     }
-    __syncthreads();
   }
-  // ---- off-diagonal blocks of the inverses, by distance d = t - s
+  // ---- off-diagonal blocks of the inverses, by distance d = t - s:
+  //   Linv_ts = -Linv_tt sum_{u=s}^{t-1} L_tu Linv_us   (tasks 0..npairs-1)
+  //   Uinv_st = -Uinv_ss sum_{u=s+1}^{t} U_su Uinv_ut   (tasks npairs..)
+  // first the sums into the (t, s) / (s, t) block, then the in-place product
   for (int d = 1; d < 4; ++d) {
-    // Linv_ts = -Linv_tt sum_u L_tu Linv_us (warps 0..3-d), staged through
-    // the upper triangle of sUi's unused block (t, s) region of sLi first
-    const int npairs = 4 - d;
-    if (warp < npairs) {
-      const int sb = warp, tb = warp + d;
-      float* T = sLi + 32 * tb * kDLD + 32 * sb;  // accumulate sum_u L_tu Linv_us
-      for (int u = sb; u < tb; ++u)
-        w_gemm_col(T, sA + 32 * tb * kDLD + 32 * u, sLi + 32 * u * kDLD + 32 * sb, 1.f, u > sb);
-      __syncwarp();
-      // T <- -Linv_tt T (lane = column)
-      w_gemm_col(T, sLi + 32 * tb * kDLD + 32 * tb, T, -1.f, false);
-    } else if (warp >= 4 && warp < 4 + npairs) {
-      // Uinv_st = -Uinv_ss sum_{u=s+1}^{t} U_su Uinv_ut
-      const int sb = warp - 4, tb = sb + d;
-      float* T = sUi + 32 * sb * kDLD + 32 * tb;
-      for (int u = sb + 1; u <= tb; ++u)
-        w_gemm_col(T, sA + 32 * sb * kDLD + 32 * u, sUi + 32 * u * kDLD + 32 * tb, 1.f, u > sb + 1);
-      __syncwarp();
-      w_gemm_col(T, sUi + 32 * sb * kDLD + 32 * sb, T, -1.f, false);
+    const int npairs = 4 - d, ntask = 2 * npairs, wpt = warps_per_task(ntask), part = 32 / wpt;
+    const int task = warp / wpt, sub = warp % wpt;
+    const bool act = task < ntask;
+    const bool lt = task < npairs;
+    const int sb = lt ? task : task - npairs, tb = sb + d;
+    float* T = lt ? sLi + 32 * tb * kDLD + 32 * sb : sUi + 32 * sb * kDLD + 32 * tb;
+    if (act) {
+      float v[32];
+      if (lt) {
+        for (int u = sb; u < tb; ++u) {
+          load_col32(v, sLi + 32 * u * kDLD + 32 * sb);
+          rows_prod(T, sA + 32 * tb * kDLD + 32 * u, v, 1.f, u > sb, sub * part, part);
+        }
+      } else {
+        for (int u = sb + 1; u <= tb; ++u) {
+          load_col32(v, sUi + 32 * u * kDLD + 32 * tb);
+          rows_prod(T, sA + 32 * sb * kDLD + 32 * u, v, 1.f, u > sb + 1, sub * part, part);
+        }
+      }
+    }
+    __syncthreads();
+    float v[32];
+    if (act) load_col32(v, T);
+    __syncthreads();
+    if (act) {
+      const float* Dg = lt ? sLi + 32 * tb * kDLD + 32 * tb : sUi + 32 * sb * kDLD + 32 * sb;
+      rows_prod(T, Dg, v, -1.f, false, sub * part, part);
     }
     __syncthreads();
   }
