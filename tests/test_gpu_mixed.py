@@ -76,3 +76,30 @@ def test_mixed_solve_system_reuses_factors(solver):
         assert rel2(phi, phi_o) <= 1e-8 and rel2(dphi, dphi_o) <= 1e-8
         if k == 1:  # the second solve prepares nothing
             assert g.stats()["t_factor_ms"] == 0.0
+
+
+@pytest.mark.parametrize("solver", [SOLVER_LU, SOLVER_GMRES_IR])
+def test_mixed_mask_change_after_assembly(solver):
+    """set_bc with a new mask after the assembly: the FP32 system is formed
+    again from the stored N and D (the copy written during the assembly
+    belongs to the old mask); an unchanged mask keeps everything."""
+    import oracle as O
+    P, m, b = oracle_problem("wigley", 2000)
+    single = np.nonzero((np.diff(P.dn_ptr) == 1) & (m.dirichlet == 0))[0]
+    mask2 = m.dirichlet.copy()
+    mask2[single[::10]] = 1
+    P2 = O.Problem(m.X, m.cells, P.dn_ptr, P.dn_idx, mask2)
+    P2.Nm, P2.Dm, P2.alpha = P.Nm, P.Dm, P.alpha
+    phi_o, dphi_o, _ = P2.solve_system(b)
+    g = BEMProblem(m.X, m.cells, m.dirichlet, P.dn_ptr, P.dn_idx, precision=PREC_MIXED,
+                   solver=solver)
+    g.assemble_system()
+    g.set_bc(mask2)
+    phi, dphi = b.copy(), b.copy()
+    g.solve_system(phi, dphi, b)
+    assert rel2(phi, phi_o) <= 1e-8 and rel2(dphi, dphi_o) <= 1e-8
+    g.set_bc(mask2)  # unchanged: nothing to prepare again
+    phi, dphi = b.copy(), b.copy()
+    g.solve_system(phi, dphi, b)
+    assert g.stats()["t_factor_ms"] == 0.0
+    assert rel2(phi, phi_o) <= 1e-8 and rel2(dphi, dphi_o) <= 1e-8

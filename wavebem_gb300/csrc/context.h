@@ -132,7 +132,10 @@ struct wbem_context {
   double* d_vec[kNumVec] = {};  // N-vectors: [0..2] GMRES, [7] transposed operator, [8..9] refinement
   double* d_part = nullptr;
   double* d_small = nullptr;
-  float* d_lu = nullptr;   // mixed LU factors
+  float* d_lu = nullptr;   // mixed: FP32 system matrix, then its LU factors
+  // state of d_lu: 0 = neither, 1 = system entries from the assembly (free
+  // term and constraint rows pending), 2 = complete system matrix
+  int s32_state = 0;
   uint16_t* d_split = nullptr;
   float* d_lutmp = nullptr;
   int* d_info = nullptr;

@@ -49,7 +49,9 @@ __global__ void __launch_bounds__(256)
               const uint8_t* __restrict__ cflag, const int* __restrict__ cptr,
               const int* __restrict__ ccol, const double* __restrict__ cval,
               float* __restrict__ A) {
-  // one CTA per row, four consecutive columns per thread and step
+  // one CTA per row, four consecutive columns per thread and step; a group
+  // of four columns with one boundary condition reads only the matrix it
+  // needs, as two 16-byte loads
   const int i = blockIdx.x;
   float* ar = A + (size_t)i * ld;
   if (cflag[i]) {
@@ -58,22 +60,39 @@ __global__ void __launch_bounds__(256)
   }
   const float2* nr = N2 + (size_t)i * N;
   const float2* dr = D2 + (size_t)i * N;
-  auto entry = [&](int j) -> float {
-    if (mask[j]) {
-      const float2 d = __ldcs(dr + j);
-      return -(float)((double)d.x + (double)d.y);
-    }
-    const float2 n = __ldcs(nr + j);
-    double s = (double)n.x + (double)n.y;
+  const bool vec = (N & 1) == 0;  // row starts 16-byte aligned
+  auto val = [&](int j, bool m, float2 v) -> float {
+    if (m) return -(float)((double)v.x + (double)v.y);
+    double s = (double)v.x + (double)v.y;
     if (j == i) s += alpha[i];
     return (float)s;
   };
   for (int j = 4 * threadIdx.x; j < N; j += 4 * blockDim.x) {
     if (j + 3 < N) {
-      const float4 v = make_float4(entry(j), entry(j + 1), entry(j + 2), entry(j + 3));
+      const uchar4 mk = *reinterpret_cast<const uchar4*>(mask + j);
+      const bool m[4] = {mk.x != 0, mk.y != 0, mk.z != 0, mk.w != 0};
+      float2 e[4];
+      const bool alld = m[0] && m[1] && m[2] && m[3];
+      const bool alln = !(m[0] || m[1] || m[2] || m[3]);
+      if (vec && (alld || alln)) {
+        const float4* p = reinterpret_cast<const float4*>((alld ? dr : nr) + j);
+        const float4 a = __ldcs(p), b = __ldcs(p + 1);
+        e[0] = make_float2(a.x, a.y);
+        e[1] = make_float2(a.z, a.w);
+        e[2] = make_float2(b.x, b.y);
+        e[3] = make_float2(b.z, b.w);
+      } else {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) e[u] = __ldcs((m[u] ? dr : nr) + j + u);
+      }
+      const float4 v = make_float4(val(j, m[0], e[0]), val(j + 1, m[1], e[1]), val(j + 2, m[2], e[2]),
+                                   val(j + 3, m[3], e[3]));
       __stcs(reinterpret_cast<float4*>(ar + j), v);
     } else {
-      for (int u = 0; j + u < N; ++u) ar[j + u] = entry(j + u);
+      for (int u = 0; j + u < N; ++u) {
+        const bool m = mask[j + u] != 0;
+        ar[j + u] = val(j + u, m, __ldcs((m ? dr : nr) + j + u));
+      }
     }
   }
 }
@@ -1179,12 +1198,8 @@ int system_ld(int N) { return (N + 31) / 32 * 32; }
 
 int build_constraint_structure(wbem_context* h);
 
-int form_system_f32(wbem_context* h) {
-  if (!h->d_cflag || !h->d_cptr_full || !h->d_N2 || !h->d_D2 || !h->d_mask || !h->d_alpha)
-    return fail(h, WBEM_ERR_STATE, "system matrix: assembly, mask or constraints missing");
-  const int N = h->N;
-  const int ld = system_ld(N);
-  const size_t nn = (size_t)N * ld;
+int ensure_system_buffer(wbem_context* h) {
+  const size_t nn = (size_t)h->N * system_ld(h->N);
   if (!h->d_lu || h->lu_elems != nn) {
     if (h->d_lu) {
       cudaFree(h->d_lu);
@@ -1192,10 +1207,45 @@ int form_system_f32(wbem_context* h) {
     }
     WB_CHK(dev_alloc(h, &h->d_lu, nn));
     h->lu_elems = nn;
+    h->s32_state = 0;
+  }
+  return WBEM_OK;
+}
+
+// Completes the system matrix written by the assembly: the free term on the
+// Neumann diagonal (hi of N_ii + alpha_i), and the constrained rows, which
+// become e_i (their entries follow in k_lu_constraint_entries).
+__global__ void k_system_finish(int N, int ld, const float2* __restrict__ N2,
+                                const uint8_t* __restrict__ mask, const double* __restrict__ alpha,
+                                const uint8_t* __restrict__ cflag, float* __restrict__ A) {
+  const int i = blockIdx.x;
+  float* ar = A + (size_t)i * ld;
+  if (cflag[i]) {
+    for (int j = threadIdx.x; j < N; j += blockDim.x) ar[j] = (j == i) ? 1.f : 0.f;
+  } else if (threadIdx.x == 0 && !mask[i]) {
+    const float2 n = N2[(size_t)i * N + i];
+    ar[i] = (float)((double)n.x + (double)n.y + alpha[i]);
+  }
+}
+
+int form_system_f32(wbem_context* h) {
+  if (!h->d_cflag || !h->d_cptr_full || !h->d_N2 || !h->d_D2 || !h->d_mask || !h->d_alpha)
+    return fail(h, WBEM_ERR_STATE, "system matrix: assembly, mask or constraints missing");
+  const int N = h->N;
+  const int ld = system_ld(N);
+  if (h->s32_state == 2) {
+    h->stats.t_system_ms = 0.0;
+    return WBEM_OK;
   }
   EvTimer tm(h->stream);
-  k_form_lu<<<N, 256, 0, h->stream>>>(N, ld, h->d_N2, h->d_D2, h->d_mask, h->d_alpha, h->d_cflag,
-                                      h->d_cptr_full, h->d_ccol_full, h->d_cval_full, h->d_lu);
+  if (h->s32_state == 1) {
+    k_system_finish<<<N, 128, 0, h->stream>>>(N, ld, h->d_N2, h->d_mask, h->d_alpha, h->d_cflag,
+                                               h->d_lu);
+  } else {
+    WB_CHK(ensure_system_buffer(h));
+    k_form_lu<<<N, 256, 0, h->stream>>>(N, ld, h->d_N2, h->d_D2, h->d_mask, h->d_alpha, h->d_cflag,
+                                        h->d_cptr_full, h->d_ccol_full, h->d_cval_full, h->d_lu);
+  }
   WB_CU(cudaGetLastError());
   h->launches++;
   if (h->n_crows > 0) {
@@ -1204,6 +1254,7 @@ int form_system_f32(wbem_context* h) {
     WB_CU(cudaGetLastError());
     h->launches++;
   }
+  h->s32_state = 2;
   h->stats.t_system_ms = tm.ms();
   return WBEM_OK;
 }
@@ -1216,6 +1267,7 @@ int factor_mixed(wbem_context* h) {
   L.N = N;
   L.ld = ld;
   WB_CHK(form_system_f32(h));
+  h->s32_state = 0;  // the factorisation overwrites the system matrix
   if (!encode_cmap(&L.cmap, h->d_lu, N, N, ld))
     return fail(h, WBEM_ERR_CUDA, "cuTensorMapEncodeTiled (LU buffer) failed");
   const int nblk = (N + kNB - 1) / kNB;

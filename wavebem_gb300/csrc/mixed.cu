@@ -60,6 +60,16 @@ __device__ __forceinline__ void q1_geo(const double P[4][3], double s, double t,
   cr[2] = jx[0] * je[1] - jx[1] * je[0];
 }
 
+// Optional FP32 copy of the system operator written during assembly: S_ij =
+// hi(N_ij) on Neumann columns, -hi(D_ij) on Dirichlet columns (row-major,
+// leading dimension ld). The diagonal free term and the constraint rows are
+// added at solve time.
+struct SysOut {
+  float* S;                  // nullptr: not written
+  int ld;
+  const uint8_t* mask;       // 1 = Dirichlet column
+};
+
 // One thread per panel: FP64 geometry -> mixed record + near-test data.
 __global__ void k_cell_records_mixed(int C, const double* __restrict__ X,
                                      const int4* __restrict__ cell_dofs, float* __restrict__ rec,
@@ -155,7 +165,8 @@ __global__ void __launch_bounds__(kRowsPerTile)
                  const int* __restrict__ tile_ptr, const int2* __restrict__ tile_ent,
                  const int4* __restrict__ cell_dofs, const float* __restrict__ rec,
                  const float4* __restrict__ cellgeo, float2* __restrict__ N2,
-                 float2* __restrict__ D2, double* __restrict__ alpha_part, DevErr* err) {
+                 float2* __restrict__ D2, double* __restrict__ alpha_part, SysOut so,
+                 DevErr* err) {
   constexpr int NQ = Q1 * Q1;
   constexpr int RF = mixed_rec_floats(NQ);
   constexpr int RT = kRowsPerTile, CT = kColsPerTile, LDA = RT + 1;
@@ -383,6 +394,7 @@ __global__ void __launch_bounds__(kRowsPerTile)
       const int o = cc * LDA + rr;
       N2[(size_t)gr * N + gc] = make_float2(aNh[o], aNl[o]);
       D2[(size_t)gr * N + gc] = make_float2(aDh[o], aDl[o]);
+      if (so.S) so.S[(size_t)gr * so.ld + gc] = so.mask[gc] ? -aDh[o] : aNh[o];
     }
   }
 }
@@ -392,7 +404,7 @@ static cudaError_t launch_tile_mixed_t(int N, const double* X, const int* dnset,
                                        const int* tile_ptr, const int2* tile_ent,
                                        const int4* cell_dofs, const float* rec,
                                        const float4* cellgeo, float2* N2, float2* D2,
-                                       double* alpha_part, DevErr* err, cudaStream_t s) {
+                                       double* alpha_part, SysOut so, DevErr* err, cudaStream_t s) {
   constexpr int RF = mixed_rec_floats(Q1 * Q1);
   const size_t acc = (size_t)kColsPerTile * (kRowsPerTile + 1);
   const size_t smem = (size_t)2 * kChunkM * RF * 4 + 4 * acc * 4 + 16 +
@@ -402,7 +414,7 @@ static cudaError_t launch_tile_mixed_t(int N, const double* X, const int* dnset,
   if (e != cudaSuccess) return e;
   dim3 grid(n_tiles, (N + kRowsPerTile - 1) / kRowsPerTile);
   k_tile_mixed<Q1><<<grid, kRowsPerTile, smem, s>>>(N, X, dnset, tile_ptr, tile_ent, cell_dofs, rec,
-                                                    cellgeo, N2, D2, alpha_part, err);
+                                                    cellgeo, N2, D2, alpha_part, so, err);
   return cudaGetLastError();
 }
 
@@ -415,7 +427,7 @@ __global__ void __launch_bounds__(256)
     k_near_mixed(int N, int C, const double* __restrict__ X, const int* __restrict__ dnset,
                  const int4* __restrict__ cell_dofs, const float4* __restrict__ cellgeo,
                  const double* __restrict__ rec64, float2* __restrict__ N2,
-                 float2* __restrict__ D2, double* __restrict__ alpha_near) {
+                 float2* __restrict__ D2, double* __restrict__ alpha_near, SysOut so) {
   const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (row >= N) return;
@@ -467,10 +479,12 @@ __global__ void __launch_bounds__(256)
           double s = (double)v.x + (double)v.y + ln[j];
           float h = __double2float_rn(s);
           N2[o] = make_float2(h, __double2float_rn(s - (double)h));
+          const float nh = h;
           v = D2[o];
           s = (double)v.x + (double)v.y + ld[j];
           h = __double2float_rn(s);
           D2[o] = make_float2(h, __double2float_rn(s - (double)h));
+          if (so.S) so.S[(size_t)row * so.ld + id[j]] = so.mask[id[j]] ? -h : nh;
           asum += ln[j];
         }
       }
@@ -484,7 +498,7 @@ __global__ void k_singular_mixed(int N, const double* __restrict__ X, const int*
                                  const int* __restrict__ sptr, const int* __restrict__ scell,
                                  const int4* __restrict__ cell_dofs, float2* __restrict__ N2,
                                  float2* __restrict__ D2, double* __restrict__ alpha_sing,
-                                 DevErr* err) {
+                                 SysOut so, DevErr* err) {
   const int row = blockIdx.x * blockDim.x + threadIdx.x;
   if (row >= N) return;
   const double xi = X[3 * (size_t)row], yi = X[3 * (size_t)row + 1], zi = X[3 * (size_t)row + 2];
@@ -529,10 +543,12 @@ __global__ void k_singular_mixed(int N, const double* __restrict__ X, const int*
       double sN = (double)vv.x + (double)vv.y + ln[j];
       float h = __double2float_rn(sN);
       N2[o] = make_float2(h, __double2float_rn(sN - (double)h));
+      const float nh = h;
       vv = D2[o];
       double sD = (double)vv.x + (double)vv.y + ld[j];
       h = __double2float_rn(sD);
       D2[o] = make_float2(h, __double2float_rn(sD - (double)h));
+      if (so.S) so.S[(size_t)row * so.ld + id[j]] = so.mask[id[j]] ? -h : nh;
       asum += ln[j];
     }
   }
@@ -558,6 +574,9 @@ void free_mixed(wbem_context* h) {
   if (h->d_lu) { cudaFree(h->d_lu); h->d_lu = nullptr; }
   h->lu_elems = 0;
 }
+
+int ensure_system_buffer(wbem_context* h);
+int system_ld(int N);
 
 int assemble_mixed(wbem_context* h) {
   const int N = h->N, C = h->C;
@@ -597,22 +616,30 @@ int assemble_mixed(wbem_context* h) {
   CUM(cudaGetLastError());
   h->stats.t_geometry_ms = tm.ms();
   const float4* geo = reinterpret_cast<const float4*>(h->d_cellgeo);
+  // the FP32 system copy for the solvers, written alongside N and D
+  SysOut so{nullptr, 0, nullptr};
+  if (h->have_mask && h->d_mask) {
+    CHKM(ensure_system_buffer(h));
+    so = SysOut{h->d_lu, system_ld(N), h->d_mask};
+  }
+  h->s32_state = 0;
   cudaError_t e;
   switch (q1) {
-    case 2: e = launch_tile_mixed_t<2>(N, h->d_X, h->d_dnset, h->n_tiles, h->d_tile_ptr, h->d_tile_ent, h->d_cell_dofs, h->d_rec32, geo, h->d_N2, h->d_D2, h->d_alpha_part, h->d_err, h->stream); break;
-    case 3: e = launch_tile_mixed_t<3>(N, h->d_X, h->d_dnset, h->n_tiles, h->d_tile_ptr, h->d_tile_ent, h->d_cell_dofs, h->d_rec32, geo, h->d_N2, h->d_D2, h->d_alpha_part, h->d_err, h->stream); break;
-    case 4: e = launch_tile_mixed_t<4>(N, h->d_X, h->d_dnset, h->n_tiles, h->d_tile_ptr, h->d_tile_ent, h->d_cell_dofs, h->d_rec32, geo, h->d_N2, h->d_D2, h->d_alpha_part, h->d_err, h->stream); break;
-    case 5: e = launch_tile_mixed_t<5>(N, h->d_X, h->d_dnset, h->n_tiles, h->d_tile_ptr, h->d_tile_ent, h->d_cell_dofs, h->d_rec32, geo, h->d_N2, h->d_D2, h->d_alpha_part, h->d_err, h->stream); break;
-    default: e = launch_tile_mixed_t<6>(N, h->d_X, h->d_dnset, h->n_tiles, h->d_tile_ptr, h->d_tile_ent, h->d_cell_dofs, h->d_rec32, geo, h->d_N2, h->d_D2, h->d_alpha_part, h->d_err, h->stream); break;
+    case 2: e = launch_tile_mixed_t<2>(N, h->d_X, h->d_dnset, h->n_tiles, h->d_tile_ptr, h->d_tile_ent, h->d_cell_dofs, h->d_rec32, geo, h->d_N2, h->d_D2, h->d_alpha_part, so, h->d_err, h->stream); break;
+    case 3: e = launch_tile_mixed_t<3>(N, h->d_X, h->d_dnset, h->n_tiles, h->d_tile_ptr, h->d_tile_ent, h->d_cell_dofs, h->d_rec32, geo, h->d_N2, h->d_D2, h->d_alpha_part, so, h->d_err, h->stream); break;
+    case 4: e = launch_tile_mixed_t<4>(N, h->d_X, h->d_dnset, h->n_tiles, h->d_tile_ptr, h->d_tile_ent, h->d_cell_dofs, h->d_rec32, geo, h->d_N2, h->d_D2, h->d_alpha_part, so, h->d_err, h->stream); break;
+    case 5: e = launch_tile_mixed_t<5>(N, h->d_X, h->d_dnset, h->n_tiles, h->d_tile_ptr, h->d_tile_ent, h->d_cell_dofs, h->d_rec32, geo, h->d_N2, h->d_D2, h->d_alpha_part, so, h->d_err, h->stream); break;
+    default: e = launch_tile_mixed_t<6>(N, h->d_X, h->d_dnset, h->n_tiles, h->d_tile_ptr, h->d_tile_ent, h->d_cell_dofs, h->d_rec32, geo, h->d_N2, h->d_D2, h->d_alpha_part, so, h->d_err, h->stream); break;
   }
   CUM(e);
   h->stats.t_assemble_ms = tm.ms();
   k_near_mixed<<<(unsigned)(((size_t)N * 32 + 255) / 256), 256, 0, h->stream>>>(
-      N, C, h->d_X, h->d_dnset, h->d_cell_dofs, geo, h->d_rec, h->d_N2, h->d_D2, h->d_alpha_near);
+      N, C, h->d_X, h->d_dnset, h->d_cell_dofs, geo, h->d_rec, h->d_N2, h->d_D2, h->d_alpha_near,
+      so);
   CUM(cudaGetLastError());
   k_singular_mixed<<<(N + 63) / 64, 64, 0, h->stream>>>(N, h->d_X, h->d_dnset, h->d_sptr,
                                                          h->d_scell, h->d_cell_dofs, h->d_N2,
-                                                         h->d_D2, h->d_alpha_sing, h->d_err);
+                                                         h->d_D2, h->d_alpha_sing, so, h->d_err);
   CUM(cudaGetLastError());
   h->stats.t_singular_ms = tm.ms();
   k_alpha_mixed<<<(N + 255) / 256, 256, 0, h->stream>>>(N, h->n_tiles, h->d_alpha_part,
@@ -620,6 +647,7 @@ int assemble_mixed(wbem_context* h) {
                                                          h->d_alpha);
   CUM(cudaGetLastError());
   h->stats.t_alpha_ms = tm.ms();
+  if (so.S) h->s32_state = 1;  // entries written; free term and constraints pending
   h->launches += 6;
   return check_device_error(h, "assemble (mixed)");
 }

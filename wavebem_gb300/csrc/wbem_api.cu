@@ -1137,14 +1137,18 @@ int wbem_set_bc(wbem_handle h, const unsigned char* m) {
   if (!h) return WBEM_ERR_ARG;
   if (!m || h->N == 0) return fail(h, WBEM_ERR_STATE, "wbem_set_bc: set the geometry first");
   cudaSetDevice(h->device);
-  h->mask.assign(m, m + h->N);
-  for (auto& v : h->mask) v = v ? 1 : 0;
+  std::vector<unsigned char> nm(m, m + h->N);
+  for (auto& v : nm) v = v ? 1 : 0;
+  // an unchanged mask keeps the factors and the FP32 system matrix
+  if (h->have_mask && nm == h->mask) return WBEM_OK;
+  h->mask.swap(nm);
   std::vector<uint8_t> mi(h->N);
   for (int i = 0; i < h->N; ++i) mi[i] = h->mask[h->perm[i]];
   CHK(upload(h, &h->d_mask, mi));
   h->have_mask = true;
   h->factors_valid = false;
   h->have_solution = false;
+  h->s32_state = 0;
   return WBEM_OK;
 }
 
