@@ -387,12 +387,14 @@ def run_gpu(args, rank, world, local):
                             "unit": "TFLOP/s", "frac": a / tc,
                             "work": "3 x 2 M N K per launch (BF16x3 products of the trailing updates)",
                             "peak_source": f"MEASURED_PEAKS.json bf16_tflops_sustained ({src})"})
-        tile_bytes = 2.0 * N * N * 8.0
+        tile_bytes = 20.0 * N * N
         a = tile_bytes / (kprof["tile_ms"] / 1e3) / 1e9
         kernels.append({"kernel": "k_tile_mixed", "bound": "hbm", "ms": kprof["tile_ms"], "launches": 1,
                         "achieved": a, "peak": hbm, "unit": "GB/s", "frac": a / hbm,
-                        "work": "N and D written as (hi, lo) float pairs: 16 N^2 bytes",
-                        "note": "FP32/MUFU-issue bound (quadrature of every pair), not HBM",
+                        "work": "N and D as (hi, lo) float pairs and the FP32 system copy: 20 N^2 bytes",
+                        "note": "bound by FP32 instruction issue (16-point quadrature of every "
+                                "(row, panel) pair), not by HBM: ncu IPC 2.9 of 4, FMA pipe 54% "
+                                "(profiles/k_tile_mixed_n8192.md)",
                         "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({src})"})
         if kprof["matvec_ms"] > 0:
             a = kprof["matvec_bytes"] / (kprof["matvec_ms"] / 1e3) / 1e9

@@ -39,6 +39,7 @@ namespace wbem {
 
 constexpr int kNB = 128;   // inner LU block size (diagonal blocks, panels)
 constexpr int kNB2 = 512;  // outer block: K of the tensor-core trailing update
+constexpr int kLookaheadSMs = 1;  // SMs the bulk trailing update leaves to the panel work
 
 // ------------------------------------------------------------------ input
 // LU input: hi part of the system operator, alpha on Neumann diagonals,
@@ -948,8 +949,10 @@ static bool encode_cmap(CUtensorMap* map, const float* base, int rows, int cols,
 // addressed through its tensor map; rows and columns past the map's extent are
 // neither read (zero fill) nor written (clipped), so tiles may overhang M / Nc
 // only where the region ends at the matrix edge.
+// spare_sms: SMs left free of the persistent CTAs (for concurrent panel work)
 static cudaError_t run_gemm(const GemmMaps& mp, const CUtensorMap& cmap, int crow0, int ccol0,
-                             int brow0, int M, int Nc, int K, DevErr* err, cudaStream_t s) {
+                             int brow0, int M, int Nc, int K, DevErr* err, cudaStream_t s,
+                             int spare_sms = 0) {
   static bool attr = false;
   static int sms = 0;
   if (!attr) {
@@ -964,7 +967,7 @@ static cudaError_t run_gemm(const GemmMaps& mp, const CUtensorMap& cmap, int cro
     attr = true;
   }
   const int ntiles = ((M + G3M - 1) / G3M) * ((Nc + G3N - 1) / G3N);
-  const int grid = std::min(ntiles, sms);
+  const int grid = std::min(ntiles, std::max(1, sms - spare_sms));
   k_gemm_bf16x3<<<grid, kG3Threads, gemm_smem(), s>>>(mp.Ahi, mp.Alo, mp.Bhi, mp.Blo, cmap, crow0, ccol0,
                                                  brow0, M, Nc, K, err);
   return cudaGetLastError();
@@ -1412,8 +1415,11 @@ int factor_mixed(wbem_context* h) {
     if (p2 < N) {
       WB_CU(cudaEventRecord(L.ev_row, sp));
       WB_CU(cudaStreamWaitEvent(st, L.ev_row, 0));
+      // one SM stays free, so the next panel's first diagonal block (one
+      // CTA) and the start of its column panel run beside this update
       pb(h->prof_gemm, st);
-      WB_CU(run_gemm(L.maps2[buf], L.cmap, p1, p2, p2 - p1, n, N - p2, p1 - p0, h->d_err, st));
+      WB_CU(run_gemm(L.maps2[buf], L.cmap, p1, p2, p2 - p1, n, N - p2, p1 - p0, h->d_err, st,
+                     prof ? 0 : kLookaheadSMs));
       pe(h->prof_gemm, st, gemm_flop(n, N - p2, p1 - p0));
       WB_CU(cudaEventRecord(L.ev_trail, st));
       trail_pending = true;

@@ -418,6 +418,74 @@ static cudaError_t launch_tile_mixed_t(int N, const double* X, const int* dnset,
   return cudaGetLastError();
 }
 
+// Candidate panels of the near field per block of kNearBlock consecutive
+// rows (a compact patch in the Morton order): those whose near sphere can
+// reach any row of the block, |centre_block - centre_panel| < r_block +
+// r_panel, in ascending panel order (ballot prefix sums, deterministic). A
+// list that would overflow kNearCap is marked with cnt = -1 and its rows scan
+// every panel instead.
+constexpr int kNearBlock = 64;
+constexpr int kNearCap = 2048;
+
+__global__ void __launch_bounds__(256)
+    k_near_candidates(int N, int C, const double* __restrict__ X, const float4* __restrict__ cellgeo,
+                      int* __restrict__ cnt, int* __restrict__ list) {
+  __shared__ float red[6][256];
+  __shared__ int woff[8];
+  __shared__ int total;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int r0 = blockIdx.x * kNearBlock;
+  // bounding box of the block's rows
+  float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+  if (tid < kNearBlock && r0 + tid < N)
+    for (int e = 0; e < 3; ++e) lo[e] = hi[e] = (float)X[3 * (size_t)(r0 + tid) + e];
+  for (int e = 0; e < 3; ++e) {
+    red[e][tid] = lo[e];
+    red[3 + e][tid] = hi[e];
+  }
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (tid < o)
+      for (int e = 0; e < 3; ++e) {
+        red[e][tid] = fminf(red[e][tid], red[e][tid + o]);
+        red[3 + e][tid] = fmaxf(red[3 + e][tid], red[3 + e][tid + o]);
+      }
+    __syncthreads();
+  }
+  float cen[3], rb2 = 0.f;
+  for (int e = 0; e < 3; ++e) {
+    cen[e] = 0.5f * (red[e][0] + red[3 + e][0]);
+    const float h = 0.5f * (red[3 + e][0] - red[e][0]);
+    rb2 += h * h;
+  }
+  // margin for FP32 rounding of the coordinates and the radii
+  const float rb = sqrtf(rb2) * 1.0001f + 1e-6f;
+  if (tid == 0) total = 0;
+  __syncthreads();
+  for (int c0 = 0; c0 < C; c0 += 256) {
+    const int c = c0 + tid;
+    bool hit = false;
+    if (c < C) {
+      const float4 g = cellgeo[c];
+      const float dx = g.x - cen[0], dy = g.y - cen[1], dz = g.z - cen[2];
+      const float reach = sqrtf(g.w) * 1.0001f + rb;
+      hit = dx * dx + dy * dy + dz * dz < reach * reach;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, hit);
+    if (lane == 0) woff[warp] = __popc(m);
+    __syncthreads();
+    int base = total;
+    for (int w = 0; w < warp; ++w) base += woff[w];
+    const int pos = base + __popc(m & ((1u << lane) - 1));
+    if (hit && pos < kNearCap) list[(size_t)blockIdx.x * kNearCap + pos] = c;
+    __syncthreads();
+    if (tid == 0)
+      for (int w = 0; w < 8; ++w) total += woff[w];
+    __syncthreads();
+  }
+  if (tid == 0) cnt[blockIdx.x] = total <= kNearCap ? total : -1;
+}
+
 // FP64 near field: one warp per row. The lanes test 32 panels at a time
 // against the near criterion (same test as the tile kernel); each near,
 // non-singular panel is then integrated with the regular rule in FP64, one
@@ -427,7 +495,8 @@ __global__ void __launch_bounds__(256)
     k_near_mixed(int N, int C, const double* __restrict__ X, const int* __restrict__ dnset,
                  const int4* __restrict__ cell_dofs, const float4* __restrict__ cellgeo,
                  const double* __restrict__ rec64, float2* __restrict__ N2,
-                 float2* __restrict__ D2, double* __restrict__ alpha_near, SysOut so) {
+                 float2* __restrict__ D2, double* __restrict__ alpha_near, SysOut so,
+                 const int* __restrict__ ncnt, const int* __restrict__ nlist) {
   const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (row >= N) return;
@@ -438,10 +507,14 @@ __global__ void __launch_bounds__(256)
   for (int k = 0; k < kMaxSet; ++k) set[k] = dnset[(size_t)row * kMaxSet + k];
   const int nq = c_qm.q1 * c_qm.q1;
   double asum = 0.0;
-  for (int c0 = 0; c0 < C; c0 += 32) {
-    const int c = c0 + lane;
+  // candidates of this row's block (ascending panel order), else every panel
+  const int nc = ncnt[row / kNearBlock];
+  const int* cl = nlist + (size_t)(row / kNearBlock) * kNearCap;
+  const int ntot = nc >= 0 ? nc : C;
+  for (int c0 = 0; c0 < ntot; c0 += 32) {
+    const int c = c0 + lane < ntot ? (nc >= 0 ? cl[c0 + lane] : c0 + lane) : -1;
     bool nr = false;
-    if (c < C && near_test(xf, yf, zf, cellgeo[c])) {
+    if (c >= 0 && near_test(xf, yf, zf, cellgeo[c])) {
       const int4 d = cell_dofs[c];
       nr = !(in_set_m(set, d.x) || in_set_m(set, d.y) || in_set_m(set, d.z) || in_set_m(set, d.w));
     }
@@ -449,7 +522,7 @@ __global__ void __launch_bounds__(256)
     while (m) {
       const int b = __ffs(m) - 1;
       m &= m - 1;
-      const int cell = c0 + b;
+      const int cell = __shfl_sync(0xffffffffu, c, b);
       const double* r = rec64 + (size_t)cell * nq * 8;
       double ln[4] = {0, 0, 0, 0}, ld[4] = {0, 0, 0, 0};
       for (int q = lane; q < nq; q += 32) {
@@ -633,9 +706,19 @@ int assemble_mixed(wbem_context* h) {
   }
   CUM(e);
   h->stats.t_assemble_ms = tm.ms();
+  {
+    const int nblk = (N + kNearBlock - 1) / kNearBlock;
+    if (h->near_cap < nblk) {
+      CHKM(dev_alloc(h, &h->d_near_cnt, (size_t)nblk));
+      CHKM(dev_alloc(h, &h->d_near_cells, (size_t)nblk * kNearCap));
+      h->near_cap = nblk;
+    }
+    k_near_candidates<<<nblk, 256, 0, h->stream>>>(N, C, h->d_X, geo, h->d_near_cnt, h->d_near_cells);
+    CUM(cudaGetLastError());
+  }
   k_near_mixed<<<(unsigned)(((size_t)N * 32 + 255) / 256), 256, 0, h->stream>>>(
       N, C, h->d_X, h->d_dnset, h->d_cell_dofs, geo, h->d_rec, h->d_N2, h->d_D2, h->d_alpha_near,
-      so);
+      so, h->d_near_cnt, h->d_near_cells);
   CUM(cudaGetLastError());
   k_singular_mixed<<<(N + 63) / 64, 64, 0, h->stream>>>(N, h->d_X, h->d_dnset, h->d_sptr,
                                                          h->d_scell, h->d_cell_dofs, h->d_N2,
