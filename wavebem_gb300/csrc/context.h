@@ -97,6 +97,14 @@ struct wbem_context {
   double* d_alpha_part = nullptr;
   double* d_alpha_near = nullptr;
   double* d_alpha_sing = nullptr;
+  // mixed assembly: near-field and singular contributions appended per row
+  // (on aux_stream, beside the far-field kernel) and merged afterwards
+  double2* d_item_val = nullptr;  // (dN, dD) per item
+  int* d_item_dof = nullptr;
+  int* d_item_cnt = nullptr;      // per row: near items, singular items
+  size_t item_rows = 0;
+  cudaStream_t aux_stream = nullptr;
+  cudaEvent_t ev_aux_fork = nullptr, ev_aux_join = nullptr;
   int* d_near_cnt = nullptr;
   int* d_near_cells = nullptr;
   int near_cap = 0;

@@ -418,6 +418,47 @@ static cudaError_t launch_tile_mixed_t(int N, const double* X, const int* dnset,
   return cudaGetLastError();
 }
 
+// Near-field and singular contributions of a row are appended as items
+// (column, dN, dD) in the order the reference adds them, so that the FP64
+// kernels run beside the FP32 far-field kernel (they use different pipes)
+// and k_merge_items adds them to the (hi, lo) entries afterwards.
+constexpr int kNearItems = 384;  // per row: 4 items per near panel
+constexpr int kSingItems = 128;  // per row: 4 items per singular panel
+constexpr int kItemCap = kNearItems + kSingItems;
+
+__device__ __forceinline__ void add_entry(float2* N2, float2* D2, SysOut so, int N, int row, int col,
+                                          double dn, double dd) {
+  const size_t o = (size_t)row * N + col;
+  float2 v = N2[o];
+  double s = (double)v.x + (double)v.y + dn;
+  float h = __double2float_rn(s);
+  N2[o] = make_float2(h, __double2float_rn(s - (double)h));
+  const float nh = h;
+  v = D2[o];
+  s = (double)v.x + (double)v.y + dd;
+  h = __double2float_rn(s);
+  D2[o] = make_float2(h, __double2float_rn(s - (double)h));
+  if (so.S) so.S[(size_t)row * so.ld + col] = so.mask[col] ? -h : nh;
+}
+
+// One thread per row: near items, then singular items, in order.
+__global__ void k_merge_items(int N, const int* __restrict__ cnt, const int* __restrict__ dof,
+                              const double2* __restrict__ val, float2* __restrict__ N2,
+                              float2* __restrict__ D2, SysOut so) {
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= N) return;
+  const size_t base = (size_t)row * kItemCap;
+  const int nn = min(cnt[2 * row], kNearItems), ns = min(cnt[2 * row + 1], kSingItems);
+  for (int k = 0; k < nn; ++k) {
+    const double2 v = val[base + k];
+    add_entry(N2, D2, so, N, row, dof[base + k], v.x, v.y);
+  }
+  for (int k = 0; k < ns; ++k) {
+    const double2 v = val[base + kNearItems + k];
+    add_entry(N2, D2, so, N, row, dof[base + kNearItems + k], v.x, v.y);
+  }
+}
+
 // Candidate panels of the near field per block of kNearBlock consecutive
 // rows (a compact patch in the Morton order): those whose near sphere can
 // reach any row of the block, |centre_block - centre_panel| < r_block +
@@ -494,9 +535,10 @@ __global__ void __launch_bounds__(256)
 __global__ void __launch_bounds__(256)
     k_near_mixed(int N, int C, const double* __restrict__ X, const int* __restrict__ dnset,
                  const int4* __restrict__ cell_dofs, const float4* __restrict__ cellgeo,
-                 const double* __restrict__ rec64, float2* __restrict__ N2,
-                 float2* __restrict__ D2, double* __restrict__ alpha_near, SysOut so,
-                 const int* __restrict__ ncnt, const int* __restrict__ nlist) {
+                 const double* __restrict__ rec64, int* __restrict__ item_cnt,
+                 int* __restrict__ item_dof, double2* __restrict__ item_val,
+                 double* __restrict__ alpha_near, const int* __restrict__ ncnt,
+                 const int* __restrict__ nlist, DevErr* err) {
   const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (row >= N) return;
@@ -507,6 +549,7 @@ __global__ void __launch_bounds__(256)
   for (int k = 0; k < kMaxSet; ++k) set[k] = dnset[(size_t)row * kMaxSet + k];
   const int nq = c_qm.q1 * c_qm.q1;
   double asum = 0.0;
+  int nitem = 0;
   // candidates of this row's block (ascending panel order), else every panel
   const int nc = ncnt[row / kNearBlock];
   const int* cl = nlist + (size_t)(row / kNearBlock) * kNearCap;
@@ -547,31 +590,30 @@ __global__ void __launch_bounds__(256)
         const int4 d = cell_dofs[cell];
         const int id[4] = {d.x, d.y, d.z, d.w};
         for (int j = 0; j < 4; ++j) {
-          const size_t o = (size_t)row * N + id[j];
-          float2 v = N2[o];
-          double s = (double)v.x + (double)v.y + ln[j];
-          float h = __double2float_rn(s);
-          N2[o] = make_float2(h, __double2float_rn(s - (double)h));
-          const float nh = h;
-          v = D2[o];
-          s = (double)v.x + (double)v.y + ld[j];
-          h = __double2float_rn(s);
-          D2[o] = make_float2(h, __double2float_rn(s - (double)h));
-          if (so.S) so.S[(size_t)row * so.ld + id[j]] = so.mask[id[j]] ? -h : nh;
+          if (nitem < kNearItems) {
+            const size_t o = (size_t)row * kItemCap + nitem;
+            item_dof[o] = id[j];
+            item_val[o] = make_double2(ln[j], ld[j]);
+          }
+          ++nitem;
           asum += ln[j];
         }
       }
     }
   }
-  if (lane == 0) alpha_near[row] = asum;
+  if (lane == 0) {
+    alpha_near[row] = asum;
+    item_cnt[2 * row] = nitem;
+    if (nitem > kNearItems) dev_fail(err, WBEM_ERR_NOMEM, 43, row, nitem);
+  }
 }
 
 // FP64 vertex-singular panels, added to the (hi, lo) entries.
 __global__ void k_singular_mixed(int N, const double* __restrict__ X, const int* __restrict__ dnset,
                                  const int* __restrict__ sptr, const int* __restrict__ scell,
-                                 const int4* __restrict__ cell_dofs, float2* __restrict__ N2,
-                                 float2* __restrict__ D2, double* __restrict__ alpha_sing,
-                                 SysOut so, DevErr* err) {
+                                 const int4* __restrict__ cell_dofs, int* __restrict__ item_cnt,
+                                 int* __restrict__ item_dof, double2* __restrict__ item_val,
+                                 double* __restrict__ alpha_sing, DevErr* err) {
   const int row = blockIdx.x * blockDim.x + threadIdx.x;
   if (row >= N) return;
   const double xi = X[3 * (size_t)row], yi = X[3 * (size_t)row + 1], zi = X[3 * (size_t)row + 2];
@@ -580,6 +622,7 @@ __global__ void k_singular_mixed(int N, const double* __restrict__ X, const int*
   for (int k = 0; k < kMaxSet; ++k) set[k] = dnset[(size_t)row * kMaxSet + k];
   const int nsp = c_qm.nsp;
   double asum = 0.0;
+  int nitem = 0;
   for (int e = sptr[row]; e < sptr[row + 1]; ++e) {
     const int cell = scell[e];
     const int4 d = cell_dofs[cell];
@@ -611,21 +654,18 @@ __global__ void k_singular_mixed(int N, const double* __restrict__ X, const int*
       }
     }
     for (int j = 0; j < 4; ++j) {
-      const size_t o = (size_t)row * N + id[j];
-      float2 vv = N2[o];
-      double sN = (double)vv.x + (double)vv.y + ln[j];
-      float h = __double2float_rn(sN);
-      N2[o] = make_float2(h, __double2float_rn(sN - (double)h));
-      const float nh = h;
-      vv = D2[o];
-      double sD = (double)vv.x + (double)vv.y + ld[j];
-      h = __double2float_rn(sD);
-      D2[o] = make_float2(h, __double2float_rn(sD - (double)h));
-      if (so.S) so.S[(size_t)row * so.ld + id[j]] = so.mask[id[j]] ? -h : nh;
+      if (nitem < kSingItems) {
+        const size_t o = (size_t)row * kItemCap + kNearItems + nitem;
+        item_dof[o] = id[j];
+        item_val[o] = make_double2(ln[j], ld[j]);
+      }
+      ++nitem;
       asum += ln[j];
     }
   }
   alpha_sing[row] = asum;
+  item_cnt[2 * row + 1] = nitem;
+  if (nitem > kSingItems) dev_fail(err, WBEM_ERR_NOMEM, 44, row, nitem);
 }
 
 __global__ void k_alpha_mixed(int N, int n_tiles, const double* __restrict__ part,
@@ -696,6 +736,41 @@ int assemble_mixed(wbem_context* h) {
     so = SysOut{h->d_lu, system_ld(N), h->d_mask};
   }
   h->s32_state = 0;
+  // near field and singular panels (FP64) on the auxiliary stream, beside the
+  // FP32 far-field kernel; their contributions are merged afterwards
+  if (!h->aux_stream) {
+    CUM(cudaStreamCreateWithFlags(&h->aux_stream, cudaStreamNonBlocking));
+    CUM(cudaEventCreateWithFlags(&h->ev_aux_fork, cudaEventDisableTiming));
+    CUM(cudaEventCreateWithFlags(&h->ev_aux_join, cudaEventDisableTiming));
+  }
+  if (h->item_rows < (size_t)N) {
+    CHKM(dev_alloc(h, &h->d_item_val, (size_t)N * kItemCap));
+    CHKM(dev_alloc(h, &h->d_item_dof, (size_t)N * kItemCap));
+    CHKM(dev_alloc(h, &h->d_item_cnt, (size_t)2 * N));
+    h->item_rows = N;
+  }
+  {
+    const int nblk = (N + kNearBlock - 1) / kNearBlock;
+    if (h->near_cap < nblk) {
+      CHKM(dev_alloc(h, &h->d_near_cnt, (size_t)nblk));
+      CHKM(dev_alloc(h, &h->d_near_cells, (size_t)nblk * kNearCap));
+      h->near_cap = nblk;
+    }
+    cudaStream_t ax = h->aux_stream;
+    CUM(cudaEventRecord(h->ev_aux_fork, h->stream));
+    CUM(cudaStreamWaitEvent(ax, h->ev_aux_fork, 0));
+    k_near_candidates<<<nblk, 256, 0, ax>>>(N, C, h->d_X, geo, h->d_near_cnt, h->d_near_cells);
+    CUM(cudaGetLastError());
+    k_near_mixed<<<(unsigned)(((size_t)N * 32 + 255) / 256), 256, 0, ax>>>(
+        N, C, h->d_X, h->d_dnset, h->d_cell_dofs, geo, h->d_rec, h->d_item_cnt, h->d_item_dof,
+        h->d_item_val, h->d_alpha_near, h->d_near_cnt, h->d_near_cells, h->d_err);
+    CUM(cudaGetLastError());
+    k_singular_mixed<<<(N + 63) / 64, 64, 0, ax>>>(N, h->d_X, h->d_dnset, h->d_sptr, h->d_scell,
+                                                    h->d_cell_dofs, h->d_item_cnt, h->d_item_dof,
+                                                    h->d_item_val, h->d_alpha_sing, h->d_err);
+    CUM(cudaGetLastError());
+    CUM(cudaEventRecord(h->ev_aux_join, ax));
+  }
   cudaError_t e;
   switch (q1) {
     case 2: e = launch_tile_mixed_t<2>(N, h->d_X, h->d_dnset, h->n_tiles, h->d_tile_ptr, h->d_tile_ent, h->d_cell_dofs, h->d_rec32, geo, h->d_N2, h->d_D2, h->d_alpha_part, so, h->d_err, h->stream); break;
@@ -706,23 +781,10 @@ int assemble_mixed(wbem_context* h) {
   }
   CUM(e);
   h->stats.t_assemble_ms = tm.ms();
-  {
-    const int nblk = (N + kNearBlock - 1) / kNearBlock;
-    if (h->near_cap < nblk) {
-      CHKM(dev_alloc(h, &h->d_near_cnt, (size_t)nblk));
-      CHKM(dev_alloc(h, &h->d_near_cells, (size_t)nblk * kNearCap));
-      h->near_cap = nblk;
-    }
-    k_near_candidates<<<nblk, 256, 0, h->stream>>>(N, C, h->d_X, geo, h->d_near_cnt, h->d_near_cells);
-    CUM(cudaGetLastError());
-  }
-  k_near_mixed<<<(unsigned)(((size_t)N * 32 + 255) / 256), 256, 0, h->stream>>>(
-      N, C, h->d_X, h->d_dnset, h->d_cell_dofs, geo, h->d_rec, h->d_N2, h->d_D2, h->d_alpha_near,
-      so, h->d_near_cnt, h->d_near_cells);
-  CUM(cudaGetLastError());
-  k_singular_mixed<<<(N + 63) / 64, 64, 0, h->stream>>>(N, h->d_X, h->d_dnset, h->d_sptr,
-                                                         h->d_scell, h->d_cell_dofs, h->d_N2,
-                                                         h->d_D2, h->d_alpha_sing, so, h->d_err);
+  // join the near / singular work and add it to the far-field entries
+  CUM(cudaStreamWaitEvent(h->stream, h->ev_aux_join, 0));
+  k_merge_items<<<(N + 127) / 128, 128, 0, h->stream>>>(N, h->d_item_cnt, h->d_item_dof,
+                                                         h->d_item_val, h->d_N2, h->d_D2, so);
   CUM(cudaGetLastError());
   h->stats.t_singular_ms = tm.ms();
   k_alpha_mixed<<<(N + 255) / 256, 256, 0, h->stream>>>(N, h->n_tiles, h->d_alpha_part,
@@ -731,7 +793,7 @@ int assemble_mixed(wbem_context* h) {
   CUM(cudaGetLastError());
   h->stats.t_alpha_ms = tm.ms();
   if (so.S) h->s32_state = 1;  // entries written; free term and constraints pending
-  h->launches += 6;
+  h->launches += 8;
   return check_device_error(h, "assemble (mixed)");
 }
 

@@ -1035,7 +1035,8 @@ int wbem_destroy(wbem_handle h) {
                   h->d_scell, h->d_perm, h->d_iperm, h->d_ncptr, h->d_ncent, h->d_mask, h->d_rec,
                   h->d_rec32, h->d_cellc, h->d_cellgeo, h->d_N, h->d_D, h->d_N2, h->d_D2,
                   h->d_alpha, h->d_alpha_part, h->d_alpha_near, h->d_alpha_sing, h->d_near_cnt,
-                  h->d_near_cells, h->d_crow, h->d_cptr, h->d_ccol, h->d_cval, h->d_cinh,
+                  h->d_near_cells, h->d_item_val, h->d_item_dof, h->d_item_cnt,
+                  h->d_crow, h->d_cptr, h->d_ccol, h->d_cval, h->d_cinh,
                   h->d_cflag, h->d_cptr_full, h->d_ccol_full, h->d_cval_full, h->d_tptr,
                   h->d_tsrc, h->d_tval, h->d_binv, h->d_V, h->d_part, h->d_small, h->d_lu,
                   h->d_split, h->d_lutmp, h->d_info, h->d_sol, h->d_rhs, h->d_b, h->d_err};
@@ -1043,6 +1044,9 @@ int wbem_destroy(wbem_handle h) {
     if (p) cudaFree(p);
   for (int k = 0; k < kNumVec; ++k)
     if (h->d_vec[k]) cudaFree(h->d_vec[k]);
+  if (h->aux_stream) cudaStreamDestroy(h->aux_stream);
+  if (h->ev_aux_fork) cudaEventDestroy(h->ev_aux_fork);
+  if (h->ev_aux_join) cudaEventDestroy(h->ev_aux_join);
   if (h->own_stream) cudaStreamDestroy(h->stream);
   delete h;
   return WBEM_OK;
