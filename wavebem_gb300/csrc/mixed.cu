@@ -739,7 +739,11 @@ int assemble_mixed(wbem_context* h) {
   // near field and singular panels (FP64) on the auxiliary stream, beside the
   // FP32 far-field kernel; their contributions are merged afterwards
   if (!h->aux_stream) {
-    CUM(cudaStreamCreateWithFlags(&h->aux_stream, cudaStreamNonBlocking));
+    // high priority: its CTAs take the free slots beside the far-field CTAs
+    // first, so the FP64 work hides under the FP32 kernel
+    int lo = 0, hi = 0;
+    CUM(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    CUM(cudaStreamCreateWithPriority(&h->aux_stream, cudaStreamNonBlocking, hi));
     CUM(cudaEventCreateWithFlags(&h->ev_aux_fork, cudaEventDisableTiming));
     CUM(cudaEventCreateWithFlags(&h->ev_aux_join, cudaEventDisableTiming));
   }
