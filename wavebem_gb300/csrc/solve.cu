@@ -73,42 +73,21 @@ cudaError_t launch_matvec_fp64(int N, int mode, const double* Nm, const double* 
 }
 
 // Same operator with (hi, lo) float pairs: entry = hi + lo, products and sums
-// in double-float on FP32 units, x split into (hi, lo) per column chunk in
-// shared memory. Each warp walks two rows; a lane takes two adjacent columns
-// per step and reads both entries with one 16-byte load when the columns
-// have the same boundary condition (the usual case in the dof order), which
-// keeps four such loads per row in flight per lane.
-constexpr int kMvRows = 2;  // rows per warp
+// in double-float on FP32 units, x given in FP64 and split on the fly.
 __global__ void __launch_bounds__(kMvWarps * 32)
     k_matvec_mixed(int N, int mode, const float2* __restrict__ N2, const float2* __restrict__ D2,
                    const uint8_t* __restrict__ mask, const double* __restrict__ alpha,
                    const double* __restrict__ x, double* __restrict__ y) {
-  __shared__ __align__(16) float2 xs[kMvChunk];
-  __shared__ __align__(4) uint8_t ms[kMvChunk];
+  __shared__ float2 xs[kMvChunk];
+  __shared__ uint8_t ms[kMvChunk];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int row0 = (blockIdx.x * kMvWarps + warp) * kMvRows;
-  const float2* A0 = (mode == 0) ? N2 : D2;  // columns with mask 0
-  const float2* A1 = (mode == 0) ? D2 : N2;  // columns with mask 1 (negated)
-  const bool vec = (N & 1) == 0;             // row starts 16-byte aligned
-  df acc[kMvRows];
-  const float2* r0[kMvRows];
-  const float2* r1[kMvRows];
-#pragma unroll
-  for (int u = 0; u < kMvRows; ++u) {
-    acc[u] = df{0.f, 0.f};
-    const int row = min(row0 + u, N - 1);
-    r0[u] = A0 + (size_t)row * N;
-    r1[u] = A1 + (size_t)row * N;
-  }
-  auto mac = [&](df& a, float2 e, bool neg, float2 xv) {
-    if (neg) {
-      e.x = -e.x;
-      e.y = -e.y;
-    }
-    df p = two_prod(e.x, xv.x);
-    p.lo = __fmaf_rn(e.x, xv.y, __fmaf_rn(e.y, xv.x, p.lo));
-    a = df_add(a, p);
-  };
+  const int row = blockIdx.x * kMvWarps + warp;
+  const bool active = row < N;
+  const float2* A0 = (mode == 0) ? N2 : D2;
+  const float2* A1 = (mode == 0) ? D2 : N2;
+  const float2* r0 = A0 + (size_t)(active ? row : 0) * N;
+  const float2* r1 = A1 + (size_t)(active ? row : 0) * N;
+  df acc = {0.f, 0.f};
   for (int c0 = 0; c0 < N; c0 += kMvChunk) {
     const int cn = min(kMvChunk, N - c0);
     __syncthreads();
@@ -118,123 +97,89 @@ __global__ void __launch_bounds__(kMvWarps * 32)
       ms[k] = mask[c0 + k];
     }
     __syncthreads();
-    if (row0 < N) {
-#pragma unroll 4
-      for (int k = 2 * lane; k < cn; k += 64) {
+    if (active) {
+#pragma unroll 8
+      for (int k = lane; k < cn; k += 32) {
         const int j = c0 + k;
-        const bool two = k + 1 < cn;
-        const bool m0 = ms[k] != 0, m1 = two && ms[k + 1] != 0;
-        const float2 x0 = xs[k], x1 = two ? xs[k + 1] : make_float2(0.f, 0.f);
-#pragma unroll
-        for (int u = 0; u < kMvRows; ++u) {
-          float2 e0, e1 = make_float2(0.f, 0.f);
-          if (vec && two && m0 == m1) {
-            const float4 q = __ldcs(reinterpret_cast<const float4*>((m0 ? r1[u] : r0[u]) + j));
-            e0 = make_float2(q.x, q.y);
-            e1 = make_float2(q.z, q.w);
-          } else {
-            e0 = __ldcs((m0 ? r1[u] : r0[u]) + j);
-            if (two) e1 = __ldcs((m1 ? r1[u] : r0[u]) + j + 1);
-          }
-          mac(acc[u], e0, m0, x0);
-          mac(acc[u], e1, m1, x1);
+        float2 a = ms[k] ? __ldcs(r1 + j) : __ldcs(r0 + j);
+        if (ms[k]) {
+          a.x = -a.x;
+          a.y = -a.y;
         }
+        const float2 xv = xs[k];
+        df p = two_prod(a.x, xv.x);
+        p.lo = __fmaf_rn(a.x, xv.y, __fmaf_rn(a.y, xv.x, p.lo));
+        acc = df_add(acc, p);
       }
     }
   }
+  double s = df_to_double(acc);
 #pragma unroll
-  for (int u = 0; u < kMvRows; ++u) {
-    double s = df_to_double(acc[u]);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    const int row = row0 + u;
-    if (row < N && lane == 0) {
-      const double xi = x[row];
-      if (mode == 0) {
-        if (!mask[row]) s = fma(alpha[row], xi, s);
-      } else {
-        if (mask[row]) s = fma(-alpha[row], xi, s);
-      }
-      y[row] = s;
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (active && lane == 0) {
+    const double xi = x[row];
+    if (mode == 0) {
+      if (!mask[row]) s = fma(alpha[row], xi, s);
+    } else {
+      if (mask[row]) s = fma(-alpha[row], xi, s);
     }
+    y[row] = s;
   }
 }
 
 cudaError_t launch_matvec_mixed(int N, int mode, const float2* N2, const float2* D2,
                                 const uint8_t* mask, const double* alpha, const double* x,
                                 double* y, cudaStream_t s) {
-  const int rows_per_cta = kMvWarps * kMvRows;
-  k_matvec_mixed<<<(N + rows_per_cta - 1) / rows_per_cta, kMvWarps * 32, 0, s>>>(N, mode, N2, D2,
-                                                                                mask, alpha, x, y);
+  k_matvec_mixed<<<(N + kMvWarps - 1) / kMvWarps, kMvWarps * 32, 0, s>>>(N, mode, N2, D2, mask,
+                                                                          alpha, x, y);
   return cudaGetLastError();
 }
 
 // y = S x for the FP32 system matrix S (row-major, leading dimension ld, the
 // constrained operator with alpha on its diagonal): the inner operator of the
-// refinement solver. Each warp walks four rows, a lane streams float4 quads
-// of each with the matching quad of x (staged per chunk in shared memory),
-// so sixteen 16-byte loads per lane are in flight per unrolled step. Products
-// and sums in FP32 with the lane sums moved into FP64 after every chunk of
-// kMvChunk columns (64 terms per FP32 partial sum), so the operator is S to
-// about 1e-6 relative, at 4 bytes of HBM traffic per entry.
-constexpr int kS32Rows = 4;  // rows per warp
+// refinement solver. One warp per row, each lane streams float4 quads of the
+// row; products and sums in FP32 with the lane sums moved into FP64 after
+// every chunk of kMvChunk columns (64 terms per FP32 partial sum), so the
+// operator is S to about 1e-6 relative, at 4 bytes of HBM traffic per entry.
 __global__ void __launch_bounds__(kMvWarps * 32)
     k_matvec_s32(int N, int ld, const float* __restrict__ S, const double* __restrict__ x,
                  double* __restrict__ y) {
   __shared__ __align__(16) float xs[kMvChunk];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int row0 = (blockIdx.x * kMvWarps + warp) * kS32Rows;
-  const float* sr[kS32Rows];
-  double acc[kS32Rows];
-#pragma unroll
-  for (int u = 0; u < kS32Rows; ++u) {
-    sr[u] = S + (size_t)min(row0 + u, N - 1) * ld;
-    acc[u] = 0.0;
-  }
+  const int row = blockIdx.x * kMvWarps + warp;
+  const bool active = row < N;
+  const float* sr = S + (size_t)(active ? row : 0) * ld;
+  double acc = 0.0;
   for (int c0 = 0; c0 < N; c0 += kMvChunk) {
     const int cn = min(kMvChunk, N - c0);
     __syncthreads();
     for (int k = threadIdx.x; k < kMvChunk; k += blockDim.x)
       xs[k] = (k < cn) ? (float)x[c0 + k] : 0.f;
     __syncthreads();
-    if (row0 < N) {
-      float a[kS32Rows][4];
-#pragma unroll
-      for (int u = 0; u < kS32Rows; ++u) a[u][0] = a[u][1] = a[u][2] = a[u][3] = 0.f;
+    if (active) {
+      float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
       const int cq = cn & ~3;  // whole quads (row starts are 16-byte aligned)
 #pragma unroll 4
       for (int k = 4 * lane; k < cq; k += 128) {
+        const float4 v = __ldcs(reinterpret_cast<const float4*>(sr + c0 + k));
         const float4 xv = *reinterpret_cast<const float4*>(xs + k);
-#pragma unroll
-        for (int u = 0; u < kS32Rows; ++u) {
-          const float4 v = __ldcs(reinterpret_cast<const float4*>(sr[u] + c0 + k));
-          a[u][0] = __fmaf_rn(v.x, xv.x, a[u][0]);
-          a[u][1] = __fmaf_rn(v.y, xv.y, a[u][1]);
-          a[u][2] = __fmaf_rn(v.z, xv.z, a[u][2]);
-          a[u][3] = __fmaf_rn(v.w, xv.w, a[u][3]);
-        }
+        a0 = __fmaf_rn(v.x, xv.x, a0);
+        a1 = __fmaf_rn(v.y, xv.y, a1);
+        a2 = __fmaf_rn(v.z, xv.z, a2);
+        a3 = __fmaf_rn(v.w, xv.w, a3);
       }
-      for (int k = cq + lane; k < cn; k += 32)
-#pragma unroll
-        for (int u = 0; u < kS32Rows; ++u) a[u][0] = __fmaf_rn(sr[u][c0 + k], xs[k], a[u][0]);
-#pragma unroll
-      for (int u = 0; u < kS32Rows; ++u)
-        acc[u] += ((double)a[u][0] + (double)a[u][1]) + ((double)a[u][2] + (double)a[u][3]);
+      for (int k = cq + lane; k < cn; k += 32) a0 = __fmaf_rn(sr[c0 + k], xs[k], a0);
+      acc += ((double)a0 + (double)a1) + ((double)a2 + (double)a3);
     }
   }
 #pragma unroll
-  for (int u = 0; u < kS32Rows; ++u) {
-    double v = acc[u];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (row0 + u < N && lane == 0) y[row0 + u] = v;
-  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (active && lane == 0) y[row] = acc;
 }
 
 cudaError_t launch_matvec_s32(int N, int ld, const float* S, const double* x, double* y,
                               cudaStream_t s) {
-  const int rows_per_cta = kMvWarps * kS32Rows;
-  k_matvec_s32<<<(N + rows_per_cta - 1) / rows_per_cta, kMvWarps * 32, 0, s>>>(N, ld, S, x, y);
+  k_matvec_s32<<<(N + kMvWarps - 1) / kMvWarps, kMvWarps * 32, 0, s>>>(N, ld, S, x, y);
   return cudaGetLastError();
 }
 
