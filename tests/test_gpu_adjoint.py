@@ -147,3 +147,33 @@ def test_adjoint_shape_parameters_autograd():
             vals.append(_force(g, mm, M.wigley_bc(mm, seed=3), hull))
         fd[j] = (vals[0] - vals[1]) / (2 * h)
     assert rel2(grad, fd) <= 1e-6, (grad, fd)
+
+
+@pytest.mark.parametrize("prec", [PREC_FP64, PREC_MIXED])
+def test_adjoint_matches_oracle_directional_differences(prec):
+    """The GPU adjoint against FP64 central differences of the CPU oracle
+    (the reference algorithm restated: assembly, constrained solve, hull
+    force), along a random direction over the hull nodes."""
+    import oracle as O
+    m, ptr, idx, hull = _setup(800, None)
+    b = M.wigley_bc(m, seed=3)
+    g = BEMProblem(m.X, m.cells, m.dirichlet, ptr, idx, precision=prec, tolerance=1e-14)
+    _force(g, m, b, hull)
+    gX, _ = g.force_adjoint(hull, b)
+    d = np.zeros_like(m.X)
+    hull_nodes = np.unique(m.cells[hull])
+    d[hull_nodes] = np.random.default_rng(11).normal(size=(len(hull_nodes), 3))
+    h = 1e-6
+
+    def oracle_force(X):
+        P = O.Problem(X, m.cells, ptr, idx, m.dirichlet)
+        P.assemble()
+        phi, dphi, _ = P.solve_system(b)
+        return P.hull_force(m.cells[hull], phi, dphi)
+
+    fd = (oracle_force(m.X + h * d) - oracle_force(m.X - h * d)) / (2 * h)
+    ad = float(np.sum(gX * d))
+    # FP64: the north-star bar; mixed: its forward map differs from FP64 by
+    # ~1e-9 and its gradient by <= 1e-6 (test_adjoint_mixed_matches_fp64)
+    tol = 1e-6 if prec == PREC_FP64 else 3e-6
+    assert abs(ad - fd) <= tol * abs(fd), (ad, fd)

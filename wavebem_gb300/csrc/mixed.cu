@@ -422,7 +422,7 @@ static cudaError_t launch_tile_mixed_t(int N, const double* X, const int* dnset,
 // (column, dN, dD) in the order the reference adds them, so that the FP64
 // kernels run beside the FP32 far-field kernel (they use different pipes)
 // and k_merge_items adds them to the (hi, lo) entries afterwards.
-constexpr int kNearItems = 384;  // per row: 4 items per near panel
+constexpr int kNearItems = 1024;  // per row: 4 items per near panel (256 panels)
 constexpr int kSingItems = 128;  // per row: 4 items per singular panel
 constexpr int kItemCap = kNearItems + kSingItems;
 
