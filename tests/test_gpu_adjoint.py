@@ -163,6 +163,14 @@ def test_adjoint_matches_oracle_directional_differences(prec):
     d = np.zeros_like(m.X)
     hull_nodes = np.unique(m.cells[hull])
     d[hull_nodes] = np.random.default_rng(11).normal(size=(len(hull_nodes), 3))
+    # a double node is one point: its copies on the free surface move with
+    # the hull copy. (Moving one copy alone tears the vertex-singular panels
+    # apart; the discrete map then has third derivatives of order 1/r^4 at the
+    # nearest quadrature points, and central differences with h = 1e-6 are off
+    # by ~1e-6 relative, shrinking as h^2, while the adjoint stays exact.)
+    for i in hull_nodes:
+        for j in idx[ptr[i]:ptr[i + 1]]:
+            d[j] = d[i]
     h = 1e-6
 
     def oracle_force(X):
@@ -175,5 +183,5 @@ def test_adjoint_matches_oracle_directional_differences(prec):
     ad = float(np.sum(gX * d))
     # FP64: the spec bar; mixed: its forward map differs from FP64 by
     # ~1e-9 and its gradient by <= 1e-6 (test_adjoint_mixed_matches_fp64)
-    tol = 1e-6 if prec == PREC_FP64 else 3e-6
+    tol = 1e-6 if prec == PREC_FP64 else 2e-6
     assert abs(ad - fd) <= tol * abs(fd), (ad, fd)

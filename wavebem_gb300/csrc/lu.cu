@@ -1089,11 +1089,17 @@ __global__ void __launch_bounds__(kTriThreads)
     if (mode >= 2 && tid < kNB) acc[tid] -= part[tid] + part[kNB + tid];
     __syncthreads();
   }
-  // diagonal block
+  // diagonal block (four independent partial sums: this is on the chain)
   if (tid < kNB) {
-    float s2 = 0.f;
-    for (int c = 0; c < kNB; ++c) s2 = __fmaf_rn(sInv[c * kNB + tid], acc[c], s2);
-    if (tid < nb) out[k0 + tid] = s2;
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+#pragma unroll 4
+    for (int c = 0; c < kNB; c += 4) {
+      s0 = __fmaf_rn(sInv[c * kNB + tid], acc[c], s0);
+      s1 = __fmaf_rn(sInv[(c + 1) * kNB + tid], acc[c + 1], s1);
+      s2 = __fmaf_rn(sInv[(c + 2) * kNB + tid], acc[c + 2], s2);
+      s3 = __fmaf_rn(sInv[(c + 3) * kNB + tid], acc[c + 3], s3);
+    }
+    if (tid < nb) out[k0 + tid] = (s0 + s1) + (s2 + s3);
   }
   __syncthreads();
   if (tid == 0) {

@@ -527,11 +527,11 @@ __global__ void __launch_bounds__(256)
   if (tid == 0) cnt[blockIdx.x] = total <= kNearCap ? total : -1;
 }
 
-// FP64 near field: one warp per row. The lanes test 32 panels at a time
-// against the near criterion (same test as the tile kernel); each near,
+// FP64 near field: one warp per row. The lanes test 32 candidate panels at a
+// time against the near criterion (same test as the tile kernel); each near,
 // non-singular panel is then integrated with the regular rule in FP64, one
-// quadrature point per lane, and added to the (hi, lo) entries by lane 0 in
-// ascending panel order.
+// quadrature point per lane, and lane 0 appends its four contributions to the
+// row's items in ascending panel order.
 __global__ void __launch_bounds__(256)
     k_near_mixed(int N, int C, const double* __restrict__ X, const int* __restrict__ dnset,
                  const int4* __restrict__ cell_dofs, const float4* __restrict__ cellgeo,
@@ -608,7 +608,8 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// FP64 vertex-singular panels, added to the (hi, lo) entries.
+// FP64 vertex-singular panels (one thread per row), appended to the row's
+// singular items.
 __global__ void k_singular_mixed(int N, const double* __restrict__ X, const int* __restrict__ dnset,
                                  const int* __restrict__ sptr, const int* __restrict__ scell,
                                  const int4* __restrict__ cell_dofs, int* __restrict__ item_cnt,
