@@ -388,6 +388,90 @@ struct PanelArgs {
   int col_split;
 };
 
+// Writes (or subtracts) a thread's 4 x 4 quads of a panel product and the
+// BF16 splits of the written values, 4 consecutive K entries per 8-byte store.
+// Rows {ty*4 + u + 64 hu}, columns {tx*4 + v + 64 hv} of the CTA tile.
+template <int RH, int CH>
+__device__ __forceinline__ void panel_epilogue(const PanelArgs& pa, const SplitOut& s1,
+                                               const SplitOut& s2, float (&acc)[4 * RH][4 * CH],
+                                               int i0, int j0, int ty, int tx) {
+#pragma unroll
+  for (int hu = 0; hu < RH; ++hu)
+#pragma unroll
+    for (int hv = 0; hv < CH; ++hv) {
+      const int ib = i0 + hu * 64 + ty * 4;  // first row of the quad
+      const int jb = j0 + hv * 64 + tx * 4;  // first column of the quad
+      if (ib >= pa.rows || jb >= pa.cols) continue;
+      const int nu = min(4, pa.rows - ib), nv = min(4, pa.cols - jb);
+      float r[4][4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) r[u][v] = acc[hu * 4 + u][hv * 4 + v];
+      for (int u = 0; u < nu; ++u) {
+        float* op = pa.O + (size_t)(ib + u) * pa.ldo + jb;
+        if (nv == 4) {
+          float4 o4 = make_float4(r[u][0], r[u][1], r[u][2], r[u][3]);
+          if (pa.sub) {
+            const float4 c = *reinterpret_cast<const float4*>(op);
+            o4 = make_float4(c.x - o4.x, c.y - o4.y, c.z - o4.z, c.w - o4.w);
+          }
+          *reinterpret_cast<float4*>(op) = o4;
+          r[u][0] = o4.x; r[u][1] = o4.y; r[u][2] = o4.z; r[u][3] = o4.w;
+        } else {
+          for (int v = 0; v < nv; ++v) {
+            r[u][v] = pa.sub ? op[v] - r[u][v] : r[u][v];
+            op[v] = r[u][v];
+          }
+        }
+      }
+      // BF16 splits, 4 consecutive K entries packed into one 8-byte store
+      for (int w = 0; w < 2; ++w) {
+        const SplitOut& so = w == 0 ? s1 : s2;
+        if (!so.hi) continue;
+        if (pa.col_split) {
+          // split row = absolute column, K index = row (4 rows contiguous)
+          for (int v = 0; v < nv; ++v) {
+            const int aj = pa.abs_col0 + jb + v;
+            if (aj < so.row0) continue;
+            const size_t o = (size_t)(aj - so.row0) * so.ld + so.coloff + ib;
+            uint16_t hh[4], ll[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) split_bf16(u < nu ? r[u][v] : 0.f, &hh[u], &ll[u]);
+            if (nu == 4) {
+              *reinterpret_cast<uint2*>(so.hi + o) = *reinterpret_cast<const uint2*>(hh);
+              *reinterpret_cast<uint2*>(so.lo + o) = *reinterpret_cast<const uint2*>(ll);
+            } else {
+              for (int u = 0; u < nu; ++u) {
+                so.hi[o + u] = hh[u];
+                so.lo[o + u] = ll[u];
+              }
+            }
+          }
+        } else {
+          // split row = absolute row, K index = column (4 columns contiguous)
+          for (int u = 0; u < nu; ++u) {
+            const int ai = pa.abs_row0 + ib + u;
+            if (ai < so.row0) continue;
+            const size_t o = (size_t)(ai - so.row0) * so.ld + so.coloff + jb;
+            uint16_t hh[4], ll[4];
+#pragma unroll
+            for (int v = 0; v < 4; ++v) split_bf16(v < nv ? r[u][v] : 0.f, &hh[v], &ll[v]);
+            if (nv == 4) {
+              *reinterpret_cast<uint2*>(so.hi + o) = *reinterpret_cast<const uint2*>(hh);
+              *reinterpret_cast<uint2*>(so.lo + o) = *reinterpret_cast<const uint2*>(ll);
+            } else {
+              for (int v = 0; v < nv; ++v) {
+                so.hi[o + v] = hh[v];
+                so.lo[o + v] = ll[v];
+              }
+            }
+          }
+        }
+      }
+    }
+}
+
 // Panel products with the whole K chunk resident in shared memory: the CTA
 // copies its Lft rows (TM x 128) and the Rgt block (128 x TN) with cp.async in
 // one go, waits once, and runs 128 FMA steps from shared memory (no per-step
@@ -475,82 +559,127 @@ __global__ void __launch_bounds__(256, 2) k_panel_tile(PanelArgs pa, SplitOut s1
         for (int v = 0; v < 4 * CH; ++v) acc[u][v] = __fmaf_rn(a[u], b[v], acc[u][v]);
     }
   }
-  // ---- epilogue: 4 x 4 blocks of (row quad, column quad)
+  panel_epilogue<RH, CH>(pa, s1, s2, acc, i0, j0, ty, tx);
+}
+
+// The same panel products with a 12 KB shared-memory footprint: K streams
+// through shared memory 16 at a time (register prefetch of the next step),
+// so these CTAs fit beside a persistent GEMM CTA (208 KB) on the same SM and
+// the panel chain of the next outer panel runs while the bulk trailing update
+// holds every SM.
+//   TM x TN = 64 x 128 (column panels, full width) or 128 x 64 (row panels
+//   and updates, full height); 256 threads, 32 outputs each.
+template <int TM, int TN, bool ATRANS>
+__global__ void __launch_bounds__(256) k_panel_small(PanelArgs pa, SplitOut s1, SplitOut s2) {
+  constexpr int BK = 16;
+  constexpr int RH = TM / 64, CH = TN / 64;
+  __shared__ __align__(16) float As[BK][TM + 4];
+  __shared__ __align__(16) float Bs[BK][TN];
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int i0 = blockIdx.x * TM, j0 = blockIdx.y * TN;
+  // staging: Lft TM x 16 (TM * 4 quads), Rgt 16 x TN (TN * 4 quads)
+  constexpr int LQ = TM * BK / 4 / 256;  // quads per thread (1 or 2)
+  constexpr int RQ = TN * BK / 4 / 256;
+  float4 la[LQ], rb[RQ];
+  auto load = [&](int kk) {
 #pragma unroll
-  for (int hu = 0; hu < RH; ++hu)
-#pragma unroll
-    for (int hv = 0; hv < CH; ++hv) {
-      const int ib = i0 + hu * 64 + ty * 4;  // first row of the quad
-      const int jb = j0 + hv * 64 + tx * 4;  // first column of the quad
-      if (ib >= pa.rows || jb >= pa.cols) continue;
-      const int nu = min(4, pa.rows - ib), nv = min(4, pa.cols - jb);
-      float r[4][4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int v = 0; v < 4; ++v) r[u][v] = acc[hu * 4 + u][hv * 4 + v];
-      for (int u = 0; u < nu; ++u) {
-        float* op = pa.O + (size_t)(ib + u) * pa.ldo + jb;
-        if (nv == 4) {
-          float4 o4 = make_float4(r[u][0], r[u][1], r[u][2], r[u][3]);
-          if (pa.sub) {
-            const float4 c = *reinterpret_cast<const float4*>(op);
-            o4 = make_float4(c.x - o4.x, c.y - o4.y, c.z - o4.z, c.w - o4.w);
-          }
-          *reinterpret_cast<float4*>(op) = o4;
-          r[u][0] = o4.x; r[u][1] = o4.y; r[u][2] = o4.z; r[u][3] = o4.w;
-        } else {
-          for (int v = 0; v < nv; ++v) {
-            r[u][v] = pa.sub ? op[v] - r[u][v] : r[u][v];
-            op[v] = r[u][v];
-          }
-        }
-      }
-      // BF16 splits, 4 consecutive K entries packed into one 8-byte store
-      for (int w = 0; w < 2; ++w) {
-        const SplitOut& so = w == 0 ? s1 : s2;
-        if (!so.hi) continue;
-        if (pa.col_split) {
-          // split row = absolute column, K index = row (4 rows contiguous)
-          for (int v = 0; v < nv; ++v) {
-            const int aj = pa.abs_col0 + jb + v;
-            if (aj < so.row0) continue;
-            const size_t o = (size_t)(aj - so.row0) * so.ld + so.coloff + ib;
-            uint16_t hh[4], ll[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) split_bf16(u < nu ? r[u][v] : 0.f, &hh[u], &ll[u]);
-            if (nu == 4) {
-              *reinterpret_cast<uint2*>(so.hi + o) = *reinterpret_cast<const uint2*>(hh);
-              *reinterpret_cast<uint2*>(so.lo + o) = *reinterpret_cast<const uint2*>(ll);
-            } else {
-              for (int u = 0; u < nu; ++u) {
-                so.hi[o + u] = hh[u];
-                so.lo[o + u] = ll[u];
-              }
-            }
-          }
-        } else {
-          // split row = absolute row, K index = column (4 columns contiguous)
-          for (int u = 0; u < nu; ++u) {
-            const int ai = pa.abs_row0 + ib + u;
-            if (ai < so.row0) continue;
-            const size_t o = (size_t)(ai - so.row0) * so.ld + so.coloff + jb;
-            uint16_t hh[4], ll[4];
-#pragma unroll
-            for (int v = 0; v < 4; ++v) split_bf16(v < nv ? r[u][v] : 0.f, &hh[v], &ll[v]);
-            if (nv == 4) {
-              *reinterpret_cast<uint2*>(so.hi + o) = *reinterpret_cast<const uint2*>(hh);
-              *reinterpret_cast<uint2*>(so.lo + o) = *reinterpret_cast<const uint2*>(ll);
-            } else {
-              for (int v = 0; v < nv; ++v) {
-                so.hi[o + v] = hh[v];
-                so.lo[o + v] = ll[v];
-              }
-            }
-          }
-        }
+    for (int u = 0; u < LQ; ++u) {
+      const int q = tid + 256 * u;
+      if (ATRANS) {  // LT(k, i): rows of TM floats
+        const int k = q / (TM / 4), c = (q % (TM / 4)) * 4;
+        la[u] = i0 + c + 3 < pa.rows
+                    ? __ldcg(reinterpret_cast<const float4*>(pa.L + (size_t)(kk + k) * pa.ldl + i0 + c))
+                    : make_float4(0.f, 0.f, 0.f, 0.f);
+      } else {       // L(i, k): rows of 16 floats
+        const int i = q >> 2, c = (q & 3) * 4;
+        la[u] = i0 + i < pa.rows
+                    ? __ldcg(reinterpret_cast<const float4*>(pa.L + (size_t)(i0 + i) * pa.ldl + kk + c))
+                    : make_float4(0.f, 0.f, 0.f, 0.f);
       }
     }
+#pragma unroll
+    for (int u = 0; u < RQ; ++u) {
+      const int q = tid + 256 * u;
+      const int k = q / (TN / 4), c = (q % (TN / 4)) * 4;
+      const int gj = j0 + c;
+      const float* rp = pa.R + (size_t)(kk + k) * pa.ldr + gj;
+      if (gj + 3 < pa.cols) {
+        rb[u] = __ldcg(reinterpret_cast<const float4*>(rp));
+      } else {
+        rb[u].x = gj < pa.cols ? rp[0] : 0.f;
+        rb[u].y = gj + 1 < pa.cols ? rp[1] : 0.f;
+        rb[u].z = gj + 2 < pa.cols ? rp[2] : 0.f;
+        rb[u].w = gj + 3 < pa.cols ? rp[3] : 0.f;
+      }
+    }
+  };
+  auto stage = [&]() {
+#pragma unroll
+    for (int u = 0; u < LQ; ++u) {
+      const int q = tid + 256 * u;
+      if (ATRANS) {
+        const int k = q / (TM / 4), c = (q % (TM / 4)) * 4;
+        *reinterpret_cast<float4*>(&As[k][c]) = la[u];
+      } else {
+        const int i = q >> 2, c = (q & 3) * 4;
+        As[c + 0][i] = la[u].x;
+        As[c + 1][i] = la[u].y;
+        As[c + 2][i] = la[u].z;
+        As[c + 3][i] = la[u].w;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < RQ; ++u) {
+      const int q = tid + 256 * u;
+      const int k = q / (TN / 4), c = (q % (TN / 4)) * 4;
+      *reinterpret_cast<float4*>(&Bs[k][c]) = rb[u];
+    }
+  };
+  float acc[4 * RH][4 * CH];
+#pragma unroll
+  for (int u = 0; u < 4 * RH; ++u)
+#pragma unroll
+    for (int v = 0; v < 4 * CH; ++v) acc[u][v] = 0.f;
+  load(0);
+  stage();
+  __syncthreads();
+  const int nk = pa.K / BK;
+  for (int kt = 0; kt < nk; ++kt) {
+    if (kt + 1 < nk) load((kt + 1) * BK);
+#pragma unroll
+    for (int k = 0; k < BK; ++k) {
+      float a[4 * RH], b[4 * CH];
+#pragma unroll
+      for (int h = 0; h < RH; ++h) {
+        const float4 t = *reinterpret_cast<const float4*>(&As[k][h * 64 + ty * 4]);
+        a[4 * h] = t.x; a[4 * h + 1] = t.y; a[4 * h + 2] = t.z; a[4 * h + 3] = t.w;
+      }
+#pragma unroll
+      for (int h = 0; h < CH; ++h) {
+        const float4 t = *reinterpret_cast<const float4*>(&Bs[k][h * 64 + tx * 4]);
+        b[4 * h] = t.x; b[4 * h + 1] = t.y; b[4 * h + 2] = t.z; b[4 * h + 3] = t.w;
+      }
+#pragma unroll
+      for (int u = 0; u < 4 * RH; ++u)
+#pragma unroll
+        for (int v = 0; v < 4 * CH; ++v) acc[u][v] = __fmaf_rn(a[u], b[v], acc[u][v]);
+    }
+    __syncthreads();
+    if (kt + 1 < nk) {
+      stage();
+      __syncthreads();
+    }
+  }
+  panel_epilogue<RH, CH>(pa, s1, s2, acc, i0, j0, ty, tx);
+}
+
+template <int TM, int TN, bool ATRANS>
+static cudaError_t run_panel_small(const PanelArgs& pa, const SplitOut& s1, const SplitOut& s2,
+                                   cudaStream_t s) {
+  dim3 g((pa.rows + TM - 1) / TM, (pa.cols + TN - 1) / TN);
+  k_panel_small<TM, TN, ATRANS><<<g, 256, 0, s>>>(pa, s1, s2);
+  return cudaGetLastError();
 }
 
 template <int TM, int TN, bool ATRANS>
@@ -1361,15 +1490,13 @@ int factor_mixed(wbem_context* h) {
       h->launches++;
       if (k1 >= N) break;
       const int m = N - k1;
-      const SplitOut Lin{b1, b1 + rows * kNB, k1, kNB, 0};
-      const SplitOut Uin{b1 + 2 * rows * kNB, b1 + 3 * rows * kNB, k1, kNB, 0};
       const SplitOut L21{b2, b2 + rows * kNB2, p1, kNB2, k0 - p0};
       // column panel (full height), inner split + outer L21 split
       // L_ik = A_ik inv(U_kk) for rows k1.., in place
       const PanelArgs pc{A + (size_t)k1 * ld + k0, ld, L.uinv + bo, kNB, A + (size_t)k1 * ld + k0,
                          ld, m, kNB, kNB, k1, k0, 0, 0};
       pb(h->prof_panel, sp);
-      WB_CU((run_panel_tile<64, 128, false>(pc, Lin, p1 < N ? L21 : none, sp)));
+      WB_CU((run_panel_small<64, 128, false>(pc, none, p1 < N ? L21 : none, sp)));
       pe(h->prof_panel, sp, 0.0);
       h->launches++;
       if (k1 < p1) {
@@ -1378,11 +1505,13 @@ int factor_mixed(wbem_context* h) {
         const PanelArgs pr{L.linvT + bo, kNB, A + (size_t)k0 * ld + k1, ld, A + (size_t)k0 * ld + k1,
                            ld, kNB, w, kNB, k0, k1, 0, 1};
         pb(h->prof_panel, sp);
-        WB_CU((run_panel_tile<128, 64, true>(pr, Uin, none, sp)));
+        WB_CU((run_panel_small<128, 64, true>(pr, none, none, sp)));
+        // inner update A[k1:, k1:p1] -= L_ik U_kj in FP32 (small footprint, so
+        // it runs beside the previous outer panel's bulk update)
+        const PanelArgs pi{A + (size_t)k1 * ld + k0, ld, A + (size_t)k0 * ld + k1, ld,
+                           A + (size_t)k1 * ld + k1, ld, m, w, kNB, k1, k1, 1, 0};
+        WB_CU((run_panel_small<64, 128, false>(pi, none, none, sp)));
         pe(h->prof_panel, sp, 0.0);
-        pb(h->prof_gemm, sp);
-        WB_CU(run_gemm(L.maps, L.cmap, k1, k1, 0, m, w, kNB, h->d_err, sp));
-        pe(h->prof_gemm, sp, gemm_flop(m, w, kNB));
         h->launches += 2;
       }
       WB_CU(cudaGetLastError());
@@ -1400,13 +1529,13 @@ int factor_mixed(wbem_context* h) {
         // A_kj -= L_k,[p0,k0) U_[p0,k0),j for the columns right of the panel
         const PanelArgs pu{A + (size_t)k0 * ld + p0, ld, A + (size_t)p0 * ld + p1, ld,
                            A + (size_t)k0 * ld + p1, ld, kNB, n, k0 - p0, k0, p1, 1, 0};
-        WB_CU((run_panel_tile<128, 64, false>(pu, none, none, sp)));
+        WB_CU((run_panel_small<128, 64, false>(pu, none, none, sp)));
         h->launches++;
       }
       const SplitOut U12{b2 + 2 * rows * kNB2, b2 + 3 * rows * kNB2, p1, kNB2, k0 - p0};
       const PanelArgs pr{L.linvT + bo, kNB, A + (size_t)k0 * ld + p1, ld, A + (size_t)k0 * ld + p1,
                          ld, kNB, n, kNB, k0, p1, 0, 1};
-      WB_CU((run_panel_tile<128, 64, true>(pr, U12, none, sp)));
+      WB_CU((run_panel_small<128, 64, true>(pr, U12, none, sp)));
       pe(h->prof_panel, sp, 0.0);
       h->launches++;
       WB_CU(cudaGetLastError());
