@@ -39,7 +39,7 @@ namespace wbem {
 
 constexpr int kNB = 128;   // inner LU block size (diagonal blocks, panels)
 constexpr int kNB2 = 512;  // outer block: K of the tensor-core trailing update
-constexpr int kLookaheadSMs = 1;  // SMs the bulk trailing update leaves to the panel work
+constexpr int kLookaheadSMs = 4;  // SMs the bulk trailing update leaves to the panel work
 
 // ------------------------------------------------------------------ input
 // LU input: hi part of the system operator, alpha on Neumann diagonals,
@@ -1550,8 +1550,9 @@ int factor_mixed(wbem_context* h) {
     if (p2 < N) {
       WB_CU(cudaEventRecord(L.ev_row, sp));
       WB_CU(cudaStreamWaitEvent(st, L.ev_row, 0));
-      // one SM stays free, so the next panel's first diagonal block (one
-      // CTA) and the start of its column panel run beside this update
+      // a few SMs stay free for the next panel's diagonal blocks (one
+      // 198 KB CTA each); its panel kernels (13 KB CTAs) run beside this
+      // update's CTAs on every SM
       pb(h->prof_gemm, st);
       WB_CU(run_gemm(L.maps2[buf], L.cmap, p1, p2, p2 - p1, n, N - p2, p1 - p0, h->d_err, st,
                      prof ? 0 : kLookaheadSMs));
