@@ -11,20 +11,20 @@
 // term on Dirichlet columns) dominates, and every pivot is checked (zero or
 // non-finite -> WBEM_ERR_SINGULAR).
 //
-// Step k (block size kNB = 128):
+// Step k (block size kNB = 128), inside outer panels of kNB2 = 512 columns:
 //   1. k_diag_block: LU of A_kk in shared memory, plus the inverses of its
 //      unit-lower and upper factors;
-//   2. k_panel_sgemm: U_kj = inv(L_kk) A_kj and L_ik = A_ik inv(U_kk) (FP32 SIMT),
-//      also writing the BF16 hi/lo splits of both panels (K-major);
-//   3. k_gemm_bf16x3: A_ij -= L_ik U_kj as Lhi Uhi + Lhi Ulo + Llo Uhi with
-//      FP32 accumulation in TMEM (128 x 128 tile per CTA, K in 64-wide TMA
-//      stages with 128B swizzle, C staged through shared memory by TMA).
-// The steps are grouped in outer panels of kNB2 = 512 columns: inside a
-// panel the trailing updates cover the panel's own columns only (K = 128);
-// the rest of the matrix gets one K = 512 update per outer panel, split
-// between the next panel's columns (high-priority stream) and the remainder
-// (low-priority stream), so the next panel's factorisation overlaps the bulk
-// of the update (look-ahead).
+//   2. k_panel_small: L_ik = A_ik inv(U_kk) and U_kj = inv(L_kk) A_kj (FP32
+//      SIMT), the column panel also writing the BF16 hi/lo split of L21;
+//      then the panel's own trailing update A_ij -= L_ik U_kj (FP32, K = 128).
+// Per outer panel P: U12 = inv(L11) A12 for the rest of its rows (FP32, with
+// the earlier blocks' updates first), then the bulk trailing update
+// A22 -= L21 U12 on the tensor cores, k_gemm_bf16x3: Lhi Uhi + Lhi Ulo +
+// Llo Uhi with FP32 accumulation in TMEM, K = 512, persistent 128 x 256
+// tiles. It is split between the next panel's columns (high-priority stream)
+// and the remainder (low-priority stream). The panel kernels have a 13 KB
+// footprint, so the next panel's chain runs beside the remainder's CTAs on
+// every SM (look-ahead); a few SMs stay free for the 198 KB diagonal blocks.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -1254,7 +1254,6 @@ struct LuState {
   float* uinv = nullptr;
   float* linvT = nullptr;  // column-major copies
   float* uinvT = nullptr;
-  uint16_t* split = nullptr;  // inner (K = 128) Lhi, Llo, Uhi, Ulo: each (N + kSplitPad) x kNB
   // outer (K = kNB2) L21hi, L21lo, U12Thi, U12Tlo, two sets: the trailing
   // update of outer panel P reads set P % 2 while panel P + 1 writes the other
   uint16_t* split2[2] = {nullptr, nullptr};
@@ -1271,7 +1270,6 @@ struct LuState {
   int N = 0;
   int ld = 0;       // leading dimension of the LU buffer (N rounded up to 32)
   CUtensorMap cmap; // the LU buffer as the GEMM's C operand
-  GemmMaps maps;
 };
 
 static LuState& lu_state(wbem_context* h) {
@@ -1286,7 +1284,6 @@ void free_lu(wbem_context* h) {
   if (L.uinv) cudaFree(L.uinv);
   if (L.linvT) cudaFree(L.linvT);
   if (L.uinvT) cudaFree(L.uinvT);
-  if (L.split) cudaFree(L.split);
   for (int b = 0; b < 2; ++b)
     if (L.split2[b]) cudaFree(L.split2[b]);
   if (L.s_panel) cudaStreamDestroy(L.s_panel);
@@ -1415,17 +1412,12 @@ int factor_mixed(wbem_context* h) {
     WB_CHK(dev_alloc(h, &L.uinv, (size_t)nblk * kNB * kNB));
     WB_CHK(dev_alloc(h, &L.linvT, (size_t)nblk * kNB * kNB));
     WB_CHK(dev_alloc(h, &L.uinvT, (size_t)nblk * kNB * kNB));
-    WB_CHK(dev_alloc(h, &L.split, (size_t)4 * rows * kNB));
     WB_CHK(dev_alloc(h, &L.split2[0], (size_t)4 * rows * kNB2));
     WB_CHK(dev_alloc(h, &L.split2[1], (size_t)4 * rows * kNB2));
     WB_CHK(dev_alloc(h, &L.w, (size_t)2 * N));
     WB_CHK(dev_alloc(h, &L.flags, (size_t)4 * nblk));
     WB_CU(cudaMemsetAsync(L.flags, 0, sizeof(unsigned) * 4 * nblk, h->stream));
-    WB_CU(cudaMemsetAsync(L.split, 0, sizeof(uint16_t) * 4 * rows * kNB, h->stream));
     L.epoch = 0;
-    uint16_t* b1 = L.split;
-    if (!encode_split3(&L.maps, b1, rows, kNB))
-      return fail(h, WBEM_ERR_CUDA, "cuTensorMapEncodeTiled failed");
     for (int b = 0; b < 2; ++b) {
       uint16_t* b2 = L.split2[b];
       WB_CU(cudaMemsetAsync(b2, 0, sizeof(uint16_t) * 4 * rows * kNB2, h->stream));
@@ -1440,7 +1432,6 @@ int factor_mixed(wbem_context* h) {
     for (cudaEvent_t* e : {&L.ev_fork, &L.ev_row, &L.ev_trail, &L.ev_join})
       WB_CU(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
   }
-  uint16_t* b1 = L.split;
   EvTimer tm(h->stream);
   float* A = h->d_lu;
   const SplitOut none{nullptr, nullptr, 0, 0, 0};
