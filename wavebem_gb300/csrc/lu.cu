@@ -351,6 +351,128 @@ __global__ void __launch_bounds__(kDiagThreads, 1)
   }
 }
 
+// The same outputs by a register-resident unblocked elimination with one
+// CTA barrier per pivot and every thread busy at every pivot. Thread (r, q)
+// holds 32 entries of row r (columns 32q .. 32q+31) in registers:
+//   * while r > k (row below the pivot) the combined row of the LU: the
+//     working matrix right of the pivot, the row of inv(L) left of it (both
+//     obey w_r -= l_rk * w_k), the pivot slot turning from a_rk into -l_rk;
+//   * from r = k on, the row of Z = inv(U1), U = D U1 (D = diag(U)): the
+//     column operations z_rj -= (u_kj / u_kk) z_rk, j > k, that take U to D.
+// Each finished row is published to a row history in shared memory (U and
+// inv(L) are read from it at the end), each column of Z to the upper
+// triangle of the L array when it is final (later steps may leave garbage in
+// register slots j <= k of a Z row, none of which is read again), and
+// inv(U) = Z D^-1. The pivot loop is unrolled by 32 so every register slot is
+// a compile-time index. Warp w takes row group g and column block q with
+// g + q = w (mod 4): each scheduler (w mod 4) holds one warp of every row
+// group and every column block, so the publishing row and the pivot column
+// land on different schedulers.
+constexpr int kDRowLD = 132;  // row history: 16-byte rows
+constexpr size_t kDiagSmemBytes = ((size_t)kNB * kDLD + (size_t)kNB * kDRowLD + 2 * kNB + kNB) * sizeof(float);
+
+__global__ void __launch_bounds__(kDiagThreads, 1)
+    k_diag_block2(int ld, int k0, int nb, float* __restrict__ A, float* __restrict__ linv,
+                  float* __restrict__ uinv, float* __restrict__ linvT, float* __restrict__ uinvT,
+                  DevErr* err) {
+  extern __shared__ __align__(16) float dsm[];
+  float* sLZ = dsm;                       // [128][129]: input; then L (strict lower), Z (upper)
+  float* sRows = sLZ + kNB * kDLD;        // [128][132]: row history (inv(L) | U)
+  float* sCol = sRows + kNB * kDRowLD;    // [2][128] pivot column of the rows below
+  float* sInv = sCol + 2 * kNB;           // [128] 1 / u_kk
+  __shared__ int bad;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int q = warp >> 2, g = ((warp & 3) - q) & 3;
+  const int r = 32 * g + lane, c0 = 32 * q;
+  for (int idx = tid; idx < kNB * kNB; idx += kDiagThreads) {
+    const int rr = idx >> 7, cc = idx & 127;
+    float* dst = sLZ + rr * kDLD + cc;
+    if (rr < nb && cc < nb)
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+                   "l"(A + (size_t)(k0 + rr) * ld + k0 + cc));
+    else
+      *dst = rr == cc ? 1.f : 0.f;
+  }
+  asm volatile("cp.async.commit_group;\n cp.async.wait_group 0;" ::: "memory");
+  if (tid == 0) bad = 0;
+  __syncthreads();
+  float w[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) w[i] = sLZ[r * kDLD + c0 + i];  // lanes are rows: distinct banks
+  __syncthreads();
+  // publish row 0 and column 0; row 0 continues as a Z row
+  if (r == 0) {
+#pragma unroll
+    for (int i = 0; i < 32; i += 4)
+      *reinterpret_cast<float4*>(sRows + c0 + i) = make_float4(w[i], w[i + 1], w[i + 2], w[i + 3]);
+    if (q == 0) {
+      const float p = w[0];
+      if (!(fabsf(p) > 0.f && isfinite(p))) bad = 1;
+      sInv[0] = __frcp_rn(p);
+      sLZ[0] = 1.f;
+    }
+#pragma unroll
+    for (int i = 0; i < 32; ++i) w[i] = 0.f;
+  }
+  if (q == 0 && r > 0) sCol[r] = w[0];
+  __syncthreads();
+#pragma unroll 1
+  for (int kb = 0; kb < 4; ++kb) {
+#pragma unroll
+    for (int s = 0; s < 32; ++s) {
+      if (s == 31 && kb == 3) break;  // the last pivot has nothing below it
+      const int k = 32 * kb + s, k1 = k + 1;
+      const int s1 = (s + 1) & 31, kb1 = kb + (s == 31 ? 1 : 0);
+      const float* row = sRows + k * kDRowLD;
+      const float src = r > k ? sCol[(s & 1) * kNB + r] : sLZ[r * kDLD + k];
+      const float m = src * sInv[k];
+#pragma unroll
+      for (int i = 0; i < 32; i += 4) {
+        const float4 v = *reinterpret_cast<const float4*>(row + c0 + i);  // broadcast
+        w[i] = __fmaf_rn(-m, v.x, w[i]);
+        w[i + 1] = __fmaf_rn(-m, v.y, w[i + 1]);
+        w[i + 2] = __fmaf_rn(-m, v.z, w[i + 2]);
+        w[i + 3] = __fmaf_rn(-m, v.w, w[i + 3]);
+      }
+      if (q == kb && r > k) {  // pivot slot of a row below: -l_rk; L keeps l_rk
+        w[s] = -m;
+        sLZ[r * kDLD + k] = m;
+      }
+      if (r == k1) {  // row k+1 is final: publish it, continue as a Z row
+        float* nrow = sRows + k1 * kDRowLD;
+#pragma unroll
+        for (int i = 0; i < 32; i += 4)
+          *reinterpret_cast<float4*>(nrow + c0 + i) = make_float4(w[i], w[i + 1], w[i + 2], w[i + 3]);
+        if (q == kb1) {
+          const float p = w[s1];
+          if (!(fabsf(p) > 0.f && isfinite(p))) bad = 1;
+          sInv[k1] = __frcp_rn(p);
+          sLZ[k1 * kDLD + k1] = 1.f;  // z_kk
+        }
+#pragma unroll
+        for (int i = 0; i < 32; ++i) w[i] = 0.f;
+      } else if (q == kb1) {  // column k+1: multipliers below, final Z column above
+        if (r > k1) sCol[((s + 1) & 1) * kNB + r] = w[s1];
+        else sLZ[r * kDLD + k1] = w[s1];
+      }
+      __syncthreads();
+    }
+  }
+  if (bad) {
+    if (tid == 0) dev_fail(err, WBEM_ERR_SINGULAR, 51, k0, 0);
+    return;  // uniform
+  }
+  for (int idx = tid; idx < kNB * kNB; idx += kDiagThreads) {
+    const int rr = idx >> 7, cc = idx & 127;
+    const float rowv = sRows[rr * kDRowLD + cc];
+    if (rr < nb && cc < nb) A[(size_t)(k0 + rr) * ld + k0 + cc] = cc < rr ? sLZ[rr * kDLD + cc] : rowv;
+    linv[idx] = cc < rr ? rowv : (cc == rr ? 1.f : 0.f);
+    linvT[idx] = rr < cc ? sRows[cc * kDRowLD + rr] : (cc == rr ? 1.f : 0.f);
+    uinv[idx] = rr <= cc ? sLZ[rr * kDLD + cc] * sInv[cc] : 0.f;
+    uinvT[idx] = cc <= rr ? sLZ[cc * kDLD + rr] * sInv[rr] : 0.f;
+  }
+}
+
 // ------------------------------------------------------------- panel GEMM
 // BF16 hi/lo split of an FP32 value: hi = bf16(v), lo = bf16(v - hi).
 __device__ __forceinline__ void split_bf16(float v, uint16_t* hi, uint16_t* lo) {
@@ -737,7 +859,7 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int 
 }
 
 // ------------------------------------------------- persistent tcgen05 GEMM
-// C[crow0 + m, ccol0 + n] -= sum_k A[m, k] B[brow0 + n, k], BF16x3, for the
+// C[crow0 + m, ccol0 + n] -= sum_k A[arow0 + m, k] B[brow0 + n, k], BF16x3, for the
 // large trailing updates. Persistent CTAs (one per SM) walk 128 x 256 output
 // tiles (M fastest, so the CTAs in flight share B tiles and stream A); warp
 // roles:
@@ -789,8 +911,8 @@ __device__ __forceinline__ bool named_bar_epi_or(int g, bool v) {
 __global__ void __launch_bounds__(kG3Threads, 1)
     k_gemm_bf16x3(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
             const __grid_constant__ CUtensorMap mBhi, const __grid_constant__ CUtensorMap mBlo,
-            const __grid_constant__ CUtensorMap mC, int crow0, int ccol0, int brow0, int M, int Nc,
-            int K, DevErr* err) {
+            const __grid_constant__ CUtensorMap mC, int crow0, int ccol0, int arow0, int brow0, int M,
+            int Nc, int K, DevErr* err) {
   extern __shared__ __align__(1024) uint8_t g3sm[];
   const uint32_t base_s = smem_u32(g3sm);
   const uint32_t pad = (1024 - (base_s & 1023)) & 1023;
@@ -849,8 +971,8 @@ __global__ void __launch_bounds__(kG3Threads, 1)
           }
           const uint32_t st = smem_u32(sm + (size_t)stage * kStage3);
           mbar_arrive_expect_tx(&full[stage], kStage3);
-          tma_load_2d(st, &mAhi, kb * G3K, m0, &full[stage]);
-          tma_load_2d(st + kA3, &mAlo, kb * G3K, m0, &full[stage]);
+          tma_load_2d(st, &mAhi, kb * G3K, arow0 + m0, &full[stage]);
+          tma_load_2d(st + kA3, &mAlo, kb * G3K, arow0 + m0, &full[stage]);
           tma_load_2d(st + 2 * kA3, &mBhi, kb * G3K, brow0 + n0, &full[stage]);
           tma_load_2d(st + 2 * kA3 + kB3, &mBlo, kb * G3K, brow0 + n0, &full[stage]);
           if (++stage == G3S) {
@@ -1074,13 +1196,14 @@ static bool encode_cmap(CUtensorMap* map, const float* base, int rows, int cols,
 
 // C[crow0 + (0..M), ccol0 + (0..Nc)] -= A B^T, with A rows in (Ahi, Alo)
 // [rowsA x K] and B rows in (Bhi, Blo) [rowsB x K], both K-major BF16; C
-// column ccol0 + j pairs with B row brow0 + j. C is
+// row crow0 + i pairs with A row arow0 + i, C column ccol0 + j with B row
+// brow0 + j. C is
 // addressed through its tensor map; rows and columns past the map's extent are
 // neither read (zero fill) nor written (clipped), so tiles may overhang M / Nc
 // only where the region ends at the matrix edge.
 // spare_sms: SMs left free of the persistent CTAs (for concurrent panel work)
 static cudaError_t run_gemm(const GemmMaps& mp, const CUtensorMap& cmap, int crow0, int ccol0,
-                             int brow0, int M, int Nc, int K, DevErr* err, cudaStream_t s,
+                             int arow0, int brow0, int M, int Nc, int K, DevErr* err, cudaStream_t s,
                              int spare_sms = 0) {
   static bool attr = false;
   static int sms = 0;
@@ -1098,7 +1221,7 @@ static cudaError_t run_gemm(const GemmMaps& mp, const CUtensorMap& cmap, int cro
   const int ntiles = ((M + G3M - 1) / G3M) * ((Nc + G3N - 1) / G3N);
   const int grid = std::min(ntiles, std::max(1, sms - spare_sms));
   k_gemm_bf16x3<<<grid, kG3Threads, gemm_smem(), s>>>(mp.Ahi, mp.Alo, mp.Bhi, mp.Blo, cmap, crow0, ccol0,
-                                                 brow0, M, Nc, K, err);
+                                                 arow0, brow0, M, Nc, K, err);
   return cudaGetLastError();
 }
 
@@ -1264,6 +1387,7 @@ struct LuState {
   cudaStream_t s_panel = nullptr;
   cudaStream_t s_trail = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_row = nullptr, ev_trail = nullptr, ev_join = nullptr;
+  cudaEvent_t ev_next_rows = nullptr;  // bulk update of the next panel's rows done
   float* w = nullptr;         // 2 x N ping-pong vectors
   unsigned* flags = nullptr;  // 4 x nblk publication flags
   unsigned epoch = 0;
@@ -1288,7 +1412,7 @@ void free_lu(wbem_context* h) {
     if (L.split2[b]) cudaFree(L.split2[b]);
   if (L.s_panel) cudaStreamDestroy(L.s_panel);
   if (L.s_trail) cudaStreamDestroy(L.s_trail);
-  for (cudaEvent_t e : {L.ev_fork, L.ev_row, L.ev_trail, L.ev_join})
+  for (cudaEvent_t e : {L.ev_fork, L.ev_row, L.ev_trail, L.ev_join, L.ev_next_rows})
     if (e) cudaEventDestroy(e);
   if (L.w) cudaFree(L.w);
   if (L.flags) cudaFree(L.flags);
@@ -1429,14 +1553,14 @@ int factor_mixed(wbem_context* h) {
     WB_CU(cudaDeviceGetStreamPriorityRange(&lo, &hi));
     WB_CU(cudaStreamCreateWithPriority(&L.s_panel, cudaStreamNonBlocking, hi));
     WB_CU(cudaStreamCreateWithPriority(&L.s_trail, cudaStreamNonBlocking, lo));
-    for (cudaEvent_t* e : {&L.ev_fork, &L.ev_row, &L.ev_trail, &L.ev_join})
+    for (cudaEvent_t* e : {&L.ev_fork, &L.ev_row, &L.ev_trail, &L.ev_join, &L.ev_next_rows})
       WB_CU(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
   }
   EvTimer tm(h->stream);
   float* A = h->d_lu;
   const SplitOut none{nullptr, nullptr, 0, 0, 0};
-  const size_t kDiagSmem = (size_t)3 * kNB * kDLD * sizeof(float);
-  WB_CU(cudaFuncSetAttribute(k_diag_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDiagSmem));
+  const size_t kDiagSmem = kDiagSmemBytes;
+  WB_CU(cudaFuncSetAttribute(k_diag_block2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDiagSmem));
   // Right-looking LU over outer panels P = [p0, p1) of kNB2 columns, with
   // look-ahead. On s_panel: the column work of P (diagonal blocks, column
   // panels, inner updates; it touches columns [p0, p1) only), then U12 of P
@@ -1475,8 +1599,8 @@ int factor_mixed(wbem_context* h) {
       const int k = k0 / kNB, nb = std::min(kNB, N - k0), k1 = k0 + nb;
       const size_t bo = (size_t)k * kNB * kNB;
       pb(h->prof_diag, sp);
-      k_diag_block<<<1, kDiagThreads, kDiagSmem, sp>>>(ld, k0, nb, A, L.linv + bo, L.uinv + bo,
-                                                       L.linvT + bo, L.uinvT + bo, h->d_err);
+      k_diag_block2<<<1, kDiagThreads, kDiagSmem, sp>>>(ld, k0, nb, A, L.linv + bo, L.uinv + bo,
+                                                        L.linvT + bo, L.uinvT + bo, h->d_err);
       pe(h->prof_diag, sp, 0.0);
       h->launches++;
       if (k1 >= N) break;
@@ -1509,8 +1633,9 @@ int factor_mixed(wbem_context* h) {
     }
     if (p1 >= N) break;
     // ---- row panel U12 = inv(L11) A12, one 128-block row at a time, after
-    // the previous trailing update has finished with these rows
-    if (trail_pending) WB_CU(cudaStreamWaitEvent(sp, L.ev_trail, 0));
+    // the previous trailing update has finished with these rows (its first
+    // part; the rest of it runs on beside this row panel)
+    if (trail_pending) WB_CU(cudaStreamWaitEvent(sp, L.ev_next_rows, 0));
     const int n = N - p1;
     for (int k0 = p0; k0 < p1; k0 += kNB) {
       const int k = k0 / kNB;
@@ -1534,20 +1659,29 @@ int factor_mixed(wbem_context* h) {
     // ---- trailing update A22 -= L21 U12 on the tensor cores (K = kNB2):
     // the next panel's columns on s_panel, the rest on s_trail
     const int p2 = std::min(N, p1 + kNB2);
+    if (trail_pending) WB_CU(cudaStreamWaitEvent(sp, L.ev_trail, 0));
     pb(h->prof_gemm, sp);
-    WB_CU(run_gemm(L.maps2[buf], L.cmap, p1, p1, 0, n, p2 - p1, p1 - p0, h->d_err, sp));
+    WB_CU(run_gemm(L.maps2[buf], L.cmap, p1, p1, 0, 0, n, p2 - p1, p1 - p0, h->d_err, sp));
     pe(h->prof_gemm, sp, gemm_flop(n, p2 - p1, p1 - p0));
     h->launches++;
     if (p2 < N) {
       WB_CU(cudaEventRecord(L.ev_row, sp));
       WB_CU(cudaStreamWaitEvent(st, L.ev_row, 0));
       // a few SMs stay free for the next panel's diagonal blocks (one
-      // 198 KB CTA each); its panel kernels (13 KB CTAs) run beside this
-      // update's CTAs on every SM
+      // 200 KB CTA each); its panel kernels (13 KB CTAs) run beside this
+      // update's CTAs on every SM. The next panel's rows [p1, p2) go first,
+      // so that its row panel can start while the rows below are updated.
+      const int spare = prof ? 0 : kLookaheadSMs;
       pb(h->prof_gemm, st);
-      WB_CU(run_gemm(L.maps2[buf], L.cmap, p1, p2, p2 - p1, n, N - p2, p1 - p0, h->d_err, st,
-                     prof ? 0 : kLookaheadSMs));
-      pe(h->prof_gemm, st, gemm_flop(n, N - p2, p1 - p0));
+      WB_CU(run_gemm(L.maps2[buf], L.cmap, p1, p2, 0, p2 - p1, p2 - p1, N - p2, p1 - p0, h->d_err, st,
+                     spare));
+      pe(h->prof_gemm, st, gemm_flop(p2 - p1, N - p2, p1 - p0));
+      WB_CU(cudaEventRecord(L.ev_next_rows, st));
+      pb(h->prof_gemm, st);
+      WB_CU(run_gemm(L.maps2[buf], L.cmap, p2, p2, p2 - p1, p2 - p1, N - p2, N - p2, p1 - p0, h->d_err,
+                     st, spare));
+      pe(h->prof_gemm, st, gemm_flop(N - p2, N - p2, p1 - p0));
+      h->launches++;
       WB_CU(cudaEventRecord(L.ev_trail, st));
       trail_pending = true;
       h->launches++;
@@ -1630,7 +1764,7 @@ extern "C" int wbem_test_gemm_bf16x3(int M, int Nc, int K, const float* dA, cons
   if (st == WBEM_OK && cudaMalloc(&err, sizeof(DevErr)) != cudaSuccess) st = WBEM_ERR_NOMEM;
   if (st == WBEM_OK) {
     cudaMemset(err, 0, sizeof(DevErr));
-    if (run_gemm(mp, cmap, 0, 0, 0, M, Nc, K, err, 0) != cudaSuccess) st = WBEM_ERR_CUDA;
+    if (run_gemm(mp, cmap, 0, 0, 0, 0, M, Nc, K, err, 0) != cudaSuccess) st = WBEM_ERR_CUDA;
     if (cudaDeviceSynchronize() != cudaSuccess) st = WBEM_ERR_CUDA;
     DevErr de{};
     cudaMemcpy(&de, err, sizeof de, cudaMemcpyDeviceToHost);
