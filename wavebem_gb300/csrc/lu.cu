@@ -1381,13 +1381,16 @@ struct LuState {
   // update of outer panel P reads set P % 2 while panel P + 1 writes the other
   uint16_t* split2[2] = {nullptr, nullptr};
   GemmMaps maps2[2];
-  // look-ahead: panel work and the next panel's columns of the trailing update
-  // on a high-priority stream, the rest of the trailing update on a
-  // low-priority one
+  // look-ahead: column work and the next panel's columns of the trailing
+  // update on a high-priority stream, the row panel one block behind it on a
+  // second one, the rest of the trailing update on a low-priority stream
   cudaStream_t s_panel = nullptr;
+  cudaStream_t s_row = nullptr;
   cudaStream_t s_trail = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_row = nullptr, ev_trail = nullptr, ev_join = nullptr;
   cudaEvent_t ev_next_rows = nullptr;  // bulk update of the next panel's rows done
+  cudaEvent_t ev_blk = nullptr;        // diagonal block ready for its row panel
+  cudaEvent_t ev_u12 = nullptr;        // row panel of the outer panel done
   float* w = nullptr;         // 2 x N ping-pong vectors
   unsigned* flags = nullptr;  // 4 x nblk publication flags
   unsigned epoch = 0;
@@ -1412,7 +1415,8 @@ void free_lu(wbem_context* h) {
     if (L.split2[b]) cudaFree(L.split2[b]);
   if (L.s_panel) cudaStreamDestroy(L.s_panel);
   if (L.s_trail) cudaStreamDestroy(L.s_trail);
-  for (cudaEvent_t e : {L.ev_fork, L.ev_row, L.ev_trail, L.ev_join, L.ev_next_rows})
+  if (L.s_row) cudaStreamDestroy(L.s_row);
+  for (cudaEvent_t e : {L.ev_fork, L.ev_row, L.ev_trail, L.ev_join, L.ev_next_rows, L.ev_blk, L.ev_u12})
     if (e) cudaEventDestroy(e);
   if (L.w) cudaFree(L.w);
   if (L.flags) cudaFree(L.flags);
@@ -1553,7 +1557,9 @@ int factor_mixed(wbem_context* h) {
     WB_CU(cudaDeviceGetStreamPriorityRange(&lo, &hi));
     WB_CU(cudaStreamCreateWithPriority(&L.s_panel, cudaStreamNonBlocking, hi));
     WB_CU(cudaStreamCreateWithPriority(&L.s_trail, cudaStreamNonBlocking, lo));
-    for (cudaEvent_t* e : {&L.ev_fork, &L.ev_row, &L.ev_trail, &L.ev_join, &L.ev_next_rows})
+    WB_CU(cudaStreamCreateWithPriority(&L.s_row, cudaStreamNonBlocking, hi < lo ? hi + 1 : hi));
+    for (cudaEvent_t* e : {&L.ev_fork, &L.ev_row, &L.ev_trail, &L.ev_join, &L.ev_next_rows, &L.ev_blk,
+                           &L.ev_u12})
       WB_CU(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
   }
   EvTimer tm(h->stream);
@@ -1562,16 +1568,23 @@ int factor_mixed(wbem_context* h) {
   const size_t kDiagSmem = kDiagSmemBytes;
   WB_CU(cudaFuncSetAttribute(k_diag_block2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDiagSmem));
   // Right-looking LU over outer panels P = [p0, p1) of kNB2 columns, with
-  // look-ahead. On s_panel: the column work of P (diagonal blocks, column
-  // panels, inner updates; it touches columns [p0, p1) only), then U12 of P
-  // (rows [p0, p1), columns [p1, N)), then the trailing update of P's
-  // successor's columns [p1, p2). On s_trail: the trailing update of the
-  // remaining columns [p2, N), which overlaps the column work of P + 1.
-  // Ordering: U12 of P waits for the trailing update of P - 1 (same rows);
-  // the trailing update of P on s_trail waits for U12 of P.
+  // look-ahead.
+  //   s_panel: the column work of P (diagonal blocks, column panels, inner
+  //     updates; columns [p0, p1) only), then the trailing update of the next
+  //     panel's columns [p1, p2).
+  //   s_row: the row panel U12 of P (rows [p0, p1), columns [p1, N)), block
+  //     row k as soon as diagonal block k is factored, beside the column work.
+  //   s_trail: the trailing update of the columns [p2, N): first the next
+  //     panel's rows [p1, p2), then the rows below, beside the column work
+  //     of P + 1.
+  // Ordering: the row panel of P waits for the first part of the trailing
+  // update of P - 1 (its rows), the update of the next panel's columns for
+  // the row panel of P and all of the trailing update of P - 1; the trailing
+  // update of P waits for the update of the next panel's columns.
   // profiling: one stream, each launch bracketed by events
   const bool prof = h->profiling;
   cudaStream_t sp = prof ? h->stream : L.s_panel, st = prof ? h->stream : L.s_trail;
+  cudaStream_t su = prof ? h->stream : L.s_row;
   if (prof) {
     h->prof_gemm.reset();
     h->prof_diag.reset();
@@ -1589,12 +1602,13 @@ int factor_mixed(wbem_context* h) {
   WB_CU(cudaEventRecord(L.ev_fork, h->stream));
   WB_CU(cudaStreamWaitEvent(sp, L.ev_fork, 0));
   WB_CU(cudaStreamWaitEvent(st, L.ev_fork, 0));
+  WB_CU(cudaStreamWaitEvent(su, L.ev_fork, 0));
   bool trail_pending = false;  // a trailing update was queued on s_trail
   for (int p0 = 0; p0 < N; p0 += kNB2) {
     const int p1 = std::min(N, p0 + kNB2);
     const int buf = (p0 / kNB2) & 1;
     uint16_t* b2 = L.split2[buf];
-    // ---- column work of the panel: 128-wide blocks, right-looking
+    const int n = N - p1;
     for (int k0 = p0; k0 < p1; k0 += kNB) {
       const int k = k0 / kNB, nb = std::min(kNB, N - k0), k1 = k0 + nb;
       const size_t bo = (size_t)k * kNB * kNB;
@@ -1603,6 +1617,27 @@ int factor_mixed(wbem_context* h) {
                                                         L.linvT + bo, L.uinvT + bo, h->d_err);
       pe(h->prof_diag, sp, 0.0);
       h->launches++;
+      if (p1 < N) {
+        // ---- row panel block row k: A_kj -= L_k,[p0,k0) U_[p0,k0),j, then
+        // U_kj = inv(L_kk) A_kj, for the columns right of the panel. L_k,[p0,k0)
+        // comes from the column panels already queued on s_panel.
+        WB_CU(cudaEventRecord(L.ev_blk, sp));
+        WB_CU(cudaStreamWaitEvent(su, L.ev_blk, 0));
+        if (k0 == p0 && trail_pending) WB_CU(cudaStreamWaitEvent(su, L.ev_next_rows, 0));
+        pb(h->prof_panel, su);
+        if (k0 > p0) {
+          const PanelArgs pu{A + (size_t)k0 * ld + p0, ld, A + (size_t)p0 * ld + p1, ld,
+                             A + (size_t)k0 * ld + p1, ld, kNB, n, k0 - p0, k0, p1, 1, 0};
+          WB_CU((run_panel_small<128, 64, false>(pu, none, none, su)));
+          h->launches++;
+        }
+        const SplitOut U12{b2 + 2 * rows * kNB2, b2 + 3 * rows * kNB2, p1, kNB2, k0 - p0};
+        const PanelArgs pr{L.linvT + bo, kNB, A + (size_t)k0 * ld + p1, ld, A + (size_t)k0 * ld + p1,
+                           ld, kNB, n, kNB, k0, p1, 0, 1};
+        WB_CU((run_panel_small<128, 64, true>(pr, U12, none, su)));
+        pe(h->prof_panel, su, 0.0);
+        h->launches++;
+      }
       if (k1 >= N) break;
       const int m = N - k1;
       const SplitOut L21{b2, b2 + rows * kNB2, p1, kNB2, k0 - p0};
@@ -1632,33 +1667,11 @@ int factor_mixed(wbem_context* h) {
       WB_CU(cudaGetLastError());
     }
     if (p1 >= N) break;
-    // ---- row panel U12 = inv(L11) A12, one 128-block row at a time, after
-    // the previous trailing update has finished with these rows (its first
-    // part; the rest of it runs on beside this row panel)
-    if (trail_pending) WB_CU(cudaStreamWaitEvent(sp, L.ev_next_rows, 0));
-    const int n = N - p1;
-    for (int k0 = p0; k0 < p1; k0 += kNB) {
-      const int k = k0 / kNB;
-      const size_t bo = (size_t)k * kNB * kNB;
-      pb(h->prof_panel, sp);
-      if (k0 > p0) {
-        // A_kj -= L_k,[p0,k0) U_[p0,k0),j for the columns right of the panel
-        const PanelArgs pu{A + (size_t)k0 * ld + p0, ld, A + (size_t)p0 * ld + p1, ld,
-                           A + (size_t)k0 * ld + p1, ld, kNB, n, k0 - p0, k0, p1, 1, 0};
-        WB_CU((run_panel_small<128, 64, false>(pu, none, none, sp)));
-        h->launches++;
-      }
-      const SplitOut U12{b2 + 2 * rows * kNB2, b2 + 3 * rows * kNB2, p1, kNB2, k0 - p0};
-      const PanelArgs pr{L.linvT + bo, kNB, A + (size_t)k0 * ld + p1, ld, A + (size_t)k0 * ld + p1,
-                         ld, kNB, n, kNB, k0, p1, 0, 1};
-      WB_CU((run_panel_small<128, 64, true>(pr, U12, none, sp)));
-      pe(h->prof_panel, sp, 0.0);
-      h->launches++;
-      WB_CU(cudaGetLastError());
-    }
     // ---- trailing update A22 -= L21 U12 on the tensor cores (K = kNB2):
     // the next panel's columns on s_panel, the rest on s_trail
     const int p2 = std::min(N, p1 + kNB2);
+    WB_CU(cudaEventRecord(L.ev_u12, su));
+    WB_CU(cudaStreamWaitEvent(sp, L.ev_u12, 0));
     if (trail_pending) WB_CU(cudaStreamWaitEvent(sp, L.ev_trail, 0));
     pb(h->prof_gemm, sp);
     WB_CU(run_gemm(L.maps2[buf], L.cmap, p1, p1, 0, 0, n, p2 - p1, p1 - p0, h->d_err, sp));
@@ -1681,13 +1694,14 @@ int factor_mixed(wbem_context* h) {
       WB_CU(run_gemm(L.maps2[buf], L.cmap, p2, p2, p2 - p1, p2 - p1, N - p2, N - p2, p1 - p0, h->d_err,
                      st, spare));
       pe(h->prof_gemm, st, gemm_flop(N - p2, N - p2, p1 - p0));
-      h->launches++;
       WB_CU(cudaEventRecord(L.ev_trail, st));
       trail_pending = true;
-      h->launches++;
+      h->launches += 2;
     }
   }
-  // join both streams back into the handle's stream
+  // join the streams back into the handle's stream
+  WB_CU(cudaEventRecord(L.ev_join, su));
+  WB_CU(cudaStreamWaitEvent(h->stream, L.ev_join, 0));
   WB_CU(cudaEventRecord(L.ev_join, sp));
   WB_CU(cudaStreamWaitEvent(h->stream, L.ev_join, 0));
   WB_CU(cudaEventRecord(L.ev_join, st));
