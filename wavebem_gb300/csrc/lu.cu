@@ -352,8 +352,9 @@ __global__ void __launch_bounds__(kDiagThreads, 1)
 }
 
 // The same outputs by a register-resident unblocked elimination with one
-// CTA barrier per pivot and every thread busy at every pivot. Thread (r, q)
-// holds 32 entries of row r (columns 32q .. 32q+31) in registers:
+// CTA barrier per pivot and every thread busy at every pivot. 1024 threads:
+// thread (r, q) holds 16 entries of row r (columns 16q .. 16q+15) in
+// registers:
 //   * while r > k (row below the pivot) the combined row of the LU: the
 //     working matrix right of the pivot, the row of inv(L) left of it (both
 //     obey w_r -= l_rk * w_k), the pivot slot turning from a_rk into -l_rk;
@@ -363,15 +364,21 @@ __global__ void __launch_bounds__(kDiagThreads, 1)
 // inv(L) are read from it at the end), each column of Z to the upper
 // triangle of the L array when it is final (later steps may leave garbage in
 // register slots j <= k of a Z row, none of which is read again), and
-// inv(U) = Z D^-1. The pivot loop is unrolled by 32 so every register slot is
-// a compile-time index. Warp w takes row group g and column block q with
-// g + q = w (mod 4): each scheduler (w mod 4) holds one warp of every row
-// group and every column block, so the publishing row and the pivot column
-// land on different schedulers.
+// inv(U) = Z D^-1. The pivot loop is unrolled by 16 so every register slot is
+// a compile-time index. Warp w takes column block q = w / 4 and row group g
+// with g + q = w (mod 4): each scheduler (w mod 4) holds two warps of every
+// row group and one of the four warps that own a pivot column.
+constexpr int kDiag2Threads = 1024;
 constexpr int kDRowLD = 132;  // row history: 16-byte rows
 constexpr size_t kDiagSmemBytes = ((size_t)kNB * kDLD + (size_t)kNB * kDRowLD + 2 * kNB + kNB) * sizeof(float);
 
-__global__ void __launch_bounds__(kDiagThreads, 1)
+__device__ __forceinline__ float rcp_approx(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+__global__ void __launch_bounds__(kDiag2Threads, 1)
     k_diag_block2(int ld, int k0, int nb, float* __restrict__ A, float* __restrict__ linv,
                   float* __restrict__ uinv, float* __restrict__ linvT, float* __restrict__ uinvT,
                   DevErr* err) {
@@ -383,8 +390,8 @@ __global__ void __launch_bounds__(kDiagThreads, 1)
   __shared__ int bad;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int q = warp >> 2, g = ((warp & 3) - q) & 3;
-  const int r = 32 * g + lane, c0 = 32 * q;
-  for (int idx = tid; idx < kNB * kNB; idx += kDiagThreads) {
+  const int r = 32 * g + lane, c0 = 16 * q;
+  for (int idx = tid; idx < kNB * kNB; idx += kDiag2Threads) {
     const int rr = idx >> 7, cc = idx & 127;
     float* dst = sLZ + rr * kDLD + cc;
     if (rr < nb && cc < nb)
@@ -396,38 +403,38 @@ __global__ void __launch_bounds__(kDiagThreads, 1)
   asm volatile("cp.async.commit_group;\n cp.async.wait_group 0;" ::: "memory");
   if (tid == 0) bad = 0;
   __syncthreads();
-  float w[32];
+  float w[16];
 #pragma unroll
-  for (int i = 0; i < 32; ++i) w[i] = sLZ[r * kDLD + c0 + i];  // lanes are rows: distinct banks
+  for (int i = 0; i < 16; ++i) w[i] = sLZ[r * kDLD + c0 + i];  // lanes are rows: distinct banks
   __syncthreads();
   // publish row 0 and column 0; row 0 continues as a Z row
   if (r == 0) {
 #pragma unroll
-    for (int i = 0; i < 32; i += 4)
+    for (int i = 0; i < 16; i += 4)
       *reinterpret_cast<float4*>(sRows + c0 + i) = make_float4(w[i], w[i + 1], w[i + 2], w[i + 3]);
     if (q == 0) {
       const float p = w[0];
       if (!(fabsf(p) > 0.f && isfinite(p))) bad = 1;
-      sInv[0] = __frcp_rn(p);
+      sInv[0] = rcp_approx(p);
       sLZ[0] = 1.f;
     }
 #pragma unroll
-    for (int i = 0; i < 32; ++i) w[i] = 0.f;
+    for (int i = 0; i < 16; ++i) w[i] = 0.f;
   }
   if (q == 0 && r > 0) sCol[r] = w[0];
   __syncthreads();
 #pragma unroll 1
-  for (int kb = 0; kb < 4; ++kb) {
+  for (int kb = 0; kb < 8; ++kb) {
 #pragma unroll
-    for (int s = 0; s < 32; ++s) {
-      if (s == 31 && kb == 3) break;  // the last pivot has nothing below it
-      const int k = 32 * kb + s, k1 = k + 1;
-      const int s1 = (s + 1) & 31, kb1 = kb + (s == 31 ? 1 : 0);
+    for (int s = 0; s < 16; ++s) {
+      if (s == 15 && kb == 7) break;  // the last pivot has nothing below it
+      const int k = 16 * kb + s, k1 = k + 1;
+      const int s1 = (s + 1) & 15, kb1 = kb + (s == 15 ? 1 : 0);
       const float* row = sRows + k * kDRowLD;
       const float src = r > k ? sCol[(s & 1) * kNB + r] : sLZ[r * kDLD + k];
       const float m = src * sInv[k];
 #pragma unroll
-      for (int i = 0; i < 32; i += 4) {
+      for (int i = 0; i < 16; i += 4) {
         const float4 v = *reinterpret_cast<const float4*>(row + c0 + i);  // broadcast
         w[i] = __fmaf_rn(-m, v.x, w[i]);
         w[i + 1] = __fmaf_rn(-m, v.y, w[i + 1]);
@@ -438,20 +445,23 @@ __global__ void __launch_bounds__(kDiagThreads, 1)
         w[s] = -m;
         sLZ[r * kDLD + k] = m;
       }
-      if (r == k1) {  // row k+1 is final: publish it, continue as a Z row
-        float* nrow = sRows + k1 * kDRowLD;
+      if (__any_sync(0xffffffffu, r == k1)) {  // warp-uniform: the warp holding row k+1
+        if (r == k1) {  // row k+1 is final: publish it, continue as a Z row
+          float* nrow = sRows + k1 * kDRowLD;
 #pragma unroll
-        for (int i = 0; i < 32; i += 4)
-          *reinterpret_cast<float4*>(nrow + c0 + i) = make_float4(w[i], w[i + 1], w[i + 2], w[i + 3]);
-        if (q == kb1) {
-          const float p = w[s1];
-          if (!(fabsf(p) > 0.f && isfinite(p))) bad = 1;
-          sInv[k1] = __frcp_rn(p);
-          sLZ[k1 * kDLD + k1] = 1.f;  // z_kk
+          for (int i = 0; i < 16; i += 4)
+            *reinterpret_cast<float4*>(nrow + c0 + i) = make_float4(w[i], w[i + 1], w[i + 2], w[i + 3]);
+          if (q == kb1) {
+            const float p = w[s1];
+            if (!(fabsf(p) > 0.f && isfinite(p))) bad = 1;
+            sInv[k1] = rcp_approx(p);
+            sLZ[k1 * kDLD + k1] = 1.f;  // z_kk
+          }
+#pragma unroll
+          for (int i = 0; i < 16; ++i) w[i] = 0.f;
         }
-#pragma unroll
-        for (int i = 0; i < 32; ++i) w[i] = 0.f;
-      } else if (q == kb1) {  // column k+1: multipliers below, final Z column above
+      }
+      if (q == kb1 && r != k1) {  // column k+1: multipliers below, final Z column above
         if (r > k1) sCol[((s + 1) & 1) * kNB + r] = w[s1];
         else sLZ[r * kDLD + k1] = w[s1];
       }
@@ -462,7 +472,7 @@ __global__ void __launch_bounds__(kDiagThreads, 1)
     if (tid == 0) dev_fail(err, WBEM_ERR_SINGULAR, 51, k0, 0);
     return;  // uniform
   }
-  for (int idx = tid; idx < kNB * kNB; idx += kDiagThreads) {
+  for (int idx = tid; idx < kNB * kNB; idx += kDiag2Threads) {
     const int rr = idx >> 7, cc = idx & 127;
     const float rowv = sRows[rr * kDRowLD + cc];
     if (rr < nb && cc < nb) A[(size_t)(k0 + rr) * ld + k0 + cc] = cc < rr ? sLZ[rr * kDLD + cc] : rowv;
@@ -1613,7 +1623,7 @@ int factor_mixed(wbem_context* h) {
       const int k = k0 / kNB, nb = std::min(kNB, N - k0), k1 = k0 + nb;
       const size_t bo = (size_t)k * kNB * kNB;
       pb(h->prof_diag, sp);
-      k_diag_block2<<<1, kDiagThreads, kDiagSmem, sp>>>(ld, k0, nb, A, L.linv + bo, L.uinv + bo,
+      k_diag_block2<<<1, kDiag2Threads, kDiagSmem, sp>>>(ld, k0, nb, A, L.linv + bo, L.uinv + bo,
                                                         L.linvT + bo, L.uinvT + bo, h->d_err);
       pe(h->prof_diag, sp, 0.0);
       h->launches++;
