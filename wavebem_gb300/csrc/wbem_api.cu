@@ -634,7 +634,8 @@ int ensure_vectors(wbem_context* h, int restart) {
   if (!h->d_rhs) CHK(dev_alloc(h, &h->d_rhs, (size_t)N));
   if (!h->d_b) CHK(dev_alloc(h, &h->d_b, (size_t)N));
   if (h->V_cap < restart + 1) {
-    CHK(dev_alloc(h, &h->d_V, (size_t)(restart + 1) * N));
+    // Arnoldi basis V (restart + 1 vectors), then the preconditioned basis Z
+    CHK(dev_alloc(h, &h->d_V, (size_t)(2 * restart + 1) * N));
     h->V_cap = restart + 1;
   }
   return WBEM_OK;
@@ -686,13 +687,19 @@ static int read_scalar(wbem_context* h, const double* d, double* v) {
 // re-orthogonalisation, Givens rotations on the host. prec(z <- M^{-1} v).
 // Stops when the residual norm is <= max(tol, 1e-14 ||rhs||) (absolute
 // tolerance as deal.II's SolverControl, floored at round-off level).
+// Flexible form (right preconditioning with the preconditioned vectors
+// z_k = M^-1 v_k kept): the update x += Z y uses exactly the vectors the
+// Arnoldi relation was built from. The FP32 LU applied in FP32 is not an
+// exactly linear map, so re-applying it to V y (the plain right-preconditioned
+// update) leaves a true residual near the FP32 round-off of x above the
+// estimate and costs a restart cycle; the flexible update does not.
 template <typename Op, typename Prec>
 int gmres(wbem_context* h, const double* rhs, double* x, int restart, int max_steps, double tol,
           Op op, Prec prec, int* iters, double* resid) {
   const int N = h->N;
   double* r = h->d_vec[0];
   double* w = h->d_vec[1];
-  double* z = h->d_vec[2];
+  double* Z = h->d_V + (size_t)h->V_cap * N;  // restart vectors
   double* hbuf = h->d_small;  // [0..restart+1] h, [256..] h2
   double* part = h->d_part;
   double bnorm;
@@ -732,6 +739,7 @@ int gmres(wbem_context* h, const double* rhs, double* x, int restart, int max_st
     for (; k < restart && it < max_steps; ++k) {
       double* vk = h->d_V + (size_t)k * N;
       double* vk1 = h->d_V + (size_t)(k + 1) * N;
+      double* z = Z + (size_t)k * N;
       CHK(prec(vk, z));
       CHK(op(z, w));
       CU(launch_multidot(N, k + 1, h->d_V, w, part, hbuf, h->stream));
@@ -775,10 +783,7 @@ int gmres(wbem_context* h, const double* rhs, double* x, int restart, int max_st
       y[j] = s / H[(size_t)j * restart + j];
     }
     CU(cudaMemcpyAsync(hbuf, y.data(), sizeof(double) * k, cudaMemcpyHostToDevice, h->stream));
-    CU(cudaMemsetAsync(w, 0, sizeof(double) * N, h->stream));
-    CU(launch_axpy_basis(N, k, h->d_V, hbuf, w, 1.0, h->stream));
-    CHK(prec(w, z));
-    CU(launch_axpby(N, 1.0, z, 1.0, x, h->stream));
+    CU(launch_axpy_basis(N, k, Z, hbuf, x, 1.0, h->stream));
     // the host vector y must stay alive until the copy above completes
     CU(cudaStreamSynchronize(h->stream));
   }
