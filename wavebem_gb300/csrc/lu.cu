@@ -12,19 +12,20 @@
 // non-finite -> WBEM_ERR_SINGULAR).
 //
 // Step k (block size kNB = 128), inside outer panels of kNB2 = 512 columns:
-//   1. k_diag_block: LU of A_kk in shared memory, plus the inverses of its
-//      unit-lower and upper factors;
+//   1. k_diag_block: LU of A_kk (one CTA, registers + shared memory), plus
+//      the inverses of its unit-lower and upper factors;
 //   2. k_panel_small: L_ik = A_ik inv(U_kk) and U_kj = inv(L_kk) A_kj (FP32
 //      SIMT), the column panel also writing the BF16 hi/lo split of L21;
 //      then the panel's own trailing update A_ij -= L_ik U_kj (FP32, K = 128).
 // Per outer panel P: U12 = inv(L11) A12 for the rest of its rows (FP32, with
-// the earlier blocks' updates first), then the bulk trailing update
+// the earlier blocks' updates first; block row k as soon as A_kk is factored,
+// on its own stream), then the bulk trailing update
 // A22 -= L21 U12 on the tensor cores, k_gemm_bf16x3: Lhi Uhi + Lhi Ulo +
 // Llo Uhi with FP32 accumulation in TMEM, K = 512, persistent 128 x 256
 // tiles. It is split between the next panel's columns (high-priority stream)
 // and the remainder (low-priority stream). The panel kernels have a 13 KB
 // footprint, so the next panel's chain runs beside the remainder's CTAs on
-// every SM (look-ahead); a few SMs stay free for the 198 KB diagonal blocks.
+// every SM (look-ahead); a few SMs stay free for the 200 KB diagonal blocks.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -110,249 +111,10 @@ __global__ void k_lu_constraint_entries(int nrows, const int* __restrict__ crow,
 
 // ------------------------------------------------------------ diagonal block
 // LU (no pivoting) of the kNB x kNB block at (k0, k0) and the inverses of its
-// unit-lower and upper factors, blocked by 32 inside one CTA (16 warps):
-//   per 32-block s: warp 0 factors the diagonal sub-block in registers with
-//   shuffles (one column per lane) and inverts its two triangles; 6 warps do
-//   the 32x32 triangular panel products; 9 warps the trailing 32x32 updates.
-// The 128x128 inverses are then assembled block by block
-//   Linv_ts = -Linv_tt sum_{u=s}^{t-1} L_tu Linv_us (and the mirror for U).
-// 4 x 3 + 3 barriers in total. Writes the factors back to A, the inverses
-// row-major (linv, uinv) and column-major (linvT, uinvT).
-constexpr int kDiagThreads = 512;
-constexpr int kDLD = kNB + 1;
-
-// C[32x32] (ld) = sign * A[32x32] * B[32x32] (+ C if acc), one warp; lane = column.
-__device__ __forceinline__ void w_gemm_col(float* C, const float* A, const float* B, float sign,
-                                           bool acc) {
-  const int lane = threadIdx.x & 31;
-  float col[32];
-#pragma unroll
-  for (int k = 0; k < 32; ++k) col[k] = B[k * kDLD + lane];
-#pragma unroll 4
-  for (int r = 0; r < 32; ++r) {
-    float sum = 0.f;
-#pragma unroll
-    for (int k = 0; k < 32; ++k) sum = __fmaf_rn(A[r * kDLD + k], col[k], sum);
-    C[r * kDLD + lane] = acc ? __fmaf_rn(sign, sum, C[r * kDLD + lane]) : sign * sum;
-  }
-}
-// Row-split products: several warps share one 32 x 32 output block. A warp
-// holds one column (lane = column) or one row (lane = row) of an operand in
-// registers and produces a range of output rows (columns). Loads and stores
-// are separated by a CTA barrier where the product is in place.
-__device__ __forceinline__ void load_col32(float v[32], const float* B) {
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int k = 0; k < 32; ++k) v[k] = B[k * kDLD + lane];
-}
-__device__ __forceinline__ void load_row32(float v[32], const float* A) {
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int k = 0; k < 32; ++k) v[k] = A[lane * kDLD + k];
-}
-// rows [r0, r0 + nr) of C = sign * A * col (+ C if acc), lane = column
-__device__ __forceinline__ void rows_prod(float* C, const float* A, const float col[32], float sign,
-                                          bool acc, int r0, int nr) {
-  const int lane = threadIdx.x & 31;
-  for (int r = r0; r < r0 + nr; ++r) {
-    float sum = 0.f;
-#pragma unroll
-    for (int k = 0; k < 32; ++k) sum = __fmaf_rn(A[r * kDLD + k], col[k], sum);
-    C[r * kDLD + lane] = acc ? __fmaf_rn(sign, sum, C[r * kDLD + lane]) : sign * sum;
-  }
-}
-// columns [c0, c0 + nc) of C = row * B, lane = row
-__device__ __forceinline__ void cols_prod(float* C, const float row[32], const float* B, int c0,
-                                          int nc) {
-  const int lane = threadIdx.x & 31;
-  for (int c = c0; c < c0 + nc; ++c) {
-    float sum = 0.f;
-#pragma unroll
-    for (int k = 0; k < 32; ++k) sum = __fmaf_rn(row[k], B[k * kDLD + c], sum);
-    C[lane * kDLD + c] = sum;
-  }
-}
-// warps per task when 16 warps share ntask 32 x 32 tasks (a power of two)
-__device__ __forceinline__ int warps_per_task(int ntask) {
-  return ntask <= 1 ? 16 : ntask <= 2 ? 8 : ntask <= 4 ? 4 : ntask <= 8 ? 2 : 1;
-}
-
-// C[32x32] = A[32x32] * B[32x32] with lane = row (A read by rows, in place on A allowed).
-__device__ __forceinline__ void w_gemm_row(float* C, const float* A, const float* B) {
-  const int lane = threadIdx.x & 31;
-  float row[32];
-#pragma unroll
-  for (int k = 0; k < 32; ++k) row[k] = A[lane * kDLD + k];
-#pragma unroll 4
-  for (int c = 0; c < 32; ++c) {
-    float sum = 0.f;
-#pragma unroll
-    for (int k = 0; k < 32; ++k) sum = __fmaf_rn(row[k], B[k * kDLD + c], sum);
-    C[lane * kDLD + c] = sum;
-  }
-}
-
-__global__ void __launch_bounds__(kDiagThreads, 1)
-    k_diag_block(int ld, int k0, int nb, float* __restrict__ A, float* __restrict__ linv,
-                 float* __restrict__ uinv, float* __restrict__ linvT, float* __restrict__ uinvT,
-                 DevErr* err) {
-  extern __shared__ __align__(16) float dsm[];
-  float* sA = dsm;                // [128][129] block, becomes L\U
-  float* sLi = sA + kNB * kDLD;   // [128][129] inv(L)
-  float* sUi = sLi + kNB * kDLD;  // [128][129] inv(U)
-  __shared__ int bad;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  for (int idx = tid; idx < kNB * kNB; idx += kDiagThreads) {
-    const int r = idx >> 7, c = idx & 127;
-    sA[r * kDLD + c] = (r < nb && c < nb) ? A[(size_t)(k0 + r) * ld + k0 + c] : (r == c ? 1.f : 0.f);
-    sLi[r * kDLD + c] = 0.f;
-    sUi[r * kDLD + c] = 0.f;
-  }
-  if (tid == 0) bad = 0;
-  __syncthreads();
-  for (int s = 0; s < 4; ++s) {
-    const int o = 32 * s;
-    if (warp == 0) {
-      // ---- LU of the diagonal 32-block, lane = column
-      float col[32];
-#pragma unroll
-      for (int r = 0; r < 32; ++r) col[r] = sA[(o + r) * kDLD + o + lane];
-      bool okp = true;
-#pragma unroll
-      for (int k = 0; k < 32; ++k) {
-        const float piv = __shfl_sync(0xffffffffu, col[k], k);
-        okp = okp && (fabsf(piv) > 0.f) && isfinite(piv);
-        const float ip = __frcp_rn(piv);
-        // constant trip count, so both loops unroll and col[] stays in registers
-#pragma unroll
-        for (int r = 1; r < 32; ++r) {
-          if (r <= k) continue;
-          const float l = __shfl_sync(0xffffffffu, col[r], k) * ip;
-          if (lane == k) col[r] = l;
-          else if (lane > k) col[r] = __fmaf_rn(-l, col[k], col[r]);
-        }
-      }
-#pragma unroll
-      for (int r = 0; r < 32; ++r) sA[(o + r) * kDLD + o + lane] = col[r];
-      if (!okp && lane == 0) bad = 1;
-    }
-    __syncthreads();
-    if (bad) {
-      if (tid == 0) dev_fail(err, WBEM_ERR_SINGULAR, 51, k0, o);
-      return;  // uniform
-    }
-    // ---- inverses of the two triangles of the 32-block (warp 0: L, warp 1:
-    // U), lane = column
-    if (warp == 0) {
-      float x[32];
-#pragma unroll
-      for (int r = 0; r < 32; ++r) {
-        float sum = 0.f;
-#pragma unroll
-        for (int t = 0; t < r; ++t) sum = __fmaf_rn(sA[(o + r) * kDLD + o + t], x[t], sum);
-        x[r] = (r == lane) ? 1.f : (r > lane ? -sum : 0.f);
-      }
-#pragma unroll
-      for (int r = 0; r < 32; ++r) sLi[(o + r) * kDLD + o + lane] = x[r];
-    } else if (warp == 1) {
-      // reciprocals of the 32 pivots, one per lane, broadcast in the sweep
-      const float rd = __frcp_rn(sA[(o + lane) * kDLD + o + lane]);
-      float x[32];
-#pragma unroll
-      for (int rr = 0; rr < 32; ++rr) {
-        const int r = 31 - rr;
-        float sum = 0.f;
-#pragma unroll
-        for (int t = r + 1; t < 32; ++t) sum = __fmaf_rn(sA[(o + r) * kDLD + o + t], x[t], sum);
-        const float di = __shfl_sync(0xffffffffu, rd, r);
-        x[r] = (r == lane) ? di : (r < lane ? -sum * di : 0.f);
-      }
-#pragma unroll
-      for (int r = 0; r < 32; ++r) sUi[(o + r) * kDLD + o + lane] = x[r];
-    }
-    __syncthreads();
-    const int np = 3 - s;
-    if (np == 0) break;
-    // ---- panels (in place): U_st = inv(L_ss) A_st (tasks 0..np-1, lane =
-    // column) and L_ts = A_ts inv(U_ss) (tasks np..2np-1, lane = row)
-    {
-      const int ntask = 2 * np, wpt = warps_per_task(ntask), part = 32 / wpt;
-      const int task = warp / wpt, sub = warp % wpt;
-      const bool act = task < ntask;
-      const bool upanel = task < np;
-      const int t = s + 1 + (upanel ? task : task - np);
-      float v[32];
-      if (act) {
-        if (upanel) load_col32(v, sA + o * kDLD + 32 * t);
-        else load_row32(v, sA + 32 * t * kDLD + o);
-      }
-      __syncthreads();
-      if (act) {
-        if (upanel) rows_prod(sA + o * kDLD + 32 * t, sLi + o * kDLD + o, v, 1.f, false, sub * part, part);
-        else cols_prod(sA + 32 * t * kDLD + o, v, sUi + o * kDLD + o, sub * part, part);
-      }
-      __syncthreads();
-    }
-    // ---- trailing: A_tu -= L_ts U_su (np * np tasks, lane = column)
-    {
-      const int ntask = np * np, wpt = warps_per_task(ntask), part = 32 / wpt;
-      const int task = warp / wpt, sub = warp % wpt;
-      if (task < ntask) {
-        const int t = s + 1 + task / np, u = s + 1 + task % np;
-        float v[32];
-        load_col32(v, sA + o * kDLD + 32 * u);
-        rows_prod(sA + 32 * t * kDLD + 32 * u, sA + 32 * t * kDLD + o, v, -1.f, true, sub * part, part);
-      }
-      __syncthreads();
-    }
-  }
-  // ---- off-diagonal blocks of the inverses, by distance d = t - s:
-  //   Linv_ts = -Linv_tt sum_{u=s}^{t-1} L_tu Linv_us   (tasks 0..npairs-1)
-  //   Uinv_st = -Uinv_ss sum_{u=s+1}^{t} U_su Uinv_ut   (tasks npairs..)
-  // first the sums into the (t, s) / (s, t) block, then the in-place product
-  for (int d = 1; d < 4; ++d) {
-    const int npairs = 4 - d, ntask = 2 * npairs, wpt = warps_per_task(ntask), part = 32 / wpt;
-    const int task = warp / wpt, sub = warp % wpt;
-    const bool act = task < ntask;
-    const bool lt = task < npairs;
-    const int sb = lt ? task : task - npairs, tb = sb + d;
-    float* T = lt ? sLi + 32 * tb * kDLD + 32 * sb : sUi + 32 * sb * kDLD + 32 * tb;
-    if (act) {
-      float v[32];
-      if (lt) {
-        for (int u = sb; u < tb; ++u) {
-          load_col32(v, sLi + 32 * u * kDLD + 32 * sb);
-          rows_prod(T, sA + 32 * tb * kDLD + 32 * u, v, 1.f, u > sb, sub * part, part);
-        }
-      } else {
-        for (int u = sb + 1; u <= tb; ++u) {
-          load_col32(v, sUi + 32 * u * kDLD + 32 * tb);
-          rows_prod(T, sA + 32 * sb * kDLD + 32 * u, v, 1.f, u > sb + 1, sub * part, part);
-        }
-      }
-    }
-    __syncthreads();
-    float v[32];
-    if (act) load_col32(v, T);
-    __syncthreads();
-    if (act) {
-      const float* Dg = lt ? sLi + 32 * tb * kDLD + 32 * tb : sUi + 32 * sb * kDLD + 32 * sb;
-      rows_prod(T, Dg, v, -1.f, false, sub * part, part);
-    }
-    __syncthreads();
-  }
-  for (int idx = tid; idx < kNB * kNB; idx += kDiagThreads) {
-    const int r = idx >> 7, c = idx & 127;
-    if (r < nb && c < nb) A[(size_t)(k0 + r) * ld + k0 + c] = sA[r * kDLD + c];
-    linv[idx] = sLi[r * kDLD + c];
-    uinv[idx] = sUi[r * kDLD + c];
-    linvT[idx] = sLi[c * kDLD + r];
-    uinvT[idx] = sUi[c * kDLD + r];
-  }
-}
-
-// The same outputs by a register-resident unblocked elimination with one
-// CTA barrier per pivot and every thread busy at every pivot. 1024 threads:
+// unit-lower and upper factors; writes the factors back to A, the inverses
+// row-major (linv, uinv) and column-major (linvT, uinvT). One CTA, a
+// register-resident unblocked elimination with one CTA barrier per pivot and
+// every thread busy at every pivot. 1024 threads:
 // thread (r, q) holds 16 entries of row r (columns 16q .. 16q+15) in
 // registers:
 //   * while r > k (row below the pivot) the combined row of the LU: the
@@ -368,8 +130,9 @@ __global__ void __launch_bounds__(kDiagThreads, 1)
 // a compile-time index. Warp w takes column block q = w / 4 and row group g
 // with g + q = w (mod 4): each scheduler (w mod 4) holds two warps of every
 // row group and one of the four warps that own a pivot column.
-constexpr int kDiag2Threads = 1024;
-constexpr int kDRowLD = 132;  // row history: 16-byte rows
+constexpr int kDLD = kNB + 1;     // padded shared rows
+constexpr int kDiagThreads = 1024;
+constexpr int kDRowLD = 132;      // row history: 16-byte rows
 constexpr size_t kDiagSmemBytes = ((size_t)kNB * kDLD + (size_t)kNB * kDRowLD + 2 * kNB + kNB) * sizeof(float);
 
 __device__ __forceinline__ float rcp_approx(float x) {
@@ -378,8 +141,8 @@ __device__ __forceinline__ float rcp_approx(float x) {
   return y;
 }
 
-__global__ void __launch_bounds__(kDiag2Threads, 1)
-    k_diag_block2(int ld, int k0, int nb, float* __restrict__ A, float* __restrict__ linv,
+__global__ void __launch_bounds__(kDiagThreads, 1)
+    k_diag_block(int ld, int k0, int nb, float* __restrict__ A, float* __restrict__ linv,
                   float* __restrict__ uinv, float* __restrict__ linvT, float* __restrict__ uinvT,
                   DevErr* err) {
   extern __shared__ __align__(16) float dsm[];
@@ -391,7 +154,7 @@ __global__ void __launch_bounds__(kDiag2Threads, 1)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int q = warp >> 2, g = ((warp & 3) - q) & 3;
   const int r = 32 * g + lane, c0 = 16 * q;
-  for (int idx = tid; idx < kNB * kNB; idx += kDiag2Threads) {
+  for (int idx = tid; idx < kNB * kNB; idx += kDiagThreads) {
     const int rr = idx >> 7, cc = idx & 127;
     float* dst = sLZ + rr * kDLD + cc;
     if (rr < nb && cc < nb)
@@ -472,7 +235,7 @@ __global__ void __launch_bounds__(kDiag2Threads, 1)
     if (tid == 0) dev_fail(err, WBEM_ERR_SINGULAR, 51, k0, 0);
     return;  // uniform
   }
-  for (int idx = tid; idx < kNB * kNB; idx += kDiag2Threads) {
+  for (int idx = tid; idx < kNB * kNB; idx += kDiagThreads) {
     const int rr = idx >> 7, cc = idx & 127;
     const float rowv = sRows[rr * kDRowLD + cc];
     if (rr < nb && cc < nb) A[(size_t)(k0 + rr) * ld + k0 + cc] = cc < rr ? sLZ[rr * kDLD + cc] : rowv;
@@ -604,98 +367,9 @@ __device__ __forceinline__ void panel_epilogue(const PanelArgs& pa, const SplitO
     }
 }
 
-// Panel products with the whole K chunk resident in shared memory: the CTA
-// copies its Lft rows (TM x 128) and the Rgt block (128 x TN) with cp.async in
-// one go, waits once, and runs 128 FMA steps from shared memory (no per-step
-// global latency). Larger K (the row-panel update) loops over 128-chunks.
-//   TM x TN = 64 x 128 (column panels: tall, full width) or 128 x 64 (row
-//   panels and their updates: full height, column strips); 256 threads, 32
-//   outputs each; 96 KB of shared memory, two CTAs per SM.
-//   ATRANS: Lft is given transposed (LT(k, i) = L[k * ldl + i], e.g. the
-//   column-major copy of inv(L_kk)), so its fragments are float4 reads.
-__device__ __forceinline__ void cp_async16(void* dst, const void* src, int src_bytes) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src),
-               "r"(src_bytes)
-               : "memory");
-}
-
-template <int TM, int TN, bool ATRANS>
-__global__ void __launch_bounds__(256, 2) k_panel_tile(PanelArgs pa, SplitOut s1, SplitOut s2) {
-  constexpr int KC = 128;
-  constexpr int ALD = ATRANS ? TM + 4 : KC + 4;  // padded smem rows
-  constexpr int BLD = TN + 4;
-  extern __shared__ __align__(16) float psm[];
-  float* As = psm;                        // ATRANS: [KC][ALD] else [TM][ALD]
-  float* Bs = psm + (ATRANS ? KC : TM) * ALD;  // [KC][BLD]
-  const int tid = threadIdx.x;
-  const int tx = tid & 15, ty = tid >> 4;
-  const int i0 = blockIdx.x * TM, j0 = blockIdx.y * TN;
-  // thread outputs: TM x TN = 64 x 128 -> rows ty*4+u, cols {tx*4+v, 64+tx*4+v}
-  //                 128 x 64          -> rows {ty*4+u, 64+ty*4+u}, cols tx*4+v
-  constexpr int RH = TM / 64, CH = TN / 64;  // row / column halves per thread
-  float acc[4 * RH][4 * CH];
-#pragma unroll
-  for (int u = 0; u < 4 * RH; ++u)
-#pragma unroll
-    for (int v = 0; v < 4 * CH; ++v) acc[u][v] = 0.f;
-  for (int kc = 0; kc < pa.K; kc += KC) {
-    if (kc > 0) __syncthreads();  // previous chunk consumed
-    // ---- stage Lft
-    if (ATRANS) {
-      for (int q = tid; q < KC * (TM / 4); q += 256) {
-        const int k = q / (TM / 4), c = (q % (TM / 4)) * 4;
-        const int gi = i0 + c;
-        const int nbytes = gi + 4 <= pa.rows ? 16 : (gi < pa.rows ? 4 * (pa.rows - gi) : 0);
-        const float* src = pa.L + (size_t)(kc + k) * pa.ldl + (nbytes ? gi : 0);
-        cp_async16(As + k * ALD + c, src, nbytes);
-      }
-    } else {
-      for (int q = tid; q < TM * (KC / 4); q += 256) {
-        const int i = q / (KC / 4), c = (q % (KC / 4)) * 4;
-        const bool ok = i0 + i < pa.rows;
-        const float* src = pa.L + (size_t)(ok ? i0 + i : 0) * pa.ldl + kc + c;
-        cp_async16(As + i * ALD + c, src, ok ? 16 : 0);
-      }
-    }
-    // ---- stage Rgt
-    for (int q = tid; q < KC * (TN / 4); q += 256) {
-      const int k = q / (TN / 4), c = (q % (TN / 4)) * 4;
-      const int gj = j0 + c;
-      const int nbytes = gj + 4 <= pa.cols ? 16 : (gj < pa.cols ? 4 * (pa.cols - gj) : 0);
-      const float* src = pa.R + (size_t)(kc + k) * pa.ldr + (nbytes ? gj : 0);
-      cp_async16(Bs + k * BLD + c, src, nbytes);
-    }
-    asm volatile("cp.async.commit_group;\n cp.async.wait_group 0;" ::: "memory");
-    __syncthreads();
-#pragma unroll 4
-    for (int k = 0; k < KC; ++k) {
-      float a[4 * RH], b[4 * CH];
-#pragma unroll
-      for (int h = 0; h < RH; ++h) {
-        if (ATRANS) {
-          const float4 t = *reinterpret_cast<const float4*>(As + k * ALD + h * 64 + ty * 4);
-          a[4 * h] = t.x; a[4 * h + 1] = t.y; a[4 * h + 2] = t.z; a[4 * h + 3] = t.w;
-        } else {
-#pragma unroll
-          for (int u = 0; u < 4; ++u) a[4 * h + u] = As[(h * 64 + ty * 4 + u) * ALD + k];
-        }
-      }
-#pragma unroll
-      for (int h = 0; h < CH; ++h) {
-        const float4 t = *reinterpret_cast<const float4*>(Bs + k * BLD + h * 64 + tx * 4);
-        b[4 * h] = t.x; b[4 * h + 1] = t.y; b[4 * h + 2] = t.z; b[4 * h + 3] = t.w;
-      }
-#pragma unroll
-      for (int u = 0; u < 4 * RH; ++u)
-#pragma unroll
-        for (int v = 0; v < 4 * CH; ++v) acc[u][v] = __fmaf_rn(a[u], b[v], acc[u][v]);
-    }
-  }
-  panel_epilogue<RH, CH>(pa, s1, s2, acc, i0, j0, ty, tx);
-}
-
-// The same panel products with a 12 KB shared-memory footprint: K streams
-// through shared memory 16 at a time (register prefetch of the next step),
+// Panel products C = sign * Lft * Rgt (+ C) in FP32 with a 13 KB shared-memory
+// footprint: K streams through shared memory 16 at a time (register prefetch
+// of the next step),
 // so these CTAs fit beside a persistent GEMM CTA (208 KB) on the same SM and
 // the panel chain of the next outer panel runs while the bulk trailing update
 // holds every SM.
@@ -811,23 +485,6 @@ static cudaError_t run_panel_small(const PanelArgs& pa, const SplitOut& s1, cons
                                    cudaStream_t s) {
   dim3 g((pa.rows + TM - 1) / TM, (pa.cols + TN - 1) / TN);
   k_panel_small<TM, TN, ATRANS><<<g, 256, 0, s>>>(pa, s1, s2);
-  return cudaGetLastError();
-}
-
-template <int TM, int TN, bool ATRANS>
-static cudaError_t run_panel_tile(const PanelArgs& pa, const SplitOut& s1, const SplitOut& s2,
-                                  cudaStream_t s) {
-  constexpr int ALD = ATRANS ? TM + 4 : 128 + 4;
-  const size_t smem = sizeof(float) * ((size_t)(ATRANS ? 128 : TM) * ALD + (size_t)128 * (TN + 4));
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_panel_tile<TM, TN, ATRANS>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
-  dim3 g((pa.rows + TM - 1) / TM, (pa.cols + TN - 1) / TN);
-  k_panel_tile<TM, TN, ATRANS><<<g, 256, smem, s>>>(pa, s1, s2);
   return cudaGetLastError();
 }
 
@@ -1576,7 +1233,7 @@ int factor_mixed(wbem_context* h) {
   float* A = h->d_lu;
   const SplitOut none{nullptr, nullptr, 0, 0, 0};
   const size_t kDiagSmem = kDiagSmemBytes;
-  WB_CU(cudaFuncSetAttribute(k_diag_block2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDiagSmem));
+  WB_CU(cudaFuncSetAttribute(k_diag_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDiagSmem));
   // Right-looking LU over outer panels P = [p0, p1) of kNB2 columns, with
   // look-ahead.
   //   s_panel: the column work of P (diagonal blocks, column panels, inner
@@ -1623,7 +1280,7 @@ int factor_mixed(wbem_context* h) {
       const int k = k0 / kNB, nb = std::min(kNB, N - k0), k1 = k0 + nb;
       const size_t bo = (size_t)k * kNB * kNB;
       pb(h->prof_diag, sp);
-      k_diag_block2<<<1, kDiag2Threads, kDiagSmem, sp>>>(ld, k0, nb, A, L.linv + bo, L.uinv + bo,
+      k_diag_block<<<1, kDiagThreads, kDiagSmem, sp>>>(ld, k0, nb, A, L.linv + bo, L.uinv + bo,
                                                         L.linvT + bo, L.uinvT + bo, h->d_err);
       pe(h->prof_diag, sp, 0.0);
       h->launches++;
