@@ -133,6 +133,12 @@ int wbem_get_matrices(wbem_handle h, double* neumann, double* dirichlet);
 /* BEMProblem::vmult (source/bem_problem.cc:620-670) and compute_rhs (:673-811). */
 int wbem_vmult(wbem_handle h, const double* src, double* dst);
 int wbem_compute_rhs(wbem_handle h, const double* src, double* dst);
+/* BEMProblem::residual (source/bem_problem.cc:903-961): res = A_c sol - rhs_c
+ * of the constrained system, with the known data of (phi, dphi_dn) (phi on
+ * Dirichlet nodes, dphi_dn elsewhere) forming the right-hand side and the
+ * other entries the solution vector. Uses the current assembly; rebuilds the
+ * constraint inhomogeneities from the known data, as a solve does. */
+int wbem_residual(wbem_handle h, const double* phi, const double* dphi_dn, double* res);
 
 /* Hull force F = sum over cells hull_cells[k] of  int p n_dir dS,
  * p = -(U . grad phi + |grad phi|^2 / 2) (steady, rho = 1, g = 0 form of

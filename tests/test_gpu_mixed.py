@@ -50,6 +50,17 @@ def test_mixed_solve_within_1e8(kind, n, solver):
         assert 1 <= st["outer_iterations"] <= 10
 
 
+def test_mixed_residual_of_solution():
+    P, m, b = oracle_problem("wigley", 2000)
+    g = BEMProblem(m.X, m.cells, m.dirichlet, P.dn_ptr, P.dn_idx, precision=PREC_MIXED)
+    phi, dphi = b.copy(), b.copy()
+    g.solve(phi, dphi, b)
+    res = np.zeros(P.N)
+    g.residual(res, phi, dphi)
+    # the residual of the double-float operator the refinement converged on
+    assert np.linalg.norm(res) <= 1e-9 * np.linalg.norm(P.system(b)[1])
+
+
 def test_mixed_hull_force_within_1e8():
     P, m, b = oracle_problem("wigley", 2000)
     phi_o, dphi_o, _ = P.solve_system(b)

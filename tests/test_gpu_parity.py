@@ -49,6 +49,27 @@ def test_fp64_operators():
     assert rel2(g.compute_rhs(v), P.compute_rhs(v)) <= 1e-12
 
 
+def test_fp64_residual():
+    """BEMProblem::residual: A_c sol - rhs_c of the constrained system for given
+    (phi, dphi_dn), against the oracle's constrained system; and ~0 for the
+    solution of a solve."""
+    P, m, b = oracle_problem("wigley", 2000)
+    g = _gpu(m, P.dn_ptr, P.dn_idx)
+    g.assemble_system()
+    rng = np.random.default_rng(11)
+    phi, dphi = rng.normal(size=P.N), rng.normal(size=P.N)
+    mask = m.dirichlet.astype(bool)
+    A, rhs = P.system(np.where(mask, phi, dphi))
+    ref = A @ np.where(mask, dphi, phi) - rhs
+    res = np.zeros(P.N)
+    g.residual(res, phi, dphi)
+    assert rel2(res, ref) <= 1e-11
+    phi, dphi = b.copy(), b.copy()
+    g.solve_system(phi, dphi, b)
+    g.residual(res, phi, dphi)
+    assert np.linalg.norm(res) <= 1e-9 * np.linalg.norm(P.system(b)[1])
+
+
 def test_fp64_double_nodes_found_by_library():
     P, m, b = oracle_problem("wigley", 2000)
     g = BEMProblem(m.X, m.cells, m.dirichlet)  # library finds the double nodes

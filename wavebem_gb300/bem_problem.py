@@ -31,7 +31,7 @@ SOLVER_AUTO, SOLVER_GMRES, SOLVER_LU, SOLVER_GMRES_IR = 0, 1, 2, 3
 EXPORTS = ["wbem_default_options", "wbem_create", "wbem_destroy", "wbem_last_error",
            "wbem_set_geometry", "wbem_update_nodes", "wbem_set_bc", "wbem_assemble",
            "wbem_solve_system", "wbem_solve", "wbem_get_alpha", "wbem_get_matrices",
-           "wbem_vmult", "wbem_compute_rhs", "wbem_hull_force", "wbem_force_adjoint",
+           "wbem_vmult", "wbem_compute_rhs", "wbem_residual", "wbem_hull_force", "wbem_force_adjoint",
            "wbem_get_stats"]
 
 
@@ -93,6 +93,7 @@ def load_library(path: str = LIB_PATH):
     L.wbem_get_matrices.argtypes = [H, C.c_void_p, C.c_void_p]
     L.wbem_vmult.argtypes = [H, dp, dp]
     L.wbem_compute_rhs.argtypes = [H, dp, dp]
+    L.wbem_residual.argtypes = [H, dp, dp, dp]
     L.wbem_hull_force.argtypes = [H, ip, C.c_int, dp, C.c_int, dp, dp, C.POINTER(C.c_double)]
     L.wbem_force_adjoint.argtypes = [H, ip, C.c_int, dp, C.c_int, dp, dp, dp]
     L.wbem_get_stats.argtypes = [H, C.POINTER(Stats)]
@@ -204,6 +205,15 @@ class BEMProblem:
         dst = np.zeros(self.n_dofs)
         self._check(self.L.wbem_compute_rhs(self.h, _f64(src), dst))
         return dst
+
+    def residual(self, res, phi, dphi_dn):
+        """BEMProblem::residual (source/bem_problem.cc:903-961): res = A_c sol -
+        rhs_c, with the known data of (phi, dphi_dn) forming the right-hand side
+        and the unknown entries the solution vector."""
+        out = np.zeros(self.n_dofs)
+        self._check(self.L.wbem_residual(self.h, _f64(phi), _f64(dphi_dn), out))
+        res[:] = out
+        return res
 
     def matrices(self, neumann=True, dirichlet=True):
         N = self.n_dofs

@@ -1355,6 +1355,46 @@ static int op_caller(wbem_handle h, int mode, const double* src, double* dst) {
 int wbem_vmult(wbem_handle h, const double* src, double* dst) { return op_caller(h, 0, src, dst); }
 int wbem_compute_rhs(wbem_handle h, const double* src, double* dst) { return op_caller(h, 1, src, dst); }
 
+// BEMProblem::residual (source/bem_problem.cc:903-961): the known data of
+// (phi, dphi_dn) forms the right-hand side (compute_rhs + constraints, as a
+// solve does), the unknown entries the solution vector, and
+// res = A_c sol - rhs_c with the constrained operator.
+int wbem_residual(wbem_handle h, const double* phi, const double* dphi_dn, double* res) {
+  if (!h) return WBEM_ERR_ARG;
+  if (!phi || !dphi_dn || !res) return fail(h, WBEM_ERR_ARG, "wbem_residual: NULL pointer");
+  if (h->assembled_prec < 0) return fail(h, WBEM_ERR_STATE, "wbem_residual: assemble first");
+  if (!h->have_mask) return fail(h, WBEM_ERR_STATE, "wbem_residual: set the boundary conditions first");
+  const int N = h->N;
+  for (int i = 0; i < N; ++i)
+    if (!std::isfinite(phi[i]) || !std::isfinite(dphi_dn[i]))
+      return fail(h, WBEM_ERR_NONFINITE, "wbem_residual: non-finite input");
+  cudaSetDevice(h->device);
+  CHK(ensure_vectors(h, h->opt.gmres_restart));
+  std::vector<double> tmp(N), xi(N), yi(N), ri(N);
+  for (int p = 0; p < N; ++p) tmp[p] = h->mask[p] ? phi[p] : dphi_dn[p];
+  CHK(prepare_rhs(h, tmp.data()));
+  for (int i = 0; i < N; ++i) {
+    const int p = h->perm[i];
+    xi[i] = h->mask[p] ? dphi_dn[p] : phi[p];
+  }
+  CU(copy_sync(h, h->d_vec[3], xi.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+  CHK(apply_system(h, h->d_vec[3], h->d_vec[4]));
+  CU(copy_sync(h, yi.data(), h->d_vec[4], sizeof(double) * N, cudaMemcpyDeviceToHost));
+  CU(copy_sync(h, ri.data(), h->d_rhs, sizeof(double) * N, cudaMemcpyDeviceToHost));
+  for (int i = 0; i < N; ++i) res[h->perm[i]] = yi[i];
+  bool any = false;
+  for (int i = 0; i < N; ++i) any |= h->mask[i] != 0;
+  if (!any) {
+    // all-Neumann case of the reference's vmult: dst -= ||dst||_2
+    double sn = 0;
+    for (int i = 0; i < N; ++i) sn += res[i] * res[i];
+    sn = std::sqrt(sn);
+    for (int i = 0; i < N; ++i) res[i] -= sn;
+  }
+  for (int i = 0; i < N; ++i) res[h->perm[i]] -= ri[i];
+  return check_device_error(h, "wbem_residual");
+}
+
 int wbem_hull_force(wbem_handle h, const int* hull_cells, int n_hull, const double* U, int dir,
                     const double* phi, const double* dphi_dn, double* force) {
   if (!h) return WBEM_ERR_ARG;
