@@ -198,10 +198,23 @@ def run_reference(args, rank, world):
 
 
 # ------------------------------------------------------------------ GPU side
-# DRAM traffic per unit of work of the roofline kernels, from one ncu capture
-# each (dram__bytes_read.sum + dram__bytes_write.sum); the capture and the
-# command that made it are in the named profile summary.
-NCU_TRAFFIC = {}
+# DRAM traffic of one launch of the roofline kernels (dram__bytes_read.sum +
+# dram__bytes_write.sum) from one ncu capture each at N = 8,192 (the summary
+# named beside each gives the command). All three move O(N^2) bytes per
+# launch, so a launch at N dofs is scaled by (N / 8192)^2.
+NCU_TRAFFIC = {
+    "k_tile_mixed": (15.570688e6 + 1293.103e6, "profiles/k_tile_mixed_n8192.md"),
+    "k_matvec_mixed": (711.111168e6 + 2.802944e6, "profiles/k_matvec_mixed_n8192.md"),
+    "k_trsv_wave": (136.424192e6 + 3.058176e6, "profiles/k_trsv_wave_n8192.md"),
+}
+
+
+def ncu_traffic(kernel, n):
+    """(bytes per launch at n dofs, how it was obtained) or (None, None)."""
+    t = NCU_TRAFFIC.get(kernel)
+    if t is None:
+        return None, None
+    return t[0] * (n / 8192.0) ** 2, f"ncu capture at N = 8192 ({t[1]}), scaled by (N / 8192)^2"
 
 
 class KernelProfile:
@@ -409,13 +422,18 @@ def run_gpu(args, rank, world, local):
                             "unit": "GB/s", "frac": a / hbm, "work": "2 N^2 bytes per sweep",
                             "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({src})"})
         kernels.append({"kernel": "k_diag_block", "ms": kprof["diag_ms"], "launches": kprof["diag_launches"]})
-        kernels.append({"kernel": "k_panel_gemm+k_rowpanel_update", "ms": kprof["panel_ms"],
+        kernels.append({"kernel": "k_panel_small", "ms": kprof["panel_ms"],
                         "launches": kprof["panel_launches"]})
+        for k in kernels:
+            tb, _ = ncu_traffic(k["kernel"], N)
+            if tb is not None:
+                k["traffic_per_launch"] = tb
         dom = max((k for k in kernels if "bound" in k), key=lambda k: k["ms"])
         per_launch = dom["ms"] / max(1, dom["launches"])
         roof = {"bound": dom["bound"], "kernel": dom["kernel"], "achieved": dom["achieved"],
                 "peak": dom["peak"], "unit": dom["unit"], "frac": dom["frac"],
-                "traffic": NCU_TRAFFIC.get(dom["kernel"]), "ms_per_launch": per_launch,
+                "traffic": ncu_traffic(dom["kernel"], N)[0],
+                "traffic_source": ncu_traffic(dom["kernel"], N)[1], "ms_per_launch": per_launch,
                 "peak_source": dom["peak_source"],
                 "timing": "CUDA events around each launch on its own stream, in an instrumented "
                           "pass after the timed region (factorisation serialised on one stream)"}

@@ -786,6 +786,10 @@ int gmres(wbem_context* h, const double* rhs, double* x, int restart, int max_st
     CU(launch_axpy_basis(N, k, Z, hbuf, x, 1.0, h->stream));
     // the host vector y must stay alive until the copy above completes
     CU(cudaStreamSynchronize(h->stream));
+    // converged on the Arnoldi estimate: with the flexible update it is the
+    // true residual up to FP64 round-off, so no residual mat-vec follows
+    // (deal.II's SolverGMRES also stops on the estimate)
+    if (res <= target) break;
   }
   if (iters) *iters = it;
   if (resid) *resid = res;
