@@ -1053,10 +1053,12 @@ struct LuState {
   // second one, the rest of the trailing update on a low-priority stream
   cudaStream_t s_panel = nullptr;
   cudaStream_t s_row = nullptr;
+  cudaStream_t s_inrow = nullptr;      // in-panel row panel, beside the column panel
   cudaStream_t s_trail = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_row = nullptr, ev_trail = nullptr, ev_join = nullptr;
   cudaEvent_t ev_next_rows = nullptr;  // bulk update of the next panel's rows done
   cudaEvent_t ev_blk = nullptr;        // diagonal block ready for its row panel
+  cudaEvent_t ev_inrow = nullptr;      // in-panel row panel done
   cudaEvent_t ev_u12 = nullptr;        // row panel of the outer panel done
   float* w = nullptr;         // 2 x N ping-pong vectors
   unsigned* flags = nullptr;  // 4 x nblk publication flags
@@ -1083,7 +1085,9 @@ void free_lu(wbem_context* h) {
   if (L.s_panel) cudaStreamDestroy(L.s_panel);
   if (L.s_trail) cudaStreamDestroy(L.s_trail);
   if (L.s_row) cudaStreamDestroy(L.s_row);
-  for (cudaEvent_t e : {L.ev_fork, L.ev_row, L.ev_trail, L.ev_join, L.ev_next_rows, L.ev_blk, L.ev_u12})
+  if (L.s_inrow) cudaStreamDestroy(L.s_inrow);
+  for (cudaEvent_t e : {L.ev_fork, L.ev_row, L.ev_trail, L.ev_join, L.ev_next_rows, L.ev_blk, L.ev_u12,
+                        L.ev_inrow})
     if (e) cudaEventDestroy(e);
   if (L.w) cudaFree(L.w);
   if (L.flags) cudaFree(L.flags);
@@ -1225,8 +1229,9 @@ int factor_mixed(wbem_context* h) {
     WB_CU(cudaStreamCreateWithPriority(&L.s_panel, cudaStreamNonBlocking, hi));
     WB_CU(cudaStreamCreateWithPriority(&L.s_trail, cudaStreamNonBlocking, lo));
     WB_CU(cudaStreamCreateWithPriority(&L.s_row, cudaStreamNonBlocking, hi < lo ? hi + 1 : hi));
+    WB_CU(cudaStreamCreateWithPriority(&L.s_inrow, cudaStreamNonBlocking, hi));
     for (cudaEvent_t* e : {&L.ev_fork, &L.ev_row, &L.ev_trail, &L.ev_join, &L.ev_next_rows, &L.ev_blk,
-                           &L.ev_u12})
+                           &L.ev_u12, &L.ev_inrow})
       WB_CU(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
   }
   EvTimer tm(h->stream);
@@ -1239,6 +1244,8 @@ int factor_mixed(wbem_context* h) {
   //   s_panel: the column work of P (diagonal blocks, column panels, inner
   //     updates; columns [p0, p1) only), then the trailing update of the next
   //     panel's columns [p1, p2).
+  //   s_inrow: the in-panel row panel of block k (U_kj for the panel's
+  //     columns right of the block), beside the column panel of block k.
   //   s_row: the row panel U12 of P (rows [p0, p1), columns [p1, N)), block
   //     row k as soon as diagonal block k is factored, beside the column work.
   //   s_trail: the trailing update of the columns [p2, N): first the next
@@ -1252,6 +1259,7 @@ int factor_mixed(wbem_context* h) {
   const bool prof = h->profiling;
   cudaStream_t sp = prof ? h->stream : L.s_panel, st = prof ? h->stream : L.s_trail;
   cudaStream_t su = prof ? h->stream : L.s_row;
+  cudaStream_t sr = prof ? h->stream : L.s_inrow;
   if (prof) {
     h->prof_gemm.reset();
     h->prof_diag.reset();
@@ -1270,6 +1278,7 @@ int factor_mixed(wbem_context* h) {
   WB_CU(cudaStreamWaitEvent(sp, L.ev_fork, 0));
   WB_CU(cudaStreamWaitEvent(st, L.ev_fork, 0));
   WB_CU(cudaStreamWaitEvent(su, L.ev_fork, 0));
+  WB_CU(cudaStreamWaitEvent(sr, L.ev_fork, 0));
   bool trail_pending = false;  // a trailing update was queued on s_trail
   for (int p0 = 0; p0 < N; p0 += kNB2) {
     const int p1 = std::min(N, p0 + kNB2);
@@ -1284,11 +1293,23 @@ int factor_mixed(wbem_context* h) {
                                                         L.linvT + bo, L.uinvT + bo, h->d_err);
       pe(h->prof_diag, sp, 0.0);
       h->launches++;
+      WB_CU(cudaEventRecord(L.ev_blk, sp));
+      if (k1 < p1) {
+        // U_kj = inv(L_kk) A_kj for the panel's remaining columns, in place,
+        // beside the column panel
+        WB_CU(cudaStreamWaitEvent(sr, L.ev_blk, 0));
+        const PanelArgs pr{L.linvT + bo, kNB, A + (size_t)k0 * ld + k1, ld, A + (size_t)k0 * ld + k1,
+                           ld, kNB, p1 - k1, kNB, k0, k1, 0, 1};
+        pb(h->prof_panel, sr);
+        WB_CU((run_panel_small<128, 64, true>(pr, none, none, sr)));
+        pe(h->prof_panel, sr, 0.0);
+        WB_CU(cudaEventRecord(L.ev_inrow, sr));
+        h->launches++;
+      }
       if (p1 < N) {
         // ---- row panel block row k: A_kj -= L_k,[p0,k0) U_[p0,k0),j, then
         // U_kj = inv(L_kk) A_kj, for the columns right of the panel. L_k,[p0,k0)
         // comes from the column panels already queued on s_panel.
-        WB_CU(cudaEventRecord(L.ev_blk, sp));
         WB_CU(cudaStreamWaitEvent(su, L.ev_blk, 0));
         if (k0 == p0 && trail_pending) WB_CU(cudaStreamWaitEvent(su, L.ev_next_rows, 0));
         pb(h->prof_panel, su);
@@ -1318,18 +1339,15 @@ int factor_mixed(wbem_context* h) {
       h->launches++;
       if (k1 < p1) {
         const int w = p1 - k1;
-        // U_kj = inv(L_kk) A_kj for the panel's remaining columns, in place
-        const PanelArgs pr{L.linvT + bo, kNB, A + (size_t)k0 * ld + k1, ld, A + (size_t)k0 * ld + k1,
-                           ld, kNB, w, kNB, k0, k1, 0, 1};
-        pb(h->prof_panel, sp);
-        WB_CU((run_panel_small<128, 64, true>(pr, none, none, sp)));
         // inner update A[k1:, k1:p1] -= L_ik U_kj in FP32 (small footprint, so
         // it runs beside the previous outer panel's bulk update)
+        WB_CU(cudaStreamWaitEvent(sp, L.ev_inrow, 0));
         const PanelArgs pi{A + (size_t)k1 * ld + k0, ld, A + (size_t)k0 * ld + k1, ld,
                            A + (size_t)k1 * ld + k1, ld, m, w, kNB, k1, k1, 1, 0};
+        pb(h->prof_panel, sp);
         WB_CU((run_panel_small<64, 128, false>(pi, none, none, sp)));
         pe(h->prof_panel, sp, 0.0);
-        h->launches += 2;
+        h->launches++;
       }
       WB_CU(cudaGetLastError());
     }
@@ -1367,6 +1385,8 @@ int factor_mixed(wbem_context* h) {
     }
   }
   // join the streams back into the handle's stream
+  WB_CU(cudaEventRecord(L.ev_join, sr));
+  WB_CU(cudaStreamWaitEvent(h->stream, L.ev_join, 0));
   WB_CU(cudaEventRecord(L.ev_join, su));
   WB_CU(cudaStreamWaitEvent(h->stream, L.ev_join, 0));
   WB_CU(cudaEventRecord(L.ev_join, sp));
