@@ -129,6 +129,21 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def fp32_peak_tflops():
+    """FP32 FMA rate of this GPU from the library's probe (libwbem_peaks.so),
+    TFLOP/s, or None."""
+    import ctypes as C
+    try:
+        from wavebem_gb300.build import PEAKS_LIB
+        lib = C.CDLL(PEAKS_LIB)
+        lib.wbem_peak_probe.restype = C.c_double
+        lib.wbem_peak_probe.argtypes = [C.c_int]
+        v = lib.wbem_peak_probe(1)
+        return v / 1e3 if v > 0 else None
+    except OSError:
+        return None
+
+
 def load_peaks():
     try:
         return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -409,6 +424,16 @@ def run_gpu(args, rank, world, local):
                                 "(row, panel) pair), not by HBM: ncu IPC 2.9 of 4, FMA pipe 54% "
                                 "(profiles/k_tile_mixed_n8192.md)",
                         "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({src})"})
+        fp32 = fp32_peak_tflops()
+        if fp32:
+            # the survey's convention: 36 flop per regular kernel evaluation,
+            # 16 evaluations per (row, panel) pair
+            t = 36.0 * 16.0 * N * m.n_cells / (kprof["tile_ms"] / 1e3) / 1e12
+            kernels[-1]["fp32_roof"] = {
+                "achieved": t, "peak": fp32, "unit": "TFLOP/s", "frac": t / fp32,
+                "work": "36 flop per regular kernel evaluation x 16 N C (plain evaluation count; the "
+                        "double-float panel term and the 1.48x column-tile redundancy are not counted)",
+                "peak_source": "FP32 FMA loop (wbem_peak_probe) on this GPU"}
         if kprof["matvec_ms"] > 0:
             a = kprof["matvec_bytes"] / (kprof["matvec_ms"] / 1e3) / 1e9
             kernels.append({"kernel": "k_matvec_mixed", "bound": "hbm", "ms": kprof["matvec_ms"],
