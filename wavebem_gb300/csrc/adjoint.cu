@@ -525,7 +525,7 @@ int adjoint_force(wbem_context* h, const int* hull_cells, int n_hull, const doub
     double* bt = h->d_vec[7];
     double* part = h->d_part + 256 * 128;
     if (mixed)
-      WB_CU(launch_matvec_t_mixed(N, h->d_D2, h->d_N2, h->d_mask, nullptr, lamu, bt, part, h->stream));
+      WB_CU(launch_matvec_t_mixed(N, h->d_B2, h->d_mask, nullptr, lamu, bt, part, h->stream));
     else
       WB_CU(launch_matvec_t_fp64(N, h->d_D, h->d_N, h->d_mask, nullptr, lamu, bt, part, h->stream));
     double* gb = h->d_vec[0];

@@ -91,8 +91,16 @@ struct wbem_context {
   // ---- matrices (internal order)
   double* d_N = nullptr;
   double* d_D = nullptr;
-  float2* d_N2 = nullptr;
-  float2* d_D2 = nullptr;
+  // mixed form: (hi, lo) float pairs of the two operators, the boundary-
+  // condition selection applied per column (so each mat-vec streams one
+  // contiguous matrix): A2 = sel_j ? -D_ij : N_ij (system operator, vmult),
+  // B2 = sel_j ? -N_ij : D_ij (right-hand side, compute_rhs)
+  float2* d_A2 = nullptr;
+  float2* d_B2 = nullptr;
+  std::vector<uint8_t> sel_mask;  // internal order: the column mask A2 / B2 are selected for
+  uint8_t* d_selmask = nullptr;
+  int* d_flips = nullptr;         // columns to reselect after a mask change
+  size_t flips_cap = 0;
   double* d_alpha = nullptr;
   double* d_alpha_part = nullptr;
   double* d_alpha_near = nullptr;

@@ -50,25 +50,12 @@ cudaError_t launch_singular_fp64(int N, const double* X, const int* dnset, const
                                  DevErr* err, cudaStream_t s);
 cudaError_t launch_alpha_rowsum(int N, const double* Nm, double* alpha, cudaStream_t s);
 
-// ---- assembly (mixed form): N2/D2 hold (hi, lo) float pairs
-cudaError_t launch_cell_records_mixed(int C, const double* X, const int4* cell_dofs, float* rec32,
-                                      double* cellc, float* cellgeo, int q1, cudaStream_t s);
-cudaError_t launch_tile_mixed(int N, int q1, const double* X, const int* dnset, int n_tiles,
-                              const int* tile_ptr, const int2* tile_ent, const int4* cell_dofs,
-                              const float* rec32, const double* cellc, const float* cellgeo,
-                              float ratio, float2* N2, float2* D2, double* alpha_part,
-                              DevErr* err, cudaStream_t s);
-cudaError_t launch_near_mixed(int N, const double* X, const int* dnset, int C,
-                              const int4* cell_dofs, const float* cellgeo, float ratio,
-                              const double* rec64, int near_cap, int* near_cnt, int* near_cells,
-                              float2* N2, float2* D2, double* alpha_near, DevErr* err,
-                              cudaStream_t s);
-cudaError_t launch_singular_mixed(int N, const double* X, const int* dnset, const int* sptr,
-                                  const int* scell, const int4* cell_dofs, float2* N2, float2* D2,
-                                  double* alpha_sing, DevErr* err, cudaStream_t s);
-cudaError_t launch_alpha_mixed(int N, int n_tiles, const double* alpha_part,
-                               const double* alpha_near, const double* alpha_sing, double* alpha,
-                               cudaStream_t s);
+// ---- assembly (mixed form): A2 / B2 hold the selected (hi, lo) float pairs
+// of the system and right-hand-side operators (context.h)
+// A2, B2 of the columns in flips[0..nflip) after their boundary condition
+// changed: (A2, B2) <- (-B2, -A2)
+cudaError_t launch_reselect_pairs(int N, int nflip, const int* flips, float2* A2, float2* B2,
+                                  cudaStream_t s);
 
 // ---- operators and solver pieces
 // y = sum_j sel(i,j) x_j (+ diagonal term), sel per mode:
@@ -77,16 +64,16 @@ cudaError_t launch_alpha_mixed(int N, int n_tiles, const double* alpha_part,
 cudaError_t launch_matvec_fp64(int N, int mode, const double* Nm, const double* Dm,
                                const uint8_t* mask, const double* alpha, const double* x,
                                double* y, cudaStream_t s);
-cudaError_t launch_matvec_mixed(int N, int mode, const float2* N2, const float2* D2,
-                                const uint8_t* mask, const double* alpha, const double* x,
-                                double* y, cudaStream_t s);
+// mixed form: P = A2 (mode 0) or B2 (mode 1), the selection already applied
+cudaError_t launch_matvec_mixed(int N, int mode, const float2* P, const uint8_t* mask,
+                                const double* alpha, const double* x, double* y, cudaStream_t s);
 // transposed system operator: y_j = sum_i sel(i,j) x_i (+ diagonal)
 cudaError_t launch_matvec_t_fp64(int N, const double* Nm, const double* Dm, const uint8_t* mask,
                                  const double* alpha, const double* x, double* y, double* part,
                                  cudaStream_t s);
-cudaError_t launch_matvec_t_mixed(int N, const float2* N2, const float2* D2, const uint8_t* mask,
-                                  const double* alpha, const double* x, double* y, double* part,
-                                  cudaStream_t s);
+// mixed form: y_j = sum_i P_ij x_i (+ (1 - mask_j) alpha_j x_j if alpha)
+cudaError_t launch_matvec_t_mixed(int N, const float2* P, const uint8_t* mask, const double* alpha,
+                                  const double* x, double* y, double* part, cudaStream_t s);
 // constrained rows: y_i = x_i - sum c_ij x_j
 cudaError_t launch_constraint_rows(int nrows, const int* crow, const int* cptr, const int* ccol,
                                    const double* cval, const double* x, double* y,
@@ -105,8 +92,8 @@ cudaError_t launch_matvec_s32(int N, int ld, const float* S, const double* x, do
                               cudaStream_t s);
 cudaError_t launch_matvec_s32_t(int N, int ld, const float* S, const double* x, double* y,
                                 double* part, cudaStream_t s);
-cudaError_t launch_bj_build(int N, const double* Nm, const double* Dm, const float2* N2,
-                            const float2* D2, const uint8_t* mask, const double* alpha,
+cudaError_t launch_bj_build(int N, const double* Nm, const double* Dm, const float2* A2,
+                            const uint8_t* mask, const double* alpha,
                             const uint8_t* cflag, const int* cptr_full, const int* ccol_full,
                             const double* cval_full, double* binv, DevErr* err, cudaStream_t s);
 cudaError_t launch_bj_apply(int N, const double* binv, const double* x, double* y, int transpose,
@@ -123,30 +110,11 @@ cudaError_t launch_nrm2(int N, const double* x, double* part, double* out, cudaS
 cudaError_t launch_gather(int N, const int* idx, const double* x, double* y, cudaStream_t s);
 cudaError_t launch_scatter(int N, const int* idx, const double* x, double* y, cudaStream_t s);
 // out[r][q] = A[ip[r0 + r]][ip[q]] for r < nr (caller-order rows of an
-// internal-order matrix; A2 = (hi, lo) pairs when A is NULL)
+// internal-order matrix). When A is NULL the entry is read from the pairs:
+// sel_j ? -P1 : P0 (N: P0 = A2, P1 = B2; D: P0 = B2, P1 = A2)
 cudaError_t launch_gather_rows(int N, int r0, int nr, const int* ip, const double* A,
-                               const float2* A2, double* out, cudaStream_t s);
-
-// LU (mixed): FP32 no-pivot blocked LU with BF16x3 tensor-core trailing updates
-struct LuWork {
-  float* A;          // N x N row-major, in place
-  uint16_t* Lhi;     // panel splits (bf16 bits)
-  uint16_t* Llo;
-  uint16_t* Uhi;
-  uint16_t* Ulo;
-  int* info;
-};
-cudaError_t launch_form_lu_input(int N, const float2* N2, const float2* D2, const double* Nm,
-                                 const double* Dm, const uint8_t* mask, const double* alpha,
-                                 const uint8_t* cflag, const int* cptr_full, const int* ccol_full,
-                                 const double* cval_full, float* A, cudaStream_t s);
-int lu_factor_mixed(int N, LuWork& w, DevErr* err, cudaStream_t s, int* launches);
-cudaError_t launch_lu_solve(int N, const float* LU, const double* b, double* x, float* tmp,
-                            int transpose, cudaStream_t s);
-// tensor-core GEMM C -= A*B (BF16x3 split), exposed for tests
-cudaError_t launch_gemm_bf16x3(int M, int Ncols, int K, const uint16_t* Ahi, const uint16_t* Alo,
-                               int lda, const uint16_t* Bhi, const uint16_t* Blo, int ldb,
-                               float* Cm, int ldc, DevErr* err, cudaStream_t s);
+                               const float2* P0, const float2* P1, const uint8_t* sel, double* out,
+                               cudaStream_t s);
 
 // hull force and adjoint
 cudaError_t launch_hull_force(int nh, const int4* hull_dofs, const double* X, const double* U,

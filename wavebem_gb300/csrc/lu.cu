@@ -43,41 +43,34 @@ constexpr int kNB2 = 512;  // outer block: K of the tensor-core trailing update
 constexpr int kLookaheadSMs = 4;  // SMs the bulk trailing update leaves to the panel work
 
 // ------------------------------------------------------------------ input
-// LU input: hi part of the system operator, alpha on Neumann diagonals,
-// constrained rows replaced by e_i - sum_j c_ij e_j.
+// LU input: the system operator's pairs rounded to FP32 (A2: the boundary
+// condition is already applied), alpha on Neumann diagonals, constrained
+// rows replaced by e_i - sum_j c_ij e_j.
 __global__ void __launch_bounds__(256)
-    k_form_lu(int N, int ld, const float2* __restrict__ N2, const float2* __restrict__ D2,
-              const uint8_t* __restrict__ mask, const double* __restrict__ alpha,
-              const uint8_t* __restrict__ cflag, const int* __restrict__ cptr,
-              const int* __restrict__ ccol, const double* __restrict__ cval,
+    k_form_lu(int N, int ld, const float2* __restrict__ A2, const uint8_t* __restrict__ mask,
+              const double* __restrict__ alpha, const uint8_t* __restrict__ cflag,
               float* __restrict__ A) {
-  // one CTA per row, four consecutive columns per thread and step; a group
-  // of four columns with one boundary condition reads only the matrix it
-  // needs, as two 16-byte loads
+  // one CTA per row, four consecutive columns per thread and step (two
+  // 16-byte loads when the row start is 16-byte aligned)
   const int i = blockIdx.x;
   float* ar = A + (size_t)i * ld;
   if (cflag[i]) {
     for (int j = threadIdx.x; j < N; j += blockDim.x) ar[j] = (j == i) ? 1.f : 0.f;
     return;
   }
-  const float2* nr = N2 + (size_t)i * N;
-  const float2* dr = D2 + (size_t)i * N;
-  const bool vec = (N & 1) == 0;  // row starts 16-byte aligned
-  auto val = [&](int j, bool m, float2 v) -> float {
-    if (m) return -(float)((double)v.x + (double)v.y);
+  const float2* pr = A2 + (size_t)i * N;
+  const bool vec = (N & 1) == 0;
+  const double di = mask[i] ? 0.0 : alpha[i];
+  auto val = [&](int j, float2 v) -> float {
     double s = (double)v.x + (double)v.y;
-    if (j == i) s += alpha[i];
+    if (j == i) s += di;
     return (float)s;
   };
   for (int j = 4 * threadIdx.x; j < N; j += 4 * blockDim.x) {
     if (j + 3 < N) {
-      const uchar4 mk = *reinterpret_cast<const uchar4*>(mask + j);
-      const bool m[4] = {mk.x != 0, mk.y != 0, mk.z != 0, mk.w != 0};
       float2 e[4];
-      const bool alld = m[0] && m[1] && m[2] && m[3];
-      const bool alln = !(m[0] || m[1] || m[2] || m[3]);
-      if (vec && (alld || alln)) {
-        const float4* p = reinterpret_cast<const float4*>((alld ? dr : nr) + j);
+      if (vec) {
+        const float4* p = reinterpret_cast<const float4*>(pr + j);
         const float4 a = __ldcs(p), b = __ldcs(p + 1);
         e[0] = make_float2(a.x, a.y);
         e[1] = make_float2(a.z, a.w);
@@ -85,16 +78,12 @@ __global__ void __launch_bounds__(256)
         e[3] = make_float2(b.z, b.w);
       } else {
 #pragma unroll
-        for (int u = 0; u < 4; ++u) e[u] = __ldcs((m[u] ? dr : nr) + j + u);
+        for (int u = 0; u < 4; ++u) e[u] = __ldcs(pr + j + u);
       }
-      const float4 v = make_float4(val(j, m[0], e[0]), val(j + 1, m[1], e[1]), val(j + 2, m[2], e[2]),
-                                   val(j + 3, m[3], e[3]));
+      const float4 v = make_float4(val(j, e[0]), val(j + 1, e[1]), val(j + 2, e[2]), val(j + 3, e[3]));
       __stcs(reinterpret_cast<float4*>(ar + j), v);
     } else {
-      for (int u = 0; j + u < N; ++u) {
-        const bool m = mask[j + u] != 0;
-        ar[j + u] = val(j + u, m, __ldcs((m ? dr : nr) + j + u));
-      }
+      for (int u = 0; j + u < N; ++u) ar[j + u] = val(j + u, __ldcs(pr + j + u));
     }
   }
 }
@@ -1149,7 +1138,7 @@ int ensure_system_buffer(wbem_context* h) {
 // Completes the system matrix written by the assembly: the free term on the
 // Neumann diagonal (hi of N_ii + alpha_i), and the constrained rows, which
 // become e_i (their entries follow in k_lu_constraint_entries).
-__global__ void k_system_finish(int N, int ld, const float2* __restrict__ N2,
+__global__ void k_system_finish(int N, int ld, const float2* __restrict__ A2,
                                 const uint8_t* __restrict__ mask, const double* __restrict__ alpha,
                                 const uint8_t* __restrict__ cflag, float* __restrict__ A) {
   const int i = blockIdx.x;
@@ -1157,13 +1146,13 @@ __global__ void k_system_finish(int N, int ld, const float2* __restrict__ N2,
   if (cflag[i]) {
     for (int j = threadIdx.x; j < N; j += blockDim.x) ar[j] = (j == i) ? 1.f : 0.f;
   } else if (threadIdx.x == 0 && !mask[i]) {
-    const float2 n = N2[(size_t)i * N + i];
+    const float2 n = A2[(size_t)i * N + i];  // N_ii on a Neumann column
     ar[i] = (float)((double)n.x + (double)n.y + alpha[i]);
   }
 }
 
 int form_system_f32(wbem_context* h) {
-  if (!h->d_cflag || !h->d_cptr_full || !h->d_N2 || !h->d_D2 || !h->d_mask || !h->d_alpha)
+  if (!h->d_cflag || !h->d_cptr_full || !h->d_A2 || !h->d_mask || !h->d_alpha)
     return fail(h, WBEM_ERR_STATE, "system matrix: assembly, mask or constraints missing");
   const int N = h->N;
   const int ld = system_ld(N);
@@ -1173,12 +1162,11 @@ int form_system_f32(wbem_context* h) {
   }
   EvTimer tm(h->stream);
   if (h->s32_state == 1) {
-    k_system_finish<<<N, 128, 0, h->stream>>>(N, ld, h->d_N2, h->d_mask, h->d_alpha, h->d_cflag,
+    k_system_finish<<<N, 128, 0, h->stream>>>(N, ld, h->d_A2, h->d_mask, h->d_alpha, h->d_cflag,
                                                h->d_lu);
   } else {
     WB_CHK(ensure_system_buffer(h));
-    k_form_lu<<<N, 256, 0, h->stream>>>(N, ld, h->d_N2, h->d_D2, h->d_mask, h->d_alpha, h->d_cflag,
-                                        h->d_cptr_full, h->d_ccol_full, h->d_cval_full, h->d_lu);
+    k_form_lu<<<N, 256, 0, h->stream>>>(N, ld, h->d_A2, h->d_mask, h->d_alpha, h->d_cflag, h->d_lu);
   }
   WB_CU(cudaGetLastError());
   h->launches++;

@@ -60,14 +60,17 @@ __device__ __forceinline__ void q1_geo(const double P[4][3], double s, double t,
   cr[2] = jx[0] * je[1] - jx[1] * je[0];
 }
 
-// Optional FP32 copy of the system operator written during assembly: S_ij =
-// hi(N_ij) on Neumann columns, -hi(D_ij) on Dirichlet columns (row-major,
-// leading dimension ld). The diagonal free term and the constraint rows are
-// added at solve time.
+// Outputs of the mixed assembly. The entries are stored with the column's
+// boundary condition already applied (sel_j = 1: Dirichlet column):
+//   A2_ij = sel_j ? -D_ij : N_ij   (system operator, as vmult applies it)
+//   B2_ij = sel_j ? -N_ij : D_ij   (right-hand-side operator, compute_rhs)
+// as (hi, lo) float pairs, so that each mat-vec streams one matrix. Optional
+// FP32 copy S_ij = hi(A2_ij) (row-major, leading dimension ld); the diagonal
+// free term and the constraint rows are added at solve time.
 struct SysOut {
   float* S;                  // nullptr: not written
   int ld;
-  const uint8_t* mask;       // 1 = Dirichlet column
+  const uint8_t* sel;        // column selection of A2 / B2
 };
 
 // One thread per panel: FP64 geometry -> mixed record + near-test data.
@@ -164,8 +167,8 @@ __global__ void __launch_bounds__(kRowsPerTile)
     k_tile_mixed(int N, const double* __restrict__ X, const int* __restrict__ dnset,
                  const int* __restrict__ tile_ptr, const int2* __restrict__ tile_ent,
                  const int4* __restrict__ cell_dofs, const float* __restrict__ rec,
-                 const float4* __restrict__ cellgeo, float2* __restrict__ N2,
-                 float2* __restrict__ D2, double* __restrict__ alpha_part, SysOut so,
+                 const float4* __restrict__ cellgeo, float2* __restrict__ A2,
+                 float2* __restrict__ B2, double* __restrict__ alpha_part, SysOut so,
                  DevErr* err) {
   constexpr int NQ = Q1 * Q1;
   constexpr int RF = mixed_rec_floats(NQ);
@@ -392,9 +395,12 @@ __global__ void __launch_bounds__(kRowsPerTile)
     const int gr = row0 + rr, gc = col0 + cc;
     if (gr < N && gc < N) {
       const int o = cc * LDA + rr;
-      N2[(size_t)gr * N + gc] = make_float2(aNh[o], aNl[o]);
-      D2[(size_t)gr * N + gc] = make_float2(aDh[o], aDl[o]);
-      if (so.S) so.S[(size_t)gr * so.ld + gc] = so.mask[gc] ? -aDh[o] : aNh[o];
+      const bool dj = so.sel[gc] != 0;
+      const float2 a = dj ? make_float2(-aDh[o], -aDl[o]) : make_float2(aNh[o], aNl[o]);
+      const float2 b = dj ? make_float2(-aNh[o], -aNl[o]) : make_float2(aDh[o], aDl[o]);
+      A2[(size_t)gr * N + gc] = a;
+      B2[(size_t)gr * N + gc] = b;
+      if (so.S) so.S[(size_t)gr * so.ld + gc] = a.x;
     }
   }
 }
@@ -403,7 +409,7 @@ template <int Q1>
 static cudaError_t launch_tile_mixed_t(int N, const double* X, const int* dnset, int n_tiles,
                                        const int* tile_ptr, const int2* tile_ent,
                                        const int4* cell_dofs, const float* rec,
-                                       const float4* cellgeo, float2* N2, float2* D2,
+                                       const float4* cellgeo, float2* A2, float2* B2,
                                        double* alpha_part, SysOut so, DevErr* err, cudaStream_t s) {
   constexpr int RF = mixed_rec_floats(Q1 * Q1);
   const size_t acc = (size_t)kColsPerTile * (kRowsPerTile + 1);
@@ -414,7 +420,7 @@ static cudaError_t launch_tile_mixed_t(int N, const double* X, const int* dnset,
   if (e != cudaSuccess) return e;
   dim3 grid(n_tiles, (N + kRowsPerTile - 1) / kRowsPerTile);
   k_tile_mixed<Q1><<<grid, kRowsPerTile, smem, s>>>(N, X, dnset, tile_ptr, tile_ent, cell_dofs, rec,
-                                                    cellgeo, N2, D2, alpha_part, so, err);
+                                                    cellgeo, A2, B2, alpha_part, so, err);
   return cudaGetLastError();
 }
 
@@ -426,36 +432,36 @@ constexpr int kNearItems = 1024;  // per row: 4 items per near panel (256 panels
 constexpr int kSingItems = 128;  // per row: 4 items per singular panel
 constexpr int kItemCap = kNearItems + kSingItems;
 
-__device__ __forceinline__ void add_entry(float2* N2, float2* D2, SysOut so, int N, int row, int col,
+__device__ __forceinline__ void add_entry(float2* A2, float2* B2, SysOut so, int N, int row, int col,
                                           double dn, double dd) {
   const size_t o = (size_t)row * N + col;
-  float2 v = N2[o];
-  double s = (double)v.x + (double)v.y + dn;
+  const bool dj = so.sel[col] != 0;
+  float2 v = A2[o];
+  double s = (double)v.x + (double)v.y + (dj ? -dd : dn);
   float h = __double2float_rn(s);
-  N2[o] = make_float2(h, __double2float_rn(s - (double)h));
-  const float nh = h;
-  v = D2[o];
-  s = (double)v.x + (double)v.y + dd;
+  A2[o] = make_float2(h, __double2float_rn(s - (double)h));
+  if (so.S) so.S[(size_t)row * so.ld + col] = h;
+  v = B2[o];
+  s = (double)v.x + (double)v.y + (dj ? -dn : dd);
   h = __double2float_rn(s);
-  D2[o] = make_float2(h, __double2float_rn(s - (double)h));
-  if (so.S) so.S[(size_t)row * so.ld + col] = so.mask[col] ? -h : nh;
+  B2[o] = make_float2(h, __double2float_rn(s - (double)h));
 }
 
 // One thread per row: near items, then singular items, in order.
 __global__ void k_merge_items(int N, const int* __restrict__ cnt, const int* __restrict__ dof,
-                              const double2* __restrict__ val, float2* __restrict__ N2,
-                              float2* __restrict__ D2, SysOut so) {
+                              const double2* __restrict__ val, float2* __restrict__ A2,
+                              float2* __restrict__ B2, SysOut so) {
   const int row = blockIdx.x * blockDim.x + threadIdx.x;
   if (row >= N) return;
   const size_t base = (size_t)row * kItemCap;
   const int nn = min(cnt[2 * row], kNearItems), ns = min(cnt[2 * row + 1], kSingItems);
   for (int k = 0; k < nn; ++k) {
     const double2 v = val[base + k];
-    add_entry(N2, D2, so, N, row, dof[base + k], v.x, v.y);
+    add_entry(A2, B2, so, N, row, dof[base + k], v.x, v.y);
   }
   for (int k = 0; k < ns; ++k) {
     const double2 v = val[base + kNearItems + k];
-    add_entry(N2, D2, so, N, row, dof[base + kNearItems + k], v.x, v.y);
+    add_entry(A2, B2, so, N, row, dof[base + kNearItems + k], v.x, v.y);
   }
 }
 
@@ -683,8 +689,8 @@ __global__ void k_alpha_mixed(int N, int n_tiles, const double* __restrict__ par
 #define CHKM WB_CHK
 
 void free_mixed(wbem_context* h) {
-  if (h->d_N2) { cudaFree(h->d_N2); h->d_N2 = nullptr; }
-  if (h->d_D2) { cudaFree(h->d_D2); h->d_D2 = nullptr; }
+  if (h->d_A2) { cudaFree(h->d_A2); h->d_A2 = nullptr; }
+  if (h->d_B2) { cudaFree(h->d_B2); h->d_B2 = nullptr; }
   if (h->d_lu) { cudaFree(h->d_lu); h->d_lu = nullptr; }
   h->lu_elems = 0;
 }
@@ -707,9 +713,9 @@ int assemble_mixed(wbem_context* h) {
   const size_t nn = (size_t)N * N;
   if (h->d_N) { cudaFree(h->d_N); h->d_N = nullptr; }
   if (h->d_D) { cudaFree(h->d_D); h->d_D = nullptr; }
-  if (!h->d_N2 || h->mat_elems != nn) {
-    CHKM(dev_alloc(h, &h->d_N2, nn));
-    CHKM(dev_alloc(h, &h->d_D2, nn));
+  if (!h->d_A2 || h->mat_elems != nn) {
+    CHKM(dev_alloc(h, &h->d_A2, nn));
+    CHKM(dev_alloc(h, &h->d_B2, nn));
     h->mat_elems = nn;
   }
   if (!h->d_alpha) CHKM(dev_alloc(h, &h->d_alpha, (size_t)N));
@@ -731,10 +737,17 @@ int assemble_mixed(wbem_context* h) {
   h->stats.t_geometry_ms = tm.ms();
   const float4* geo = reinterpret_cast<const float4*>(h->d_cellgeo);
   // the FP32 system copy for the solvers, written alongside N and D
-  SysOut so{nullptr, 0, nullptr};
+  // the column selection of A2 / B2: the current mask (none yet: Neumann)
+  h->sel_mask.assign(N, 0);
+  if (h->have_mask)
+    for (int i = 0; i < N; ++i) h->sel_mask[i] = h->mask[h->perm[i]];
+  if (!h->d_selmask) CHKM(dev_alloc(h, &h->d_selmask, (size_t)N));
+  CUM(cudaMemcpyAsync(h->d_selmask, h->sel_mask.data(), (size_t)N, cudaMemcpyHostToDevice, h->stream));
+  SysOut so{nullptr, 0, h->d_selmask};
   if (h->have_mask && h->d_mask) {
     CHKM(ensure_system_buffer(h));
-    so = SysOut{h->d_lu, system_ld(N), h->d_mask};
+    so.S = h->d_lu;
+    so.ld = system_ld(N);
   }
   h->s32_state = 0;
   // near field and singular panels (FP64) on the auxiliary stream, beside the
@@ -778,18 +791,18 @@ int assemble_mixed(wbem_context* h) {
   }
   cudaError_t e;
   switch (q1) {
-    case 2: e = launch_tile_mixed_t<2>(N, h->d_X, h->d_dnset, h->n_tiles, h->d_tile_ptr, h->d_tile_ent, h->d_cell_dofs, h->d_rec32, geo, h->d_N2, h->d_D2, h->d_alpha_part, so, h->d_err, h->stream); break;
-    case 3: e = launch_tile_mixed_t<3>(N, h->d_X, h->d_dnset, h->n_tiles, h->d_tile_ptr, h->d_tile_ent, h->d_cell_dofs, h->d_rec32, geo, h->d_N2, h->d_D2, h->d_alpha_part, so, h->d_err, h->stream); break;
-    case 4: e = launch_tile_mixed_t<4>(N, h->d_X, h->d_dnset, h->n_tiles, h->d_tile_ptr, h->d_tile_ent, h->d_cell_dofs, h->d_rec32, geo, h->d_N2, h->d_D2, h->d_alpha_part, so, h->d_err, h->stream); break;
-    case 5: e = launch_tile_mixed_t<5>(N, h->d_X, h->d_dnset, h->n_tiles, h->d_tile_ptr, h->d_tile_ent, h->d_cell_dofs, h->d_rec32, geo, h->d_N2, h->d_D2, h->d_alpha_part, so, h->d_err, h->stream); break;
-    default: e = launch_tile_mixed_t<6>(N, h->d_X, h->d_dnset, h->n_tiles, h->d_tile_ptr, h->d_tile_ent, h->d_cell_dofs, h->d_rec32, geo, h->d_N2, h->d_D2, h->d_alpha_part, so, h->d_err, h->stream); break;
+    case 2: e = launch_tile_mixed_t<2>(N, h->d_X, h->d_dnset, h->n_tiles, h->d_tile_ptr, h->d_tile_ent, h->d_cell_dofs, h->d_rec32, geo, h->d_A2, h->d_B2, h->d_alpha_part, so, h->d_err, h->stream); break;
+    case 3: e = launch_tile_mixed_t<3>(N, h->d_X, h->d_dnset, h->n_tiles, h->d_tile_ptr, h->d_tile_ent, h->d_cell_dofs, h->d_rec32, geo, h->d_A2, h->d_B2, h->d_alpha_part, so, h->d_err, h->stream); break;
+    case 4: e = launch_tile_mixed_t<4>(N, h->d_X, h->d_dnset, h->n_tiles, h->d_tile_ptr, h->d_tile_ent, h->d_cell_dofs, h->d_rec32, geo, h->d_A2, h->d_B2, h->d_alpha_part, so, h->d_err, h->stream); break;
+    case 5: e = launch_tile_mixed_t<5>(N, h->d_X, h->d_dnset, h->n_tiles, h->d_tile_ptr, h->d_tile_ent, h->d_cell_dofs, h->d_rec32, geo, h->d_A2, h->d_B2, h->d_alpha_part, so, h->d_err, h->stream); break;
+    default: e = launch_tile_mixed_t<6>(N, h->d_X, h->d_dnset, h->n_tiles, h->d_tile_ptr, h->d_tile_ent, h->d_cell_dofs, h->d_rec32, geo, h->d_A2, h->d_B2, h->d_alpha_part, so, h->d_err, h->stream); break;
   }
   CUM(e);
   h->stats.t_assemble_ms = tm.ms();
   // join the near / singular work and add it to the far-field entries
   CUM(cudaStreamWaitEvent(h->stream, h->ev_aux_join, 0));
   k_merge_items<<<(N + 127) / 128, 128, 0, h->stream>>>(N, h->d_item_cnt, h->d_item_dof,
-                                                         h->d_item_val, h->d_N2, h->d_D2, so);
+                                                         h->d_item_val, h->d_A2, h->d_B2, so);
   CUM(cudaGetLastError());
   h->stats.t_singular_ms = tm.ms();
   k_alpha_mixed<<<(N + 255) / 256, 256, 0, h->stream>>>(N, h->n_tiles, h->d_alpha_part,

@@ -72,21 +72,19 @@ cudaError_t launch_matvec_fp64(int N, int mode, const double* Nm, const double* 
   return cudaGetLastError();
 }
 
-// Same operator with (hi, lo) float pairs: entry = hi + lo, products and sums
-// in double-float on FP32 units, x given in FP64 and split on the fly.
+// Same operator with (hi, lo) float pairs whose boundary-condition selection
+// was applied at assembly (P = A2 for mode 0, B2 for mode 1): one contiguous
+// matrix per apply. entry = hi + lo; products and sums in double-float on
+// FP32 units, x given in FP64 and split on the fly.
 __global__ void __launch_bounds__(kMvWarps * 32)
-    k_matvec_mixed(int N, int mode, const float2* __restrict__ N2, const float2* __restrict__ D2,
-                   const uint8_t* __restrict__ mask, const double* __restrict__ alpha,
-                   const double* __restrict__ x, double* __restrict__ y) {
+    k_matvec_mixed(int N, int mode, const float2* __restrict__ P, const uint8_t* __restrict__ mask,
+                   const double* __restrict__ alpha, const double* __restrict__ x,
+                   double* __restrict__ y) {
   __shared__ float2 xs[kMvChunk];
-  __shared__ uint8_t ms[kMvChunk];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int row = blockIdx.x * kMvWarps + warp;
   const bool active = row < N;
-  const float2* A0 = (mode == 0) ? N2 : D2;
-  const float2* A1 = (mode == 0) ? D2 : N2;
-  const float2* r0 = A0 + (size_t)(active ? row : 0) * N;
-  const float2* r1 = A1 + (size_t)(active ? row : 0) * N;
+  const float2* r0 = P + (size_t)(active ? row : 0) * N;
   df acc = {0.f, 0.f};
   for (int c0 = 0; c0 < N; c0 += kMvChunk) {
     const int cn = min(kMvChunk, N - c0);
@@ -94,18 +92,12 @@ __global__ void __launch_bounds__(kMvWarps * 32)
     for (int k = threadIdx.x; k < cn; k += blockDim.x) {
       const df v = df_from_double(x[c0 + k]);
       xs[k] = make_float2(v.hi, v.lo);
-      ms[k] = mask[c0 + k];
     }
     __syncthreads();
     if (active) {
 #pragma unroll 8
       for (int k = lane; k < cn; k += 32) {
-        const int j = c0 + k;
-        float2 a = ms[k] ? __ldcs(r1 + j) : __ldcs(r0 + j);
-        if (ms[k]) {
-          a.x = -a.x;
-          a.y = -a.y;
-        }
+        const float2 a = __ldcs(r0 + c0 + k);
         const float2 xv = xs[k];
         df p = two_prod(a.x, xv.x);
         p.lo = __fmaf_rn(a.x, xv.y, __fmaf_rn(a.y, xv.x, p.lo));
@@ -127,11 +119,10 @@ __global__ void __launch_bounds__(kMvWarps * 32)
   }
 }
 
-cudaError_t launch_matvec_mixed(int N, int mode, const float2* N2, const float2* D2,
-                                const uint8_t* mask, const double* alpha, const double* x,
-                                double* y, cudaStream_t s) {
-  k_matvec_mixed<<<(N + kMvWarps - 1) / kMvWarps, kMvWarps * 32, 0, s>>>(N, mode, N2, D2, mask,
-                                                                          alpha, x, y);
+cudaError_t launch_matvec_mixed(int N, int mode, const float2* P, const uint8_t* mask,
+                                const double* alpha, const double* x, double* y, cudaStream_t s) {
+  k_matvec_mixed<<<(N + kMvWarps - 1) / kMvWarps, kMvWarps * 32, 0, s>>>(N, mode, P, mask, alpha,
+                                                                          x, y);
   return cudaGetLastError();
 }
 
@@ -201,16 +192,18 @@ __device__ __forceinline__ double load_entry<float2>(const float2* p) {
   return (double)v.x + (double)v.y;
 }
 
+// sel: the column mask that picks N or -D (NULL: Nm already holds the
+// selected operator)
 template <typename T>
 __global__ void k_matvec_t(int N, const T* __restrict__ Nm, const T* __restrict__ Dm,
-                           const uint8_t* __restrict__ mask, const double* __restrict__ x,
+                           const uint8_t* __restrict__ sel, const double* __restrict__ x,
                            double* __restrict__ part) {
   const int col = blockIdx.x * kMvtCols + threadIdx.x;
   const int slice = blockIdx.y;
   const int rows_per = (N + kMvtSlices - 1) / kMvtSlices;
   const int r0 = slice * rows_per, r1 = min(N, r0 + rows_per);
   if (col >= N) return;
-  const bool m = mask[col] != 0;
+  const bool m = sel != nullptr && sel[col] != 0;
   const T* A = m ? Dm : Nm;
   double acc = 0.0;
   for (int i = r0; i < r1; ++i) acc = fma(load_entry<T>(A + (size_t)i * N + col), x[i], acc);
@@ -237,11 +230,10 @@ cudaError_t launch_matvec_t_fp64(int N, const double* Nm, const double* Dm, cons
   return cudaGetLastError();
 }
 
-cudaError_t launch_matvec_t_mixed(int N, const float2* N2, const float2* D2, const uint8_t* mask,
-                                  const double* alpha, const double* x, double* y, double* part,
-                                  cudaStream_t s) {
+cudaError_t launch_matvec_t_mixed(int N, const float2* P, const uint8_t* mask, const double* alpha,
+                                  const double* x, double* y, double* part, cudaStream_t s) {
   dim3 g((N + kMvtCols - 1) / kMvtCols, kMvtSlices);
-  k_matvec_t<float2><<<g, kMvtCols, 0, s>>>(N, N2, D2, mask, x, part);
+  k_matvec_t<float2><<<g, kMvtCols, 0, s>>>(N, P, P, nullptr, x, part);
   k_matvec_t_finish<<<(N + 255) / 256, 256, 0, s>>>(N, mask, alpha, x, part, y);
   return cudaGetLastError();
 }
@@ -342,8 +334,8 @@ cudaError_t launch_set_rows(int nrows, const int* crow, const double* val, doubl
 // (column k of the inverse contiguous) for coalesced application.
 __global__ void __launch_bounds__(kBJ)
     k_bj_build(int N, const double* __restrict__ Nm, const double* __restrict__ Dm,
-               const float2* __restrict__ N2, const float2* __restrict__ D2,
-               const uint8_t* __restrict__ mask, const double* __restrict__ alpha,
+               const float2* __restrict__ A2, const uint8_t* __restrict__ mask,
+               const double* __restrict__ alpha,
                const uint8_t* __restrict__ cflag, const int* __restrict__ cptr,
                const int* __restrict__ ccol, const double* __restrict__ cval,
                double* __restrict__ binv, DevErr* err) {
@@ -367,15 +359,8 @@ __global__ void __launch_bounds__(kBJ)
       v = (r == c) ? 1.0 : 0.0;
     } else {
       const size_t o = (size_t)i * N + j;
-      double nv, dv;
-      if (Nm) {
-        nv = Nm[o];
-        dv = Dm[o];
-      } else {
-        nv = (double)N2[o].x + (double)N2[o].y;
-        dv = (double)D2[o].x + (double)D2[o].y;
-      }
-      v = mask[j] ? -dv : nv;
+      if (Nm) v = mask[j] ? -Dm[o] : Nm[o];
+      else v = (double)A2[o].x + (double)A2[o].y;  // selected at assembly
       if (i == j && !mask[j]) v += alpha[i];
     }
     A[r * LD + c] = v;
@@ -443,8 +428,8 @@ __global__ void __launch_bounds__(kBJ)
   for (int c = 0; c < kBJ; ++c) out[(size_t)perm[c] * kBJ + r] = A[r * LD + c];
 }
 
-cudaError_t launch_bj_build(int N, const double* Nm, const double* Dm, const float2* N2,
-                            const float2* D2, const uint8_t* mask, const double* alpha,
+cudaError_t launch_bj_build(int N, const double* Nm, const double* Dm, const float2* A2,
+                            const uint8_t* mask, const double* alpha,
                             const uint8_t* cflag, const int* cptr_full, const int* ccol_full,
                             const double* cval_full, double* binv, DevErr* err, cudaStream_t s) {
   const size_t smem = (size_t)kBJ * (kBJ + 1) * sizeof(double);
@@ -452,7 +437,7 @@ cudaError_t launch_bj_build(int N, const double* Nm, const double* Dm, const flo
                                        (int)smem);
   if (e != cudaSuccess) return e;
   const int nb = (N + kBJ - 1) / kBJ;
-  k_bj_build<<<nb, kBJ, smem, s>>>(N, Nm, Dm, N2, D2, mask, alpha, cflag, cptr_full, ccol_full,
+  k_bj_build<<<nb, kBJ, smem, s>>>(N, Nm, Dm, A2, mask, alpha, cflag, cptr_full, ccol_full,
                                    cval_full, binv, err);
   return cudaGetLastError();
 }
@@ -598,26 +583,53 @@ cudaError_t launch_scatter(int N, const int* idx, const double* x, double* y, cu
   return cudaGetLastError();
 }
 
-// Caller-order rows of an internal-order matrix: out[r][q] = A[ip[r0+r]][ip[q]].
+// Caller-order rows of an internal-order matrix: out[r][q] = A[ip[r0+r]][ip[q]],
+// or from the selected pairs: sel_j ? -P1 : P0.
 __global__ void k_gather_rows(int N, int r0, const int* __restrict__ ip, const double* __restrict__ A,
-                              const float2* __restrict__ A2, double* __restrict__ out) {
+                              const float2* __restrict__ P0, const float2* __restrict__ P1,
+                              const uint8_t* __restrict__ sel, double* __restrict__ out) {
   const int r = blockIdx.y;
   const size_t src = (size_t)ip[r0 + r] * N;
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < N; q += gridDim.x * blockDim.x) {
+    const int j = ip[q];
     double v;
     if (A) {
-      v = A[src + ip[q]];
+      v = A[src + j];
+    } else if (sel[j]) {
+      const float2 t = P1[src + j];
+      v = -((double)t.x + (double)t.y);
     } else {
-      const float2 t = A2[src + ip[q]];
+      const float2 t = P0[src + j];
       v = (double)t.x + (double)t.y;
     }
     out[(size_t)r * N + q] = v;
   }
 }
 cudaError_t launch_gather_rows(int N, int r0, int nr, const int* ip, const double* A,
-                               const float2* A2, double* out, cudaStream_t s) {
+                               const float2* P0, const float2* P1, const uint8_t* sel, double* out,
+                               cudaStream_t s) {
   dim3 g(std::min(64, (N + 255) / 256), nr);
-  k_gather_rows<<<g, 256, 0, s>>>(N, r0, ip, A, A2, out);
+  k_gather_rows<<<g, 256, 0, s>>>(N, r0, ip, A, P0, P1, sel, out);
+  return cudaGetLastError();
+}
+
+// After a boundary-condition change of the columns flips[0..nflip): the
+// selected pairs swap roles, A2' = sel' ? -D : N = -B2 and B2' = -A2.
+__global__ void k_reselect_pairs(int N, int nflip, const int* __restrict__ flips,
+                                 float2* __restrict__ A2, float2* __restrict__ B2) {
+  const int i = blockIdx.y;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nflip; k += gridDim.x * blockDim.x) {
+    const size_t o = (size_t)i * N + flips[k];
+    const float2 a = A2[o], b = B2[o];
+    A2[o] = make_float2(-b.x, -b.y);
+    B2[o] = make_float2(-a.x, -a.y);
+  }
+}
+cudaError_t launch_reselect_pairs(int N, int nflip, const int* flips, float2* A2, float2* B2,
+                                  cudaStream_t s) {
+  if (nflip == 0) return cudaSuccess;
+  dim3 g(std::min(64, (nflip + 255) / 256), N);
+  k_reselect_pairs<<<g, 256, 0, s>>>(N, nflip, flips, A2, B2);
   return cudaGetLastError();
 }
 

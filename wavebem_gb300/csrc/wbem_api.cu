@@ -647,7 +647,7 @@ int apply_system(wbem_context* h, const double* x, double* y) {
     CU(launch_matvec_fp64(h->N, 0, h->d_N, h->d_D, h->d_mask, h->d_alpha, x, y, h->stream));
   else {
     if (h->profiling) h->prof_matvec.begin(h->stream);
-    CU(launch_matvec_mixed(h->N, 0, h->d_N2, h->d_D2, h->d_mask, h->d_alpha, x, y, h->stream));
+    CU(launch_matvec_mixed(h->N, 0, h->d_A2, h->d_mask, h->d_alpha, x, y, h->stream));
     if (h->profiling) h->prof_matvec.end(h->stream, 8.0 * (double)h->N * h->N);
   }
   CU(launch_constraint_rows(h->n_crows, h->d_crow, h->d_cptr, h->d_ccol, h->d_cval, x, y, h->stream));
@@ -669,7 +669,7 @@ int apply_system_t(wbem_context* h, const double* x, double* y) {
   if (h->assembled_prec == WBEM_PREC_FP64)
     CU(launch_matvec_t_fp64(h->N, h->d_N, h->d_D, h->d_mask, h->d_alpha, xz, y, part, h->stream));
   else
-    CU(launch_matvec_t_mixed(h->N, h->d_N2, h->d_D2, h->d_mask, h->d_alpha, xz, y, part, h->stream));
+    CU(launch_matvec_t_mixed(h->N, h->d_A2, h->d_mask, h->d_alpha, xz, y, part, h->stream));
   if (h->n_crows)
     CU(launch_constraint_rows_t(h->N, h->n_crows, h->d_crow, h->d_cptr, h->d_ccol, h->d_cval,
                                 h->d_tptr, h->d_tsrc, h->d_tval, h->d_cflag, x, y, h->stream));
@@ -835,7 +835,7 @@ int build_block_jacobi(wbem_context* h) {
   const int nb = (h->N + kBJ - 1) / kBJ;
   CHK(dev_alloc(h, &h->d_binv, (size_t)nb * kBJ * kBJ));
   const bool fp64 = h->assembled_prec == WBEM_PREC_FP64;
-  CU(launch_bj_build(h->N, fp64 ? h->d_N : nullptr, fp64 ? h->d_D : nullptr, h->d_N2, h->d_D2,
+  CU(launch_bj_build(h->N, fp64 ? h->d_N : nullptr, fp64 ? h->d_D : nullptr, h->d_A2,
                      h->d_mask, h->d_alpha, h->d_cflag, h->d_cptr_full, h->d_ccol_full,
                      h->d_cval_full, h->d_binv, h->d_err, h->stream));
   h->launches++;
@@ -1042,8 +1042,8 @@ int wbem_destroy(wbem_handle h) {
   free_lu(h);
   void* ptrs[] = {h->d_X, h->d_cell_dofs, h->d_dnset, h->d_tile_ptr, h->d_tile_ent, h->d_sptr,
                   h->d_scell, h->d_perm, h->d_iperm, h->d_ncptr, h->d_ncent, h->d_mask, h->d_rec,
-                  h->d_rec32, h->d_cellc, h->d_cellgeo, h->d_N, h->d_D, h->d_N2, h->d_D2,
-                  h->d_alpha, h->d_alpha_part, h->d_alpha_near, h->d_alpha_sing, h->d_near_cnt,
+                  h->d_rec32, h->d_cellc, h->d_cellgeo, h->d_N, h->d_D, h->d_A2, h->d_B2,
+                  h->d_selmask, h->d_flips, h->d_alpha, h->d_alpha_part, h->d_alpha_near, h->d_alpha_sing, h->d_near_cnt,
                   h->d_near_cells, h->d_item_val, h->d_item_dof, h->d_item_cnt,
                   h->d_crow, h->d_cptr, h->d_ccol, h->d_cval, h->d_cinh,
                   h->d_cflag, h->d_cptr_full, h->d_ccol_full, h->d_cval_full, h->d_tptr,
@@ -1158,6 +1158,25 @@ int wbem_set_bc(wbem_handle h, const unsigned char* m) {
   std::vector<uint8_t> mi(h->N);
   for (int i = 0; i < h->N; ++i) mi[i] = h->mask[h->perm[i]];
   CHK(upload(h, &h->d_mask, mi));
+  if (h->assembled_prec == WBEM_PREC_MIXED && h->d_A2 && (int)h->sel_mask.size() == h->N) {
+    // the mixed pairs carry the old selection: swap the changed columns
+    std::vector<int> flips;
+    for (int i = 0; i < h->N; ++i)
+      if (h->sel_mask[i] != mi[i]) flips.push_back(i);
+    if (!flips.empty()) {
+      if (h->flips_cap < flips.size()) {
+        CHK(dev_alloc(h, &h->d_flips, flips.size()));
+        h->flips_cap = flips.size();
+      }
+      CU(cudaMemcpyAsync(h->d_flips, flips.data(), sizeof(int) * flips.size(), cudaMemcpyHostToDevice,
+                         h->stream));
+      CU(launch_reselect_pairs(h->N, (int)flips.size(), h->d_flips, h->d_A2, h->d_B2, h->stream));
+      h->sel_mask = mi;
+      CU(cudaMemcpyAsync(h->d_selmask, h->sel_mask.data(), (size_t)h->N, cudaMemcpyHostToDevice,
+                         h->stream));
+      CU(cudaStreamSynchronize(h->stream));
+    }
+  }
   h->have_mask = true;
   h->factors_valid = false;
   h->have_solution = false;
@@ -1191,9 +1210,9 @@ int wbem_assemble(wbem_handle h, const wbem_options* opt) {
   if (o.precision == WBEM_PREC_FP64) {
     free_mixed(h);
     const size_t nn = (size_t)N * N;
-    if (!h->d_N || h->mat_elems != nn || h->d_N2) {
-      if (h->d_N2) { cudaFree(h->d_N2); h->d_N2 = nullptr; }
-      if (h->d_D2) { cudaFree(h->d_D2); h->d_D2 = nullptr; }
+    if (!h->d_N || h->mat_elems != nn || h->d_A2) {
+      if (h->d_A2) { cudaFree(h->d_A2); h->d_A2 = nullptr; }
+      if (h->d_B2) { cudaFree(h->d_B2); h->d_B2 = nullptr; }
       CHK(dev_alloc(h, &h->d_N, nn));
       CHK(dev_alloc(h, &h->d_D, nn));
       h->mat_elems = nn;
@@ -1234,7 +1253,7 @@ static int prepare_rhs(wbem_handle h, const double* tmp_rhs) {
   if (h->assembled_prec == WBEM_PREC_FP64)
     CU(launch_matvec_fp64(N, 1, h->d_N, h->d_D, h->d_mask, h->d_alpha, h->d_b, h->d_rhs, h->stream));
   else
-    CU(launch_matvec_mixed(N, 1, h->d_N2, h->d_D2, h->d_mask, h->d_alpha, h->d_b, h->d_rhs, h->stream));
+    CU(launch_matvec_mixed(N, 1, h->d_B2, h->d_mask, h->d_alpha, h->d_b, h->d_rhs, h->stream));
   CU(launch_set_rows(h->n_crows, h->d_crow, h->d_cinh, h->d_rhs, h->stream));
   h->launches += 2;
   CU(cudaStreamSynchronize(h->stream));
@@ -1308,10 +1327,12 @@ int wbem_get_matrices(wbem_handle h, double* neumann, double* dirichlet) {
     double* out = which == 0 ? neumann : dirichlet;
     if (!out) continue;
     const double* A = which == 0 ? h->d_N : h->d_D;
-    const float2* A2 = which == 0 ? h->d_N2 : h->d_D2;
+    // mixed: N = sel ? -B2 : A2, D = sel ? -A2 : B2
+    const float2* P0 = which == 0 ? h->d_A2 : h->d_B2;
+    const float2* P1 = which == 0 ? h->d_B2 : h->d_A2;
     for (int r0 = 0; r0 < N && st == WBEM_OK; r0 += rows_per) {
       const int nr = std::min(rows_per, N - r0);
-      cudaError_t e = launch_gather_rows(N, r0, nr, h->d_iperm, A, A2, buf, h->stream);
+      cudaError_t e = launch_gather_rows(N, r0, nr, h->d_iperm, A, P0, P1, h->d_selmask, buf, h->stream);
       if (e != cudaSuccess) st = fail(h, WBEM_ERR_CUDA, cudaGetErrorString(e));
       if (st == WBEM_OK) {
         e = cudaMemcpyAsync(out + (size_t)r0 * N, buf, sizeof(double) * (size_t)nr * N,
@@ -1339,7 +1360,8 @@ static int op_caller(wbem_handle h, int mode, const double* src, double* dst) {
   if (h->assembled_prec == WBEM_PREC_FP64)
     CU(launch_matvec_fp64(N, mode, h->d_N, h->d_D, h->d_mask, h->d_alpha, h->d_vec[3], h->d_vec[4], h->stream));
   else
-    CU(launch_matvec_mixed(N, mode, h->d_N2, h->d_D2, h->d_mask, h->d_alpha, h->d_vec[3], h->d_vec[4], h->stream));
+    CU(launch_matvec_mixed(N, mode, mode == 0 ? h->d_A2 : h->d_B2, h->d_mask, h->d_alpha, h->d_vec[3],
+                           h->d_vec[4], h->stream));
   CU(copy_sync(h, yi.data(), h->d_vec[4], sizeof(double) * N, cudaMemcpyDeviceToHost));
   for (int i = 0; i < N; ++i) dst[h->perm[i]] = yi[i];
   if (mode == 0) {
