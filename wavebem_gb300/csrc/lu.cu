@@ -183,8 +183,8 @@ __global__ void __launch_bounds__(kDiagThreads, 1)
       const int k = 16 * kb + s, k1 = k + 1;
       const int s1 = (s + 1) & 15, kb1 = kb + (s == 15 ? 1 : 0);
       const float* row = sRows + k * kDRowLD;
-      const float src = r > k ? sCol[(s & 1) * kNB + r] : sLZ[r * kDLD + k];
-      const float m = src * sInv[k];
+      const float* srcp = r > k ? sCol + (s & 1) * kNB + r : sLZ + r * kDLD + k;
+      const float m = *srcp * sInv[k];
 #pragma unroll
       for (int i = 0; i < 16; i += 4) {
         const float4 v = *reinterpret_cast<const float4*>(row + c0 + i);  // broadcast
@@ -214,8 +214,8 @@ __global__ void __launch_bounds__(kDiagThreads, 1)
         }
       }
       if (q == kb1 && r != k1) {  // column k+1: multipliers below, final Z column above
-        if (r > k1) sCol[((s + 1) & 1) * kNB + r] = w[s1];
-        else sLZ[r * kDLD + k1] = w[s1];
+        float* dst = r > k1 ? sCol + ((s + 1) & 1) * kNB + r : sLZ + r * kDLD + k1;
+        *dst = w[s1];
       }
       __syncthreads();
     }
