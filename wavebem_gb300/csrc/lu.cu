@@ -185,13 +185,17 @@ __global__ void __launch_bounds__(kDiagThreads, 1)
       const float* row = sRows + k * kDRowLD;
       const float* srcp = r > k ? sCol + (s & 1) * kNB + r : sLZ + r * kDLD + k;
       const float m = *srcp * sInv[k];
+      // a warp whose rows are all Z rows and whose columns are all left of
+      // the pivot holds only slots that are never read again: skip it
+      if (32 * g + 31 > k || c0 + 15 > k) {
 #pragma unroll
-      for (int i = 0; i < 16; i += 4) {
-        const float4 v = *reinterpret_cast<const float4*>(row + c0 + i);  // broadcast
-        w[i] = __fmaf_rn(-m, v.x, w[i]);
-        w[i + 1] = __fmaf_rn(-m, v.y, w[i + 1]);
-        w[i + 2] = __fmaf_rn(-m, v.z, w[i + 2]);
-        w[i + 3] = __fmaf_rn(-m, v.w, w[i + 3]);
+        for (int i = 0; i < 16; i += 4) {
+          const float4 v = *reinterpret_cast<const float4*>(row + c0 + i);  // broadcast
+          w[i] = __fmaf_rn(-m, v.x, w[i]);
+          w[i + 1] = __fmaf_rn(-m, v.y, w[i + 1]);
+          w[i + 2] = __fmaf_rn(-m, v.z, w[i + 2]);
+          w[i + 3] = __fmaf_rn(-m, v.w, w[i + 3]);
+        }
       }
       if (q == kb && r > k) {  // pivot slot of a row below: -l_rk; L keeps l_rk
         w[s] = -m;
