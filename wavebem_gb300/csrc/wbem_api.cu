@@ -77,16 +77,13 @@ static void gauss_legendre01(int n, std::vector<double>& x, std::vector<double>&
   for (int i = 0; i < n; ++i) {
     long double z = cosl(pi * (i + 0.75L) / (n + 0.5L)), dp = 1;
     for (int it = 0; it < 100; ++it) {
-      long double p0 = 1, p1 = z;
-      if (n == 1) p1 = z, p0 = 1;
+      // P_n(z) and P_{n-1}(z) by the three-term recurrence
       long double pn = (n == 0) ? 1 : z, pm = 1;
       for (int k = 2; k <= n; ++k) {
         long double pk = ((2 * k - 1) * z * pn - (k - 1) * pm) / k;
         pm = pn;
         pn = pk;
       }
-      (void)p0;
-      (void)p1;
       dp = n * (z * pn - pm) / (z * z - 1);
       long double dz = pn / dp;
       z -= dz;
