@@ -139,7 +139,10 @@ struct wbem_context {
   int* d_tptr = nullptr;   // transposed constraint entries (by column)
   int* d_tsrc = nullptr;
   double* d_tval = nullptr;
-  size_t cons_cap_rows = 0, cons_cap_ent = 0;
+  // host copy of the constraint structure last uploaded: a solve whose lines
+  // and entries are unchanged uploads only the inhomogeneities
+  std::vector<int> c_crow, c_cptr, c_ccol;
+  std::vector<double> c_cval;
 
   // ---- solver workspaces
   double* d_binv = nullptr;

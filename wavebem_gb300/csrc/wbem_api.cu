@@ -568,20 +568,31 @@ static int build_constraints(wbem_context* h, const double* tmp_rhs) {
   std::sort(rows.begin(), rows.end());
   std::vector<int> crow, cptr{0}, ccol;
   std::vector<double> cval, cinh;
-  std::vector<uint8_t> cflag(N, 0);
-  std::vector<int> cptr_full(N + 1, 0), ccol_full;
-  std::vector<double> cval_full;
-  std::vector<std::vector<std::pair<int, double>>> byrow(N);
   for (auto& r : rows) {
     crow.push_back(r.first);
-    cflag[r.first] = 1;
     cinh.push_back(c.inh[r.second]);
     for (auto& e : c.l[r.second]) {
       ccol.push_back(ip[e.first]);
       cval.push_back(e.second);
-      byrow[r.first].push_back({ip[e.first], e.second});
     }
     cptr.push_back((int)ccol.size());
+  }
+  h->n_crows = (int)crow.size();
+  if (h->d_cinh && h->d_cflag && crow == h->c_crow && cptr == h->c_cptr && ccol == h->c_ccol &&
+      cval == h->c_cval) {
+    // same lines and entries as the last upload (the usual case from one
+    // solve_system to the next): only the inhomogeneities change
+    if (!cinh.empty())
+      CU(copy_sync(h, h->d_cinh, cinh.data(), sizeof(double) * cinh.size(), cudaMemcpyHostToDevice));
+    return WBEM_OK;
+  }
+  std::vector<uint8_t> cflag(N, 0);
+  std::vector<int> cptr_full(N + 1, 0), ccol_full;
+  std::vector<double> cval_full;
+  std::vector<std::vector<std::pair<int, double>>> byrow(N);
+  for (size_t k = 0; k < crow.size(); ++k) {
+    cflag[crow[k]] = 1;
+    for (int e = cptr[k]; e < cptr[k + 1]; ++e) byrow[crow[k]].push_back({ccol[e], cval[e]});
   }
   for (int i = 0; i < N; ++i) {
     for (auto& e : byrow[i]) {
@@ -603,7 +614,6 @@ static int build_constraints(wbem_context* h, const double* tmp_rhs) {
     }
     tptr[j + 1] = (int)tsrc.size();
   }
-  h->n_crows = (int)crow.size();
   CHK(upload(h, &h->d_crow, crow));
   CHK(upload(h, &h->d_cptr, cptr));
   CHK(upload(h, &h->d_ccol, ccol));
@@ -616,6 +626,10 @@ static int build_constraints(wbem_context* h, const double* tmp_rhs) {
   CHK(upload(h, &h->d_tptr, tptr));
   CHK(upload(h, &h->d_tsrc, tsrc));
   CHK(upload(h, &h->d_tval, tval));
+  h->c_crow.swap(crow);
+  h->c_cptr.swap(cptr);
+  h->c_ccol.swap(ccol);
+  h->c_cval.swap(cval);
   return WBEM_OK;
 }
 
