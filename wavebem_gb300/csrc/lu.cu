@@ -985,11 +985,17 @@ __global__ void __launch_bounds__(kTriThreads)
         if (lane == 0) acc[warp * 16 + i] -= s2;
       }
     } else {
+      // four independent partial sums (the dot product is on the chain)
       const int c = tid & (kNB - 1), h = tid >> 7;
-      float s2 = 0.f;
+      float q0 = 0.f, q1 = 0.f, q2 = 0.f, q3 = 0.f;
 #pragma unroll
-      for (int i = 0; i < 64; ++i) s2 = __fmaf_rn(t[i], v[h + 2 * i], s2);
-      part[h * kNB + c] = s2;
+      for (int i = 0; i < 64; i += 4) {
+        q0 = __fmaf_rn(t[i], v[h + 2 * i], q0);
+        q1 = __fmaf_rn(t[i + 1], v[h + 2 * i + 2], q1);
+        q2 = __fmaf_rn(t[i + 2], v[h + 2 * i + 4], q2);
+        q3 = __fmaf_rn(t[i + 3], v[h + 2 * i + 6], q3);
+      }
+      part[h * kNB + c] = (q0 + q1) + (q2 + q3);
     }
     // prefetch the next block while the next flag is pending
     const int jn2 = j + jstep;
