@@ -50,6 +50,7 @@ def lib():
         L.orc_hull_force.argtypes = [C.c_int, dp, C.c_int, ip, C.c_int, dp, dp, dp]
         L.orc_hull_force.restype = C.c_double
         L.orc_num_threads.restype = C.c_int
+        L.orc_set_threads.argtypes = [C.c_int]
         _lib = L
     return _lib
 
@@ -188,3 +189,7 @@ class Problem:
 
 def num_threads():
     return lib().orc_num_threads()
+
+
+def set_threads(n):
+    lib().orc_set_threads(int(n))

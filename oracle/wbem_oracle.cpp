@@ -957,4 +957,14 @@ int orc_num_threads() {
 #endif
 }
 
+// Threads of the OpenMP row loops from here on (the CPU-baseline legs time
+// 1 thread and all host threads in one process).
+void orc_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+
 }  // extern "C"
