@@ -364,23 +364,22 @@ __global__ void __launch_bounds__(kRowsPerTile)
         if (sl != 255u) {
           // acc += k(c) M_j + (FP32 point sum): exact hi product, one
           // two_sum into the accumulator, everything else into its lo part
+          // (the pair is renormalised once, when it is written out)
           const float Mh = cd[12 + j], Ml = cd[16 + j];
           const int o = sl * LDA + tid;
           {
             const df p = two_prod(gR.hi, Mh);
             const float pl = __fmaf_rn(gR.hi, Ml, __fmaf_rn(gR.lo, Mh, p.lo));
             const df s2 = two_sum(aNh[o], p.hi);
-            const df a = fast_two_sum(s2.hi, s2.lo + (aNl[o] + (pl + lnv[j])));
-            aNh[o] = a.hi;
-            aNl[o] = a.lo;
+            aNh[o] = s2.hi;
+            aNl[o] = aNl[o] + (s2.lo + (pl + lnv[j]));
           }
           {
             const df p = two_prod(rinv.hi, Mh);
             const float pl = __fmaf_rn(rinv.hi, Ml, __fmaf_rn(rinv.lo, Mh, p.lo));
             const df s2 = two_sum(aDh[o], p.hi);
-            const df a = fast_two_sum(s2.hi, s2.lo + (aDl[o] + (pl + lsv[j])));
-            aDh[o] = a.hi;
-            aDl[o] = a.lo;
+            aDh[o] = s2.hi;
+            aDl[o] = aDl[o] + (s2.lo + (pl + lsv[j]));
           }
         }
       }
@@ -396,8 +395,9 @@ __global__ void __launch_bounds__(kRowsPerTile)
     if (gr < N && gc < N) {
       const int o = cc * LDA + rr;
       const bool dj = so.sel[gc] != 0;
-      const float2 a = dj ? make_float2(-aDh[o], -aDl[o]) : make_float2(aNh[o], aNl[o]);
-      const float2 b = dj ? make_float2(-aNh[o], -aNl[o]) : make_float2(aDh[o], aDl[o]);
+      const df en = two_sum(aNh[o], aNl[o]), ed = two_sum(aDh[o], aDl[o]);
+      const float2 a = dj ? make_float2(-ed.hi, -ed.lo) : make_float2(en.hi, en.lo);
+      const float2 b = dj ? make_float2(-en.hi, -en.lo) : make_float2(ed.hi, ed.lo);
       A2[(size_t)gr * N + gc] = a;
       B2[(size_t)gr * N + gc] = b;
       if (so.S) so.S[(size_t)gr * so.ld + gc] = a.x;
