@@ -617,18 +617,18 @@ cudaError_t launch_gather_rows(int N, int r0, int nr, const int* ip, const doubl
 // selected pairs swap roles, A2' = sel' ? -D : N = -B2 and B2' = -A2.
 __global__ void k_reselect_pairs(int N, int nflip, const int* __restrict__ flips,
                                  float2* __restrict__ A2, float2* __restrict__ B2) {
-  const int i = blockIdx.y;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nflip; k += gridDim.x * blockDim.x) {
-    const size_t o = (size_t)i * N + flips[k];
-    const float2 a = A2[o], b = B2[o];
-    A2[o] = make_float2(-b.x, -b.y);
-    B2[o] = make_float2(-a.x, -a.y);
-  }
+  for (int i = blockIdx.y; i < N; i += gridDim.y)
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nflip; k += gridDim.x * blockDim.x) {
+      const size_t o = (size_t)i * N + flips[k];
+      const float2 a = A2[o], b = B2[o];
+      A2[o] = make_float2(-b.x, -b.y);
+      B2[o] = make_float2(-a.x, -a.y);
+    }
 }
 cudaError_t launch_reselect_pairs(int N, int nflip, const int* flips, float2* A2, float2* B2,
                                   cudaStream_t s) {
   if (nflip == 0) return cudaSuccess;
-  dim3 g(std::min(64, (nflip + 255) / 256), N);
+  dim3 g(std::min(64, (nflip + 255) / 256), std::min(N, 65535));
   k_reselect_pairs<<<g, 256, 0, s>>>(N, nflip, flips, A2, B2);
   return cudaGetLastError();
 }
