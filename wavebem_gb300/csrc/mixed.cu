@@ -738,10 +738,11 @@ int assemble_mixed(wbem_context* h) {
   const float4* geo = reinterpret_cast<const float4*>(h->d_cellgeo);
   // the FP32 system copy for the solvers, written alongside N and D
   // the column selection of A2 / B2: the current mask (none yet: Neumann)
+  const bool new_sel = !h->d_selmask || h->sel_mask.size() != (size_t)N;
   h->sel_mask.assign(N, 0);
   if (h->have_mask)
     for (int i = 0; i < N; ++i) h->sel_mask[i] = h->mask[h->perm[i]];
-  if (!h->d_selmask) CHKM(dev_alloc(h, &h->d_selmask, (size_t)N));
+  if (new_sel) CHKM(dev_alloc(h, &h->d_selmask, (size_t)N));
   CUM(cudaMemcpyAsync(h->d_selmask, h->sel_mask.data(), (size_t)N, cudaMemcpyHostToDevice, h->stream));
   SysOut so{nullptr, 0, h->d_selmask};
   if (h->have_mask && h->d_mask) {
