@@ -114,3 +114,26 @@ def test_mixed_mask_change_after_assembly(solver):
     g.solve_system(phi, dphi, b)
     assert g.stats()["t_factor_ms"] == 0.0
     assert rel2(phi, phi_o) <= 1e-8 and rel2(dphi, dphi_o) <= 1e-8
+
+
+@pytest.mark.parametrize("prec", [PREC_MIXED, 0])
+def test_handle_reused_for_a_mesh_of_another_size(prec):
+    """One handle, two meshes of different size (the sphere after the tank):
+    every size-dependent device buffer is allocated anew."""
+    P1, m1, b1 = oracle_problem("wigley", 2000)
+    P2, m2, b2 = oracle_problem("sphere", 12)
+    g = BEMProblem(m1.X, m1.cells, m1.dirichlet, P1.dn_ptr, P1.dn_idx, precision=prec)
+    phi, dphi = b1.copy(), b1.copy()
+    g.solve(phi, dphi, b1)
+    g.set_geometry(m2.X, m2.cells, P2.dn_ptr, P2.dn_idx)
+    g.set_bc(m2.dirichlet)
+    phi_o, dphi_o, _ = P2.solve_system(b2)
+    phi, dphi = b2.copy(), b2.copy()
+    g.solve(phi, dphi, b2)
+    assert rel2(phi, phi_o) <= 1e-8 and rel2(dphi, dphi_o) <= 1e-8
+    g.set_geometry(m1.X, m1.cells, P1.dn_ptr, P1.dn_idx)  # and back
+    g.set_bc(m1.dirichlet)
+    phi_o, dphi_o, _ = P1.solve_system(b1)
+    phi, dphi = b1.copy(), b1.copy()
+    g.solve(phi, dphi, b1)
+    assert rel2(phi, phi_o) <= 1e-8 and rel2(dphi, dphi_o) <= 1e-8

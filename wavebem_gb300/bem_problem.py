@@ -125,6 +125,13 @@ class BEMProblem:
         if st != WBEM_OK:
             raise WBEMError(st, "wbem_create failed (no usable CUDA device?)")
         self.options = default_options(**options)
+        self.set_geometry(X, cells, dn_ptr, dn_idx)
+        if dirichlet is not None:
+            self.set_bc(dirichlet)
+
+    def set_geometry(self, X, cells, dn_ptr=None, dn_idx=None):
+        """A new mesh (support points, Q1 cells, double-node sets) for this
+        handle; a mesh of another size re-allocates the device buffers."""
         self.X = _f64(X).reshape(-1, 3)
         self.cells = np.ascontiguousarray(cells, dtype=np.int32).reshape(-1, 4)
         self.n_dofs = self.X.shape[0]
@@ -136,8 +143,6 @@ class BEMProblem:
             pp = pi = None
         self._check(self.L.wbem_set_geometry(self.h, self.X.ravel(), self.n_dofs, self.cells.ravel(),
                                              self.cells.shape[0], pp, pi))
-        if dirichlet is not None:
-            self.set_bc(dirichlet)
 
     # -- plumbing
     def _check(self, st):

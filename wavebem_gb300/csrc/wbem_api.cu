@@ -1046,24 +1046,61 @@ int wbem_create(wbem_handle* out, int device) {
   return WBEM_OK;
 }
 
+// Frees every device buffer whose size depends on the mesh (all but the
+// error word) and forgets the sizes, so that the next calls allocate for the
+// current mesh.
+static void release_mesh_buffers(wbem_context* h) {
+  cudaStreamSynchronize(h->stream);
+  free_lu(h);
+  void** ptrs[] = {(void**)&h->d_X, (void**)&h->d_cell_dofs, (void**)&h->d_dnset, (void**)&h->d_tile_ptr,
+                   (void**)&h->d_tile_ent, (void**)&h->d_sptr, (void**)&h->d_scell, (void**)&h->d_perm,
+                   (void**)&h->d_iperm, (void**)&h->d_ncptr, (void**)&h->d_ncent, (void**)&h->d_mask,
+                   (void**)&h->d_rec, (void**)&h->d_rec32, (void**)&h->d_cellc, (void**)&h->d_cellgeo,
+                   (void**)&h->d_N, (void**)&h->d_D, (void**)&h->d_A2, (void**)&h->d_B2,
+                   (void**)&h->d_selmask, (void**)&h->d_flips, (void**)&h->d_alpha,
+                   (void**)&h->d_alpha_part, (void**)&h->d_alpha_near, (void**)&h->d_alpha_sing,
+                   (void**)&h->d_near_cnt, (void**)&h->d_near_cells, (void**)&h->d_item_val,
+                   (void**)&h->d_item_dof, (void**)&h->d_item_cnt, (void**)&h->d_crow, (void**)&h->d_cptr,
+                   (void**)&h->d_ccol, (void**)&h->d_cval, (void**)&h->d_cinh, (void**)&h->d_cflag,
+                   (void**)&h->d_cptr_full, (void**)&h->d_ccol_full, (void**)&h->d_cval_full,
+                   (void**)&h->d_tptr, (void**)&h->d_tsrc, (void**)&h->d_tval, (void**)&h->d_binv,
+                   (void**)&h->d_V, (void**)&h->d_part, (void**)&h->d_small, (void**)&h->d_lu,
+                   (void**)&h->d_split, (void**)&h->d_lutmp, (void**)&h->d_info, (void**)&h->d_sol,
+                   (void**)&h->d_rhs, (void**)&h->d_b};
+  for (void** p : ptrs)
+    if (*p) {
+      cudaFree(*p);
+      *p = nullptr;
+    }
+  for (int k = 0; k < kNumVec; ++k)
+    if (h->d_vec[k]) {
+      cudaFree(h->d_vec[k]);
+      h->d_vec[k] = nullptr;
+    }
+  h->rec_cells = 0;
+  h->mat_elems = 0;
+  h->item_rows = 0;
+  h->near_cap = 0;
+  h->V_cap = 0;
+  h->lu_elems = 0;
+  h->flips_cap = 0;
+  h->s32_state = 0;
+  h->assembled_prec = -1;
+  h->factors_valid = false;
+  h->have_solution = false;
+  h->sel_mask.clear();
+  h->c_crow.clear();
+  h->c_cptr.clear();
+  h->c_ccol.clear();
+  h->c_cval.clear();
+  h->n_crows = 0;
+}
+
 int wbem_destroy(wbem_handle h) {
   if (!h) return WBEM_ERR_ARG;
   cudaSetDevice(h->device);
-  cudaStreamSynchronize(h->stream);
-  free_lu(h);
-  void* ptrs[] = {h->d_X, h->d_cell_dofs, h->d_dnset, h->d_tile_ptr, h->d_tile_ent, h->d_sptr,
-                  h->d_scell, h->d_perm, h->d_iperm, h->d_ncptr, h->d_ncent, h->d_mask, h->d_rec,
-                  h->d_rec32, h->d_cellc, h->d_cellgeo, h->d_N, h->d_D, h->d_A2, h->d_B2,
-                  h->d_selmask, h->d_flips, h->d_alpha, h->d_alpha_part, h->d_alpha_near, h->d_alpha_sing, h->d_near_cnt,
-                  h->d_near_cells, h->d_item_val, h->d_item_dof, h->d_item_cnt,
-                  h->d_crow, h->d_cptr, h->d_ccol, h->d_cval, h->d_cinh,
-                  h->d_cflag, h->d_cptr_full, h->d_ccol_full, h->d_cval_full, h->d_tptr,
-                  h->d_tsrc, h->d_tval, h->d_binv, h->d_V, h->d_part, h->d_small, h->d_lu,
-                  h->d_split, h->d_lutmp, h->d_info, h->d_sol, h->d_rhs, h->d_b, h->d_err};
-  for (void* p : ptrs)
-    if (p) cudaFree(p);
-  for (int k = 0; k < kNumVec; ++k)
-    if (h->d_vec[k]) cudaFree(h->d_vec[k]);
+  release_mesh_buffers(h);
+  if (h->d_err) cudaFree(h->d_err);
   if (h->aux_stream) cudaStreamDestroy(h->aux_stream);
   if (h->ev_aux_fork) cudaEventDestroy(h->ev_aux_fork);
   if (h->ev_aux_join) cudaEventDestroy(h->ev_aux_join);
@@ -1097,6 +1134,8 @@ int wbem_set_geometry(wbem_handle h, const double* X, int n_dofs, const int* cel
         if (cells[4 * c + a] == cells[4 * c + b])
           return fail(h, WBEM_ERR_ARG, "wbem_set_geometry: repeated vertex in a cell");
   cudaSetDevice(h->device);
+  // a mesh of another size: every size-dependent buffer is allocated anew
+  if (h->N != 0 && (h->N != n_dofs || h->C != n_cells)) release_mesh_buffers(h);
   h->N = n_dofs;
   h->C = n_cells;
   h->X.assign(X, X + 3 * (size_t)n_dofs);
