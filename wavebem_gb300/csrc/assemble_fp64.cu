@@ -226,12 +226,13 @@ __global__ void __launch_bounds__(kRowsPerTile)
     __syncthreads();
   }
 
-  // coalesced write-out of the tile (row-major N x N)
-  const int col0 = tile * CT;
+  // coalesced write-out of the tile (row-major N x N); the tile's columns:
+  // tile_ptr[gridDim.x + 1 + tile] .. (+ 1)
+  const int col0 = tile_ptr[gridDim.x + 1 + tile], ncol = tile_ptr[gridDim.x + 2 + tile] - col0;
   for (int idx = tid; idx < RT * CT; idx += RT) {
     const int rr = idx / CT, cc = idx % CT;
     const int gr = row0 + rr, gc = col0 + cc;
-    if (gr < N && gc < N) {
+    if (gr < N && cc < ncol) {
       Nm[(size_t)gr * N + gc] = accN[cc * LDA + rr];
       Dm[(size_t)gr * N + gc] = accD[cc * LDA + rr];
     }

@@ -388,11 +388,12 @@ __global__ void __launch_bounds__(kRowsPerTile)
     __syncthreads();
   }
   if (active) alpha_part[(size_t)tile * N + row] = df_to_double(alpha_acc);
-  const int col0 = tile * CT;
+  // the tile's columns: tile_ptr[gridDim.x + 1 + tile] .. (+ 1)
+  const int col0 = tile_ptr[gridDim.x + 1 + tile], ncol = tile_ptr[gridDim.x + 2 + tile] - col0;
   for (int idx = tid; idx < RT * CT; idx += RT) {
     const int rr = idx / CT, cc = idx % CT;
     const int gr = row0 + rr, gc = col0 + cc;
-    if (gr < N && gc < N) {
+    if (gr < N && cc < ncol) {
       const int o = cc * LDA + rr;
       const bool dj = so.sel[gc] != 0;
       const df en = two_sum(aNh[o], aNl[o]), ed = two_sum(aDh[o], aDl[o]);
@@ -466,7 +467,7 @@ __global__ void k_merge_items(int N, const int* __restrict__ cnt, const int* __r
 }
 
 // Candidate panels of the near field per block of kNearBlock consecutive
-// rows (a compact patch in the Morton order): those whose near sphere can
+// rows (compact surface patches, see the internal dof order): those whose near sphere can
 // reach any row of the block, |centre_block - centre_panel| < r_block +
 // r_panel, in ascending panel order (ballot prefix sums, deterministic). A
 // list that would overflow kNearCap is marked with cnt = -1 and its rows scan

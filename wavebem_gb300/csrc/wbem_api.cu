@@ -214,8 +214,8 @@ static uint64_t spread21(uint64_t v) {
   return v;
 }
 
-// Internal dof order: Morton (Z-order) of the support points, so that a tile
-// of consecutive dofs is a compact patch of the surface.
+// Morton (Z-order) of the support points: the seed order of the patches
+// below.
 static void morton_order(int N, const double* X, std::vector<int>& perm, std::vector<int>& iperm) {
   double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
   for (int i = 0; i < N; ++i)
@@ -244,34 +244,93 @@ static void morton_order(int N, const double* X, std::vector<int>& perm, std::ve
   }
 }
 
+// Internal dof order in surface patches of at most ct nodes: each patch
+// grows breadth-first over the mesh graph (nodes sharing a cell) from the
+// first node not yet taken in the Morton order, so consecutive patches stay
+// close in space. A patch is a column tile of the assembly: BFS patches are
+// rounder than runs of the Morton order, so fewer panels straddle two tiles
+// (measured on the 32,768-dof tank: 1.33 tiles per panel against 1.47).
+// tstart[t] is the first internal dof of patch t, tstart[T] = N.
+static void patch_order(int N, const double* X, int C, const int* cells, int ct, std::vector<int>& perm,
+                        std::vector<int>& iperm, std::vector<int>& tstart) {
+  std::vector<int> seed, seedinv;
+  morton_order(N, X, seed, seedinv);
+  std::vector<int> aptr(N + 1, 0), adj;
+  {
+    std::vector<std::pair<int, int>> e;
+    e.reserve((size_t)C * 12);
+    for (int c = 0; c < C; ++c)
+      for (int a = 0; a < 4; ++a)
+        for (int b = 0; b < 4; ++b)
+          if (a != b) e.push_back({cells[4 * c + a], cells[4 * c + b]});
+    std::sort(e.begin(), e.end());
+    e.erase(std::unique(e.begin(), e.end()), e.end());
+    for (auto& p : e) aptr[p.first + 1]++;
+    for (int i = 0; i < N; ++i) aptr[i + 1] += aptr[i];
+    adj.resize(e.size());
+    for (size_t k = 0; k < e.size(); ++k) adj[k] = e[k].second;  // sorted by first, then second
+  }
+  std::vector<char> taken(N, 0);
+  perm.clear();
+  perm.reserve(N);
+  tstart.assign(1, 0);
+  size_t next = 0;
+  while ((int)perm.size() < N) {
+    while (taken[seed[next]]) ++next;
+    const int s = seed[next];
+    taken[s] = 1;
+    perm.push_back(s);
+    size_t head = perm.size() - 1;
+    int got = 1;
+    while (head < perm.size() && got < ct) {
+      const int u = perm[head++];
+      for (int k = aptr[u]; k < aptr[u + 1] && got < ct; ++k) {
+        const int v = adj[k];
+        if (!taken[v]) {
+          taken[v] = 1;
+          perm.push_back(v);
+          ++got;
+        }
+      }
+    }
+    tstart.push_back((int)perm.size());
+  }
+  iperm.resize(N);
+  for (int i = 0; i < N; ++i) iperm[perm[i]] = i;
+}
+
 static int build_topology(wbem_context* h) {
   const int N = h->N, C = h->C;
-  morton_order(N, h->X.data(), h->perm, h->iperm);
+  const int CT = kColsPerTile;
+  std::vector<int> tstart;
+  patch_order(N, h->X.data(), C, h->cells.data(), CT, h->perm, h->iperm, tstart);
   const auto& ip = h->iperm;
   // cell dofs (internal)
   std::vector<int4> cd(C);
   for (int c = 0; c < C; ++c)
     cd[c] = make_int4(ip[h->cells[4 * c]], ip[h->cells[4 * c + 1]], ip[h->cells[4 * c + 2]],
                       ip[h->cells[4 * c + 3]]);
-  // column tiles
-  const int CT = kColsPerTile;
-  h->n_tiles = (N + CT - 1) / CT;
+  // column tiles = the patches
+  h->n_tiles = (int)tstart.size() - 1;
+  std::vector<int> tile_of(N);
+  for (int t = 0; t < h->n_tiles; ++t)
+    for (int i = tstart[t]; i < tstart[t + 1]; ++i) tile_of[i] = t;
   std::vector<std::vector<int2>> tl(h->n_tiles);
   for (int c = 0; c < C; ++c) {
     const int d[4] = {cd[c].x, cd[c].y, cd[c].z, cd[c].w};
     int tiles[4];
     int nt = 0;
     for (int k = 0; k < 4; ++k) {
-      int t = d[k] / CT;
+      int t = tile_of[d[k]];
       bool seen = false;
       for (int u = 0; u < nt; ++u) seen |= tiles[u] == t;
       if (!seen) tiles[nt++] = t;
     }
-    const int owner = d[0] / CT;
+    const int owner = tile_of[d[0]];
     for (int u = 0; u < nt; ++u) {
       uint32_t slots = 0;
       for (int k = 0; k < 4; ++k) {
-        uint32_t sl = (d[k] / CT == tiles[u]) ? (uint32_t)(d[k] % CT) : 255u;
+        uint32_t sl = (tile_of[d[k]] == tiles[u]) ? (uint32_t)(d[k] - tstart[tiles[u]]) : 255u;
         slots |= sl << (8 * k);
       }
       int2 e;
@@ -280,12 +339,15 @@ static int build_topology(wbem_context* h) {
       tl[tiles[u]].push_back(e);
     }
   }
+  // tile_ptr: [0, T] entry offsets, then [T + 1, 2T + 1] the tiles' first
+  // columns (tstart); the tile kernels find the second half at gridDim.x + 1
   std::vector<int> tptr(h->n_tiles + 1, 0);
   std::vector<int2> tent;
   for (int t = 0; t < h->n_tiles; ++t) {
     tent.insert(tent.end(), tl[t].begin(), tl[t].end());
     tptr[t + 1] = (int)tent.size();
   }
+  tptr.insert(tptr.end(), tstart.begin(), tstart.end());
   // double-node sets (internal)
   std::vector<int> dnset((size_t)N * kMaxSet, -1);
   for (int p = 0; p < N; ++p) {
