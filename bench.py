@@ -440,7 +440,7 @@ def run_gpu(args, rank, world, local):
             kernels[-1]["fp32_roof"] = {
                 "achieved": t, "peak": fp32, "unit": "TFLOP/s", "frac": t / fp32,
                 "work": "36 flop per regular kernel evaluation x 16 N C (plain evaluation count; the "
-                        "double-float panel term and the 1.48x column-tile redundancy are not counted)",
+                        "double-float panel term and the 1.33x column-tile redundancy are not counted)",
                 "peak_source": "FP32 FMA loop (wbem_peak_probe) on this GPU"}
         if kprof["matvec_ms"] > 0:
             a = kprof["matvec_bytes"] / (kprof["matvec_ms"] / 1e3) / 1e9
