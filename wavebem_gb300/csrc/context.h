@@ -113,6 +113,12 @@ struct wbem_context {
   size_t item_rows = 0;
   cudaStream_t aux_stream = nullptr;
   cudaEvent_t ev_aux_fork = nullptr, ev_aux_join = nullptr;
+  // right-hand side computed on rhs_stream (lowest priority: it fills the
+  // SMs the factorisation leaves idle) beside the factorisation; the Krylov
+  // solve waits for ev_rhs when rhs_pending
+  cudaStream_t rhs_stream = nullptr;
+  cudaEvent_t ev_rhs = nullptr;
+  bool rhs_pending = false;
   int* d_near_cnt = nullptr;
   int* d_near_cells = nullptr;
   int near_cap = 0;

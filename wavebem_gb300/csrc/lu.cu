@@ -1148,17 +1148,22 @@ int ensure_system_buffer(wbem_context* h) {
 // Completes the system matrix written by the assembly: the free term on the
 // Neumann diagonal (hi of N_ii + alpha_i), and the constrained rows, which
 // become e_i (their entries follow in k_lu_constraint_entries).
-__global__ void k_system_finish(int N, int ld, const float2* __restrict__ A2,
-                                const uint8_t* __restrict__ mask, const double* __restrict__ alpha,
-                                const uint8_t* __restrict__ cflag, float* __restrict__ A) {
-  const int i = blockIdx.x;
+// The free term on the Neumann diagonals of the unconstrained rows, one
+// thread per row (the assembly wrote every other entry).
+__global__ void k_system_diag(int N, int ld, const float2* __restrict__ A2,
+                              const uint8_t* __restrict__ mask, const double* __restrict__ alpha,
+                              const uint8_t* __restrict__ cflag, float* __restrict__ A) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N || cflag[i] || mask[i]) return;
+  const float2 n = A2[(size_t)i * N + i];  // N_ii on a Neumann column
+  A[(size_t)i * ld + i] = (float)((double)n.x + (double)n.y + alpha[i]);
+}
+
+// Constrained rows: identity part, one CTA per constrained row.
+__global__ void k_system_crows(int N, int ld, const int* __restrict__ crow, float* __restrict__ A) {
+  const int i = crow[blockIdx.x];
   float* ar = A + (size_t)i * ld;
-  if (cflag[i]) {
-    for (int j = threadIdx.x; j < N; j += blockDim.x) ar[j] = (j == i) ? 1.f : 0.f;
-  } else if (threadIdx.x == 0 && !mask[i]) {
-    const float2 n = A2[(size_t)i * N + i];  // N_ii on a Neumann column
-    ar[i] = (float)((double)n.x + (double)n.y + alpha[i]);
-  }
+  for (int j = threadIdx.x; j < N; j += blockDim.x) ar[j] = (j == i) ? 1.f : 0.f;
 }
 
 int form_system_f32(wbem_context* h) {
@@ -1172,8 +1177,13 @@ int form_system_f32(wbem_context* h) {
   }
   EvTimer tm(h->stream);
   if (h->s32_state == 1) {
-    k_system_finish<<<N, 128, 0, h->stream>>>(N, ld, h->d_A2, h->d_mask, h->d_alpha, h->d_cflag,
-                                               h->d_lu);
+    k_system_diag<<<(N + 255) / 256, 256, 0, h->stream>>>(N, ld, h->d_A2, h->d_mask, h->d_alpha,
+                                                          h->d_cflag, h->d_lu);
+    if (h->n_crows > 0) {
+      WB_CU(cudaGetLastError());
+      k_system_crows<<<h->n_crows, 256, 0, h->stream>>>(N, ld, h->d_crow, h->d_lu);
+      h->launches++;
+    }
   } else {
     WB_CHK(ensure_system_buffer(h));
     k_form_lu<<<N, 256, 0, h->stream>>>(N, ld, h->d_A2, h->d_mask, h->d_alpha, h->d_cflag, h->d_lu);

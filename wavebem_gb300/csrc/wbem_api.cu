@@ -1033,6 +1033,10 @@ int solve_assembled(wbem_context* h, const double* rhs, double* x, int transpose
     h->stats.t_factor_ms = 0.0;
   }
   h->stats.outer_iterations = 0;
+  if (h->rhs_pending) {  // the right-hand side computed beside the preparation
+    CU(cudaStreamWaitEvent(h->stream, h->ev_rhs, 0));
+    h->rhs_pending = false;
+  }
   if (solver == WBEM_SOLVER_GMRES) return gmres_fp64(h, rhs, x, transpose);
   if (solver == WBEM_SOLVER_LU) return solve_mixed(h, rhs, x, transpose);
   return gmres_ir(h, rhs, x, transpose);
@@ -1166,6 +1170,8 @@ int wbem_destroy(wbem_handle h) {
   if (h->aux_stream) cudaStreamDestroy(h->aux_stream);
   if (h->ev_aux_fork) cudaEventDestroy(h->ev_aux_fork);
   if (h->ev_aux_join) cudaEventDestroy(h->ev_aux_join);
+  if (h->ev_rhs) cudaEventDestroy(h->ev_rhs);
+  if (h->rhs_stream) cudaStreamDestroy(h->rhs_stream);
   if (h->own_stream) cudaStreamDestroy(h->stream);
   delete h;
   return WBEM_OK;
@@ -1355,20 +1361,39 @@ int wbem_assemble(wbem_handle h, const wbem_options* opt) {
   return WBEM_OK;
 }
 
-static int prepare_rhs(wbem_handle h, const double* tmp_rhs) {
-  // known data in internal order, rhs = compute_rhs(tmp_rhs), constraints
+// Known data in internal order, rhs = compute_rhs(tmp_rhs), constraints.
+// beside = true: the mat-vec runs on a low-priority stream, beside whatever
+// the caller queues next on the handle's stream (the factorisation); the
+// Krylov solve waits for it (rhs_pending / ev_rhs).
+static int prepare_rhs(wbem_handle h, const double* tmp_rhs, bool beside = false) {
   const int N = h->N;
   CHK(build_constraints(h, tmp_rhs));
   std::vector<double> bi(N);
   for (int i = 0; i < N; ++i) bi[i] = tmp_rhs[h->perm[i]];
   CU(cudaMemcpyAsync(h->d_b, bi.data(), sizeof(double) * N, cudaMemcpyHostToDevice, h->stream));
+  cudaStream_t rs = h->stream;
+  if (beside) {
+    if (!h->rhs_stream) {
+      int lo = 0, hi = 0;
+      CU(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+      CU(cudaStreamCreateWithPriority(&h->rhs_stream, cudaStreamNonBlocking, lo));
+      CU(cudaEventCreateWithFlags(&h->ev_rhs, cudaEventDisableTiming));
+    }
+    CU(cudaEventRecord(h->ev_rhs, h->stream));
+    CU(cudaStreamWaitEvent(h->rhs_stream, h->ev_rhs, 0));
+    rs = h->rhs_stream;
+  }
   if (h->assembled_prec == WBEM_PREC_FP64)
-    CU(launch_matvec_fp64(N, 1, h->d_N, h->d_D, h->d_mask, h->d_alpha, h->d_b, h->d_rhs, h->stream));
+    CU(launch_matvec_fp64(N, 1, h->d_N, h->d_D, h->d_mask, h->d_alpha, h->d_b, h->d_rhs, rs));
   else
-    CU(launch_matvec_mixed(N, 1, h->d_B2, h->d_mask, h->d_alpha, h->d_b, h->d_rhs, h->stream));
-  CU(launch_set_rows(h->n_crows, h->d_crow, h->d_cinh, h->d_rhs, h->stream));
+    CU(launch_matvec_mixed(N, 1, h->d_B2, h->d_mask, h->d_alpha, h->d_b, h->d_rhs, rs));
+  CU(launch_set_rows(h->n_crows, h->d_crow, h->d_cinh, h->d_rhs, rs));
   h->launches += 2;
-  CU(cudaStreamSynchronize(h->stream));
+  if (rs != h->stream) {
+    CU(cudaEventRecord(h->ev_rhs, rs));
+    h->rhs_pending = true;
+  }
+  CU(cudaStreamSynchronize(h->stream));  // bi is read by the copy above
   return WBEM_OK;
 }
 
@@ -1388,7 +1413,7 @@ int wbem_solve_system(wbem_handle h, const double* tmp_rhs, double* phi, double*
   cudaSetDevice(h->device);
   CHK(ensure_vectors(h, h->opt.gmres_restart));
   Timer tm(h->stream);
-  CHK(prepare_rhs(h, tmp_rhs));
+  CHK(prepare_rhs(h, tmp_rhs, /*beside=*/true));
   const double t_rhs = tm.ms();
   CHK(solve_assembled(h, h->d_rhs, h->d_sol, 0));
   // right-hand side + Krylov iterations, without the preconditioner set-up
