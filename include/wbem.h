@@ -102,7 +102,9 @@ const char* wbem_last_error(wbem_handle h);
  * ComputationalDomain: dh/fe/mapping support points, cell dof indices and
  * double_nodes_set (source/bem_problem.cc:168-169, :223-230). dn_ptr/dn_idx
  * may be NULL, in which case the library finds the double nodes itself with
- * the reference's rule (boundary dofs, coincidence below 1e-8).
+ * the reference's rule (boundary dofs, coincidence below 1e-8). A handle may
+ * be given a new mesh at any time; the previous assembly is discarded, and a
+ * mesh of another size re-allocates the handle's device buffers.
  */
 int wbem_set_geometry(wbem_handle h, const double* X, int n_dofs, const int* cells, int n_cells,
                       const int* dn_ptr, const int* dn_idx);
