@@ -232,6 +232,12 @@ NCU_TRAFFIC = {
 }
 
 
+# Warp instructions of one far-field assembly launch at N = 8,192 (ncu
+# smsp__inst_executed.sum, profiles/k_tile_mixed_n8192.md); they scale with
+# the (row, panel) pairs, i.e. with N^2 on the same family of meshes.
+NCU_TILE_INSTR = 2677553771.0
+
+
 def ncu_traffic(kernel, n):
     """(bytes per launch at n dofs, how it was obtained) or (None, None)."""
     t = NCU_TRAFFIC.get(kernel)
@@ -432,6 +438,17 @@ def run_gpu(args, rank, world, local):
                                 "(row, panel) pair), not by HBM: ncu IPC 2.9 of 4, FMA pipe 54% "
                                 "(profiles/k_tile_mixed_n8192.md)",
                         "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({src})"})
+        sm_mhz = (clk or {}).get("sm_mhz")
+        if sm_mhz:
+            # instruction issue: 4 warp instructions per SM per clock at most
+            import torch
+            sms = torch.cuda.get_device_properties(local).multi_processor_count
+            ins = NCU_TILE_INSTR * (N / 8192.0) ** 2 / (kprof["tile_ms"] / 1e3)
+            pk = 4.0 * sms * sm_mhz * 1e6
+            kernels[-1]["issue_roof"] = {
+                "achieved": ins / 1e12, "peak": pk / 1e12, "unit": "T warp-instr/s", "frac": ins / pk,
+                "work": "warp instructions of one launch from the N = 8,192 ncu capture, scaled by (N / 8192)^2",
+                "peak_source": "4 per SM per clock at the median SM clock sampled during the timed region"}
         fp32 = fp32_peak_tflops()
         if fp32:
             # the survey's convention: 36 flop per regular kernel evaluation,
