@@ -538,6 +538,7 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int 
 // granularity: Nc is a multiple of 32 or reaches the matrix edge); rows past
 // the matrix edge are clipped by the tensor map.
 constexpr int G3M = 128, G3N = 256, G3K = 32, G3S = 3;
+constexpr int G3CB = 2;  // C chunk buffers per epilogue group
 constexpr uint32_t kA3 = G3M * G3K * 2;                  // 8 KB
 constexpr uint32_t kB3 = G3N * G3K * 2;                  // 16 KB
 constexpr uint32_t kStage3 = 2 * kA3 + 2 * kB3;          // 48 KB
@@ -577,13 +578,13 @@ __global__ void __launch_bounds__(kG3Threads, 1)
   const uint32_t base_s = smem_u32(g3sm);
   const uint32_t pad = (1024 - (base_s & 1023)) & 1023;
   uint8_t* sm = g3sm + pad;                    // [G3S stages][Ahi Alo Bhi Blo]
-  uint8_t* csm = sm + G3S * kStage3;           // [2 groups][2] C chunk buffers, 1024-aligned
-  uint64_t* full = reinterpret_cast<uint64_t*>(csm + 4 * kC3);
+  uint8_t* csm = sm + G3S * kStage3;           // [2 groups][G3CB] C chunk buffers, 1024-aligned
+  uint64_t* full = reinterpret_cast<uint64_t*>(csm + 2 * G3CB * kC3);
   uint64_t* empty = full + G3S;
   uint64_t* tfull = empty + G3S;
   uint64_t* tempty = tfull + 2;
-  uint64_t* cfull = tempty + 2;                // [2 groups][2]
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(cfull + 4);
+  uint64_t* cfull = tempty + 2;                // [2 groups][G3CB]
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(cfull + 2 * G3CB);
   int* abort_flag = reinterpret_cast<int*>(tslot + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int tiles_m = (M + G3M - 1) / G3M, tiles_n = (Nc + G3N - 1) / G3N;
@@ -606,7 +607,7 @@ __global__ void __launch_bounds__(kG3Threads, 1)
       mbar_init(&tfull[i], 1);
       mbar_init(&tempty[i], 4);  // one arrival per warp of the epilogue group
     }
-    for (int i = 0; i < 4; ++i) mbar_init(&cfull[i], 1);
+    for (int i = 0; i < 2 * G3CB; ++i) mbar_init(&cfull[i], 1);
     *abort_flag = 0;
     fence_mbar_init();
   }
@@ -707,13 +708,13 @@ __global__ void __launch_bounds__(kG3Threads, 1)
     const int acc = grp;
     uint32_t aphase = 0;
     uint32_t cph[2] = {0u, 0u};
-    uint8_t* gcsm = csm + (size_t)grp * 2 * kC3;
-    uint64_t* gcfull = cfull + 2 * grp;
+    uint8_t* gcsm = csm + (size_t)grp * G3CB * kC3;
+    uint64_t* gcfull = cfull + G3CB * grp;
     for (int t = blockIdx.x + grp * gridDim.x; t < ntiles; t += 2 * gridDim.x) {
       const int m0 = (t % tiles_m) * G3M, n0 = (t / tiles_m) * G3N;
       const int nch = min(G3N / 32, (Nc - n0 + 31) / 32);
       if (etid == 0) {
-        for (int j = 0; j < 2 && j < nch; ++j) {
+        for (int j = 0; j < G3CB && j < nch; ++j) {
           mbar_arrive_expect_tx(&gcfull[j], kC3);
           tma_load_2d(smem_u32(gcsm + j * kC3), &mC, ccol0 + n0 + 32 * j, crow0 + m0, &gcfull[j]);
         }
@@ -726,7 +727,7 @@ __global__ void __launch_bounds__(kG3Threads, 1)
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       bool stop = false;
       for (int j = 0; j < nch; ++j) {
-        const int b = j & 1;
+        const int b = j % G3CB;
         if (!mbar_wait_bounded(&gcfull[b], cph[b])) {
           *vabort = 1;
           dev_fail(err, WBEM_ERR_TIMEOUT, 85, blockIdx.x, t);
@@ -766,11 +767,11 @@ __global__ void __launch_bounds__(kG3Threads, 1)
         if (etid == 0) {
           tma_store_2d(&mC, ccol0 + n0 + 32 * j, crow0 + m0, smem_u32(gcsm + b * kC3));
           asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-          // the buffer is refilled two chunks ahead once the store has read it
+          // the buffer is refilled G3CB chunks ahead once the store has read it
           asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-          if (j + 2 < nch) {
+          if (j + G3CB < nch) {
             mbar_arrive_expect_tx(&gcfull[b], kC3);
-            tma_load_2d(smem_u32(gcsm + b * kC3), &mC, ccol0 + n0 + 32 * (j + 2), crow0 + m0,
+            tma_load_2d(smem_u32(gcsm + b * kC3), &mC, ccol0 + n0 + 32 * (j + G3CB), crow0 + m0,
                         &gcfull[b]);
           }
         }
@@ -792,7 +793,7 @@ __global__ void __launch_bounds__(kG3Threads, 1)
                  : "memory");
 }
 
-static size_t gemm_smem() { return (size_t)G3S * kStage3 + 4 * kC3 + 1024 + 256; }
+static size_t gemm_smem() { return (size_t)G3S * kStage3 + 2 * G3CB * kC3 + 1024 + 256; }
 
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (the
