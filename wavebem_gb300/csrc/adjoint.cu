@@ -101,27 +101,77 @@ __device__ __forceinline__ void point_grad(const T R[3], const T c[3], T J, T s1
 constexpr int kAdjChunk = 8;
 constexpr int kPt = 12;
 
-// One CTA: 128 rows x a chunk of panels. FP64 everywhere when MIXED == false;
-// otherwise FP32 for panels that fail the near test and FP64 for the rest.
-template <int Q1, bool MIXED>
+// FP64 point data of regular point q of the panel with dofs d (layout above).
+__device__ __forceinline__ void adj_point(const double* __restrict__ X, int4 d, int q,
+                                          const double* __restrict__ phi,
+                                          const double* __restrict__ dn, double* p) {
+  const int id[4] = {d.x, d.y, d.z, d.w};
+  const double s = c_qa.gp[q][0], u = c_qa.gp[q][1], w = c_qa.gp[q][2] * kI4P;
+  const double Ns[4] = {-(1 - u), (1 - u), -u, u};
+  const double Nt[4] = {-(1 - s), -s, (1 - s), s};
+  double x[3] = {0, 0, 0}, jx[3] = {0, 0, 0}, je[3] = {0, 0, 0}, fp = 0, fn = 0;
+  for (int v = 0; v < 4; ++v) {
+    const double nv = c_qa.phi[q][v];
+    for (int e = 0; e < 3; ++e) {
+      const double P = X[3 * (size_t)id[v] + e];
+      x[e] += nv * P;
+      jx[e] += Ns[v] * P;
+      je[e] += Nt[v] * P;
+    }
+    fp += nv * phi[id[v]];
+    fn += nv * dn[id[v]];
+  }
+  for (int e = 0; e < 3; ++e) {
+    p[e] = x[e];
+    p[3 + e] = jx[e];
+    p[6 + e] = je[e];
+  }
+  const double cr0 = jx[1] * je[2] - jx[2] * je[1], cr1 = jx[2] * je[0] - jx[0] * je[2],
+               cr2 = jx[0] * je[1] - jx[1] * je[0];
+  p[9] = sqrt(cr0 * cr0 + cr1 * cr1 + cr2 * cr2);
+  p[10] = w * fp;
+  p[11] = w * fn;
+}
+
+// FP64 terms of one (row, regular point) pair: row part into grow, the 4
+// panel-vertex parts into g (vertex v, component e at 3 v + e).
+__device__ __forceinline__ void adj_point_terms(const double* p, int q, const double xi[3],
+                                                double li, double phii, double g[12],
+                                                double grow[3]) {
+  const double R[3] = {p[0] - xi[0], p[1] - xi[1], p[2] - xi[2]};
+  const double c[3] = {p[4] * p[8] - p[5] * p[7], p[5] * p[6] - p[3] * p[8],
+                       p[3] * p[7] - p[4] * p[6]};
+  const double w = c_qa.gp[q][2] * kI4P;
+  const double s1 = li * (p[10] - w * phii), s2 = li * p[11];
+  double aR[3], ac[3];
+  point_grad<double>(R, c, p[9], s1, s2, aR, ac);
+  const double s = c_qa.gp[q][0], u = c_qa.gp[q][1];
+  const double Ns[4] = {-(1 - u), (1 - u), -u, u};
+  const double Nt[4] = {-(1 - s), -s, (1 - s), s};
+  const double gjx[3] = {p[7] * ac[2] - p[8] * ac[1], p[8] * ac[0] - p[6] * ac[2],
+                         p[6] * ac[1] - p[7] * ac[0]};
+  const double gje[3] = {ac[1] * p[5] - ac[2] * p[4], ac[2] * p[3] - ac[0] * p[5],
+                         ac[0] * p[4] - ac[1] * p[3]};
+  for (int e = 0; e < 3; ++e) grow[e] -= aR[e];
+  for (int v = 0; v < 4; ++v)
+    for (int e = 0; e < 3; ++e)
+      g[3 * v + e] += c_qa.phi[q][v] * aR[e] + Ns[v] * gjx[e] + Nt[v] * gje[e];
+}
+
+// Plain form. One CTA: 128 rows x a range of panels, FP64 throughout.
+template <int Q1>
 __global__ void __launch_bounds__(128)
     k_adj_tile(int N, int C, const double* __restrict__ X, const int* __restrict__ dnset,
-               const int4* __restrict__ cell_dofs, const float4* __restrict__ cellgeo,
-               const double* __restrict__ lam, const double* __restrict__ phi,
-               const double* __restrict__ dn, double* __restrict__ grow_part,
-               double* __restrict__ gcell_part, int cells_per_block) {
+               const int4* __restrict__ cell_dofs, const double* __restrict__ lam,
+               const double* __restrict__ phi, const double* __restrict__ dn,
+               double* __restrict__ grow_part, double* __restrict__ gcell_part,
+               int cells_per_block) {
   constexpr int NQ = Q1 * Q1;
   __shared__ double pt[kAdjChunk][NQ][kPt];
-  __shared__ float ptf[kAdjChunk][NQ][kPt];
   __shared__ double wred[4][kAdjChunk][12];
-  __shared__ double cT[3];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int row = blockIdx.y * 128 + tid;
   const bool active = row < N;
-  if (tid == 0) {
-    const int r0 = blockIdx.y * 128;
-    for (int d = 0; d < 3; ++d) cT[d] = X[3 * (size_t)r0 + d];
-  }
   double xi[3] = {0, 0, 0}, li = 0, phii = 0;
   int set[kMaxSet];
   for (int k = 0; k < kMaxSet; ++k) set[k] = -2;
@@ -131,122 +181,26 @@ __global__ void __launch_bounds__(128)
     phii = phi[row];
     for (int k = 0; k < kMaxSet; ++k) set[k] = dnset[(size_t)row * kMaxSet + k];
   }
-  __syncthreads();
-  const float xf = (float)xi[0], yf = (float)xi[1], zf = (float)xi[2];
-  const float xr[3] = {(float)(xi[0] - cT[0]), (float)(xi[1] - cT[1]), (float)(xi[2] - cT[2])};
   double grow[3] = {0, 0, 0};
   const int c_begin = blockIdx.x * cells_per_block;
   const int c_end = min(C, c_begin + cells_per_block);
   for (int cb = c_begin; cb < c_end; cb += kAdjChunk) {
     const int cnt = min(kAdjChunk, c_end - cb);
     __syncthreads();
-    // point data of the chunk
     for (int t = tid; t < cnt * NQ; t += 128) {
       const int k = t / NQ, q = t % NQ;
-      const int4 d = cell_dofs[cb + k];
-      const int id[4] = {d.x, d.y, d.z, d.w};
-      const double s = c_qa.gp[q][0], u = c_qa.gp[q][1], w = c_qa.gp[q][2] * kI4P;
-      const double Ns[4] = {-(1 - u), (1 - u), -u, u};
-      const double Nt[4] = {-(1 - s), -s, (1 - s), s};
-      double x[3] = {0, 0, 0}, jx[3] = {0, 0, 0}, je[3] = {0, 0, 0}, fp = 0, fn = 0;
-      for (int v = 0; v < 4; ++v) {
-        const double nv = c_qa.phi[q][v];
-        for (int e = 0; e < 3; ++e) {
-          const double P = X[3 * (size_t)id[v] + e];
-          x[e] += nv * P;
-          jx[e] += Ns[v] * P;
-          je[e] += Nt[v] * P;
-        }
-        fp += nv * phi[id[v]];
-        fn += nv * dn[id[v]];
-      }
-      double* p = pt[k][q];
-      float* pf = ptf[k][q];
-      for (int e = 0; e < 3; ++e) {
-        p[e] = x[e];
-        p[3 + e] = jx[e];
-        p[6 + e] = je[e];
-        pf[e] = (float)(x[e] - cT[e]);
-        pf[3 + e] = (float)jx[e];
-        pf[6 + e] = (float)je[e];
-      }
-      const double cr0 = jx[1] * je[2] - jx[2] * je[1], cr1 = jx[2] * je[0] - jx[0] * je[2],
-                   cr2 = jx[0] * je[1] - jx[1] * je[0];
-      p[9] = sqrt(cr0 * cr0 + cr1 * cr1 + cr2 * cr2);
-      p[10] = w * fp;
-      p[11] = w * fn;
-      pf[9] = (float)p[9];
-      pf[10] = (float)p[10];
-      pf[11] = (float)p[11];
+      adj_point(X, cell_dofs[cb + k], q, phi, dn, pt[k][q]);
     }
     __syncthreads();
     for (int k = 0; k < cnt; ++k) {
-      const int cell = cb + k;
-      const int4 d = cell_dofs[cell];
+      const int4 d = cell_dofs[cb + k];
       bool sing = false;
       for (int s = 0; s < kMaxSet; ++s)
         sing |= (set[s] == d.x) | (set[s] == d.y) | (set[s] == d.z) | (set[s] == d.w);
       double g[12];
       for (int t = 0; t < 12; ++t) g[t] = 0;
-      if (active && !sing && li != 0.0) {
-        const bool use64 = !MIXED || near_test_a(xf, yf, zf, cellgeo[cell]);
-        if (use64) {
-          for (int q = 0; q < NQ; ++q) {
-            const double* p = pt[k][q];
-            const double R[3] = {p[0] - xi[0], p[1] - xi[1], p[2] - xi[2]};
-            const double c[3] = {p[4] * p[8] - p[5] * p[7], p[5] * p[6] - p[3] * p[8],
-                                 p[3] * p[7] - p[4] * p[6]};
-            const double w = c_qa.gp[q][2] * kI4P;
-            const double s1 = li * (p[10] - w * phii), s2 = li * p[11];
-            double aR[3], ac[3];
-            point_grad<double>(R, c, p[9], s1, s2, aR, ac);
-            const double s = c_qa.gp[q][0], u = c_qa.gp[q][1];
-            const double Ns[4] = {-(1 - u), (1 - u), -u, u};
-            const double Nt[4] = {-(1 - s), -s, (1 - s), s};
-            const double gjx[3] = {p[7] * ac[2] - p[8] * ac[1], p[8] * ac[0] - p[6] * ac[2],
-                                   p[6] * ac[1] - p[7] * ac[0]};
-            const double gje[3] = {ac[1] * p[5] - ac[2] * p[4], ac[2] * p[3] - ac[0] * p[5],
-                                   ac[0] * p[4] - ac[1] * p[3]};
-            for (int e = 0; e < 3; ++e) grow[e] -= aR[e];
-            for (int v = 0; v < 4; ++v)
-              for (int e = 0; e < 3; ++e)
-                g[3 * v + e] += c_qa.phi[q][v] * aR[e] + Ns[v] * gjx[e] + Nt[v] * gje[e];
-          }
-        } else {
-          float gf[12];
-          for (int t = 0; t < 12; ++t) gf[t] = 0.f;
-          float grf[3] = {0.f, 0.f, 0.f};
-          const float lif = (float)li, phif = (float)phii;
-#pragma unroll 4
-          for (int q = 0; q < NQ; ++q) {
-            const float* p = ptf[k][q];
-            const float R[3] = {p[0] - xr[0], p[1] - xr[1], p[2] - xr[2]};
-            const float jx[3] = {p[3], p[4], p[5]};
-            const float je[3] = {p[6], p[7], p[8]};
-            const float c[3] = {jx[1] * je[2] - jx[2] * je[1], jx[2] * je[0] - jx[0] * je[2],
-                                jx[0] * je[1] - jx[1] * je[0]};
-            const float w = c_qa.gpf[q][2] * (float)kI4P;
-            const float s1 = lif * (p[10] - w * phif), s2 = lif * p[11];
-            float aR[3], ac[3];
-            point_grad<float>(R, c, p[9], s1, s2, aR, ac);
-            const float s = c_qa.gpf[q][0], u = c_qa.gpf[q][1];
-            const float Ns[4] = {-(1 - u), (1 - u), -u, u};
-            const float Nt[4] = {-(1 - s), -s, (1 - s), s};
-            const float gjx[3] = {je[1] * ac[2] - je[2] * ac[1], je[2] * ac[0] - je[0] * ac[2],
-                                  je[0] * ac[1] - je[1] * ac[0]};
-            const float gje[3] = {ac[1] * jx[2] - ac[2] * jx[1], ac[2] * jx[0] - ac[0] * jx[2],
-                                  ac[0] * jx[1] - ac[1] * jx[0]};
-            for (int e = 0; e < 3; ++e) grf[e] -= aR[e];
-            for (int v = 0; v < 4; ++v) {
-              const float nv = c_qa.phif[q][v];
-              for (int e = 0; e < 3; ++e)
-                gf[3 * v + e] += nv * aR[e] + Ns[v] * gjx[e] + Nt[v] * gje[e];
-            }
-          }
-          for (int e = 0; e < 3; ++e) grow[e] += grf[e];
-          for (int t = 0; t < 12; ++t) g[t] = gf[t];
-        }
-      }
+      if (active && !sing && li != 0.0)
+        for (int q = 0; q < NQ; ++q) adj_point_terms(pt[k][q], q, xi, li, phii, g, grow);
       // sum the 12 panel-vertex terms over the 32 rows of the warp
       for (int t = 0; t < 12; ++t) {
         double v = g[t];
@@ -263,6 +217,320 @@ __global__ void __launch_bounds__(128)
   }
   if (active)
     for (int e = 0; e < 3; ++e) grow_part[((size_t)blockIdx.x * N + row) * 3 + e] = grow[e];
+}
+
+// ---------------------------------------------------- mixed form (K7 mixed)
+// Far pairs (panels that fail the assembly's near test) run in FP32, near
+// pairs in FP64, singular pairs in k_adj_singular.
+//
+// The far-field sum over the regular points q of one panel is kept in the
+// bilinear basis N4_v(q) of the panel:
+//     B_v = sum_q N4_v aR_q,   D_v = sum_q N4_v ac_q      (v = 0..3)
+// with aR, ac the derivatives with respect to the point offset R and the
+// cross product c (point_grad). Since jx = (1-u) F0 + u F1 and
+// je = (1-s) E0 + s E1 (F0 = P1-P0, F1 = P3-P2, E0 = P2-P0, E1 = P3-P1),
+// the vertex gradients sum_q [N4_v aR + Ns_v (je x ac) + Nt_v (ac x jx)] are
+//     g0 = B0 - X01 - Y02,  g1 = B1 + X01 - Y13,
+//     g2 = B2 - X23 + Y02,  g3 = B3 + X23 + Y13,
+//     X01 = E0 x D0 + E1 x D1,  X23 = E0 x D2 + E1 x D3,
+//     Y02 = D0 x F0 + D2 x F1,  Y13 = D1 x F0 + D3 x F1.
+// B and D are linear in the rows, so each thread sums them over its rows,
+// the warp reduces them once per panel and the cross products are taken
+// once per (CTA, panel) in FP64.
+constexpr int kAdjRpt = 4;                  // rows per thread
+constexpr int kAdjRowsCta = 128 * kAdjRpt;  // rows per CTA (consecutive, 128 per warp)
+static_assert(kMaxSet % 4 == 0, "double-node sets are read as int4");
+static_assert(kAdjRpt * kAdjChunk <= 32, "near mask of a chunk in one word");
+
+// Per (panel, regular point), once per adjoint call:
+//   recd (12 doubles): the FP64 point data of adj_point (near pairs);
+//   recf (3 float4):   (x_hi, c.x), (x_lo, c.y), (c.z, w'phi, w'dn |c|, w'dn / |c|)
+//                      with x = x_hi + x_lo and c = jx x je;
+// per panel pgeo (12 doubles): E0, E1, F0, F1.
+template <int Q1>
+__global__ void k_adj_points(int C, const double* __restrict__ X,
+                             const int4* __restrict__ cell_dofs, const double* __restrict__ phi,
+                             const double* __restrict__ dn, double* __restrict__ recd,
+                             float4* __restrict__ recf, double* __restrict__ pgeo) {
+  constexpr int NQ = Q1 * Q1;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= C * NQ) return;
+  const int cell = t / NQ, q = t - cell * NQ;
+  const int4 d = cell_dofs[cell];
+  double p[kPt];
+  adj_point(X, d, q, phi, dn, p);
+  double* pd = recd + (size_t)t * kPt;
+  for (int e = 0; e < kPt; ++e) pd[e] = p[e];
+  const double c0 = p[4] * p[8] - p[5] * p[7], c1 = p[5] * p[6] - p[3] * p[8],
+               c2 = p[3] * p[7] - p[4] * p[6];
+  float hi[3], lo[3];
+  for (int e = 0; e < 3; ++e) {
+    hi[e] = (float)p[e];
+    lo[e] = (float)(p[e] - (double)hi[e]);
+  }
+  recf[3 * (size_t)t + 0] = make_float4(hi[0], hi[1], hi[2], (float)c0);
+  recf[3 * (size_t)t + 1] = make_float4(lo[0], lo[1], lo[2], (float)c1);
+  recf[3 * (size_t)t + 2] =
+      make_float4((float)c2, (float)p[10], (float)(p[11] * p[9]), (float)(p[11] / p[9]));
+  if (q == 0) {
+    const int id[4] = {d.x, d.y, d.z, d.w};
+    double P[4][3];
+    for (int v = 0; v < 4; ++v)
+      for (int e = 0; e < 3; ++e) P[v][e] = X[3 * (size_t)id[v] + e];
+    double* g = pgeo + (size_t)cell * 12;
+    for (int e = 0; e < 3; ++e) {
+      g[e] = P[2][e] - P[0][e];
+      g[3 + e] = P[3][e] - P[1][e];
+      g[6 + e] = P[1][e] - P[0][e];
+      g[9 + e] = P[3][e] - P[2][e];
+    }
+  }
+}
+
+// Sum of v[0..23] over the 32 lanes of the warp by reduce-scatter (27
+// shuffles): lane l returns the sums of v[3 (l >> 2) + i], i = 0..2.
+__device__ __forceinline__ void warp_sum24(const float v[24], int lane, float out[3]) {
+  const bool h1 = lane & 16, h2 = lane & 8, h3 = lane & 4;
+  float w[12], x[6];
+#pragma unroll
+  for (int i = 0; i < 12; ++i) {
+    const float keep = h1 ? v[12 + i] : v[i], send = h1 ? v[i] : v[12 + i];
+    w[i] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+  }
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    const float keep = h2 ? w[6 + i] : w[i], send = h2 ? w[i] : w[6 + i];
+    x[i] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float keep = h3 ? x[3 + i] : x[i], send = h3 ? x[i] : x[3 + i];
+    float y = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    y += __shfl_xor_sync(0xffffffffu, y, 2);
+    y += __shfl_xor_sync(0xffffffffu, y, 1);
+    out[i] = y;
+  }
+}
+
+// One CTA: kAdjRowsCta rows (kAdjRpt consecutive rows per thread) x a range
+// of panels, in chunks of kAdjChunk panels whose FP32 point data (offsets from
+// the CTA's first row, so that the FP32 differences stay accurate) sit in
+// shared memory.
+template <int Q1>
+__global__ void __launch_bounds__(128, 4)
+    k_adj_tile_mixed(int N, int C, const double* __restrict__ X, const int* __restrict__ dnset,
+                     const int4* __restrict__ cell_dofs, const float4* __restrict__ cellgeo,
+                     const float4* __restrict__ recf, const double* __restrict__ recd,
+                     const double* __restrict__ pgeo, const double* __restrict__ lam,
+                     const double* __restrict__ phi, double* __restrict__ grow_part,
+                     double* __restrict__ gcell_part, int cells_per_block) {
+  constexpr int NQ = Q1 * Q1;
+  __shared__ __align__(16) float sp[kAdjChunk][NQ][12];
+  __shared__ float wmom[4][kAdjChunk][24];
+  __shared__ double wnear[4][kAdjChunk][12];
+  __shared__ double smom[kAdjChunk][24];
+  __shared__ double sgrow[kAdjRpt][3][128];
+  __shared__ float sxf[kAdjRpt][3][128];
+  __shared__ int4 sdofs[kAdjChunk];
+  __shared__ float4 sgeo[kAdjChunk];
+  __shared__ double cTd[3];
+  __shared__ float cTs[6];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int r0 = blockIdx.y * kAdjRowsCta;
+  const int rbase = r0 + kAdjRpt * tid;
+  if (tid < 3) {
+    const double c = X[3 * (size_t)r0 + tid];
+    const float hi = (float)c;
+    cTd[tid] = c;
+    cTs[tid] = hi;
+    cTs[3 + tid] = (float)(c - (double)hi);
+  }
+  __syncthreads();
+  float xr[kAdjRpt][3], lf[kAdjRpt], lpf[kAdjRpt];
+  unsigned live = 0;
+#pragma unroll
+  for (int j = 0; j < kAdjRpt; ++j) {
+    const int row = rbase + j;
+    double x[3] = {cTd[0], cTd[1], cTd[2]}, li = 0, ph = 0;
+    if (row < N) {
+      for (int e = 0; e < 3; ++e) x[e] = X[3 * (size_t)row + e];
+      li = lam[row];
+      ph = phi[row];
+      if (li != 0.0) live |= 1u << j;
+    }
+    for (int e = 0; e < 3; ++e) {
+      xr[j][e] = (float)(x[e] - cTd[e]);
+      sxf[j][e][tid] = (float)x[e];
+      sgrow[j][e][tid] = 0.0;
+    }
+    lf[j] = (float)li;
+    lpf[j] = (float)(li * ph * kI4P);
+  }
+  const int c_begin = blockIdx.x * cells_per_block;
+  const int c_end = min(C, c_begin + cells_per_block);
+  for (int cb = c_begin; cb < c_end; cb += kAdjChunk) {
+    const int cnt = min(kAdjChunk, c_end - cb);
+    __syncthreads();
+    for (int t = tid; t < cnt * NQ; t += 128) {
+      const float4* r = recf + 3 * ((size_t)cb * NQ + t);
+      const float4 a = r[0], b = r[1], c = r[2];
+      float* s = &sp[0][0][0] + 12 * t;
+      s[0] = (a.x - cTs[0]) + (b.x - cTs[3]);
+      s[1] = (a.y - cTs[1]) + (b.y - cTs[4]);
+      s[2] = (a.z - cTs[2]) + (b.z - cTs[5]);
+      s[3] = a.w;
+      s[4] = b.w;
+      s[5] = c.x;
+      s[6] = c.y;
+      s[7] = c.z;
+      s[8] = c.w;
+    }
+    if (tid < cnt) {
+      sdofs[tid] = cell_dofs[cb + tid];
+      sgeo[tid] = cellgeo[cb + tid];
+    }
+    __syncthreads();
+    float gr[kAdjRpt][3];
+#pragma unroll
+    for (int j = 0; j < kAdjRpt; ++j) gr[j][0] = gr[j][1] = gr[j][2] = 0.f;
+    unsigned nmask = 0;  // near (row j, panel k) pairs of the chunk at bit kAdjRpt k + j
+    for (int k = 0; k < cnt; ++k) {
+      const float4 g = sgeo[k];
+      bool far[kAdjRpt];
+      float lk[kAdjRpt], lpk[kAdjRpt];
+#pragma unroll
+      for (int j = 0; j < kAdjRpt; ++j) {
+        const bool nt = near_test_a(sxf[j][0][tid], sxf[j][1][tid], sxf[j][2][tid], g);
+        const bool lv = (live >> j) & 1u;
+        far[j] = lv && !nt;
+        if (lv && nt) nmask |= 1u << (kAdjRpt * k + j);
+        lk[j] = far[j] ? lf[j] : 0.f;
+        lpk[j] = far[j] ? lpf[j] : 0.f;
+      }
+      float v[24];
+#pragma unroll
+      for (int i = 0; i < 24; ++i) v[i] = 0.f;
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) {
+        const float* p = sp[k][q];
+        const float4 A = *reinterpret_cast<const float4*>(p);
+        const float4 B = *reinterpret_cast<const float4*>(p + 4);
+        const float wnoj = p[8];
+        const float c[3] = {A.w, B.x, B.y};
+        const float gw = c_qa.gpf[q][2];
+        float aR[3] = {0.f, 0.f, 0.f}, ac[3] = {0.f, 0.f, 0.f}, Ks = 0.f, Kc = 0.f;
+#pragma unroll
+        for (int j = 0; j < kAdjRpt; ++j) {
+          const float R[3] = {A.x - xr[j][0], A.y - xr[j][1], A.z - xr[j][2]};
+          float r2 = R[0] * R[0] + R[1] * R[1] + R[2] * R[2];
+          r2 = far[j] ? r2 : 1.f;
+          const float ri = rsqrtf(r2), ri2 = ri * ri, ri3 = ri2 * ri;
+          const float u = R[0] * c[0] + R[1] * c[1] + R[2] * c[2];
+          const float s1 = fmaf(lk[j], B.z, -lpk[j] * gw);
+          const float a = s1 * ri3;
+          const float kr = fmaf(s1 * u, ri3 * (3.f * ri2), (lk[j] * B.w) * ri3);
+          const float kc = (lk[j] * wnoj) * ri;
+          Ks += a;
+          Kc += kc;
+#pragma unroll
+          for (int e = 0; e < 3; ++e) {
+            aR[e] = fmaf(kr, R[e], aR[e]);
+            ac[e] = fmaf(-a, R[e], ac[e]);
+            gr[j][e] = fmaf(kr, R[e], fmaf(-a, c[e], gr[j][e]));
+          }
+        }
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+          aR[e] = fmaf(-Ks, c[e], aR[e]);
+          ac[e] = fmaf(-Kc, c[e], ac[e]);
+        }
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+          const float nv = c_qa.phif[q][w];
+#pragma unroll
+          for (int e = 0; e < 3; ++e) {
+            v[3 * w + e] = fmaf(nv, aR[e], v[3 * w + e]);
+            v[12 + 3 * w + e] = fmaf(nv, ac[e], v[12 + 3 * w + e]);
+          }
+        }
+      }
+      float o3[3];
+      warp_sum24(v, lane, o3);
+      if ((lane & 3) == 0)
+        for (int i = 0; i < 3; ++i) wmom[warp][k][3 * (lane >> 2) + i] = o3[i];
+    }
+#pragma unroll
+    for (int j = 0; j < kAdjRpt; ++j)
+      for (int e = 0; e < 3; ++e) sgrow[j][e][tid] -= (double)gr[j][e];
+    // near pairs of the chunk: FP64 terms, unless the pair is singular
+    for (int k = 0; k < cnt; ++k) {
+      unsigned nm = (nmask >> (kAdjRpt * k)) & ((1u << kAdjRpt) - 1u);
+      if (__any_sync(0xffffffffu, nm != 0u)) {
+        double g64[12];
+        for (int t = 0; t < 12; ++t) g64[t] = 0.0;
+        const int4 d = sdofs[k];
+        const double* pc = recd + (size_t)(cb + k) * NQ * kPt;
+        while (nm) {
+          const int j = __ffs(nm) - 1;
+          nm &= nm - 1u;
+          const int row = rbase + j;
+          const int4* s4 = reinterpret_cast<const int4*>(dnset + (size_t)row * kMaxSet);
+          bool sing = false;
+          for (int h = 0; h < kMaxSet / 4; ++h) {
+            const int4 s = s4[h];
+            const int m[4] = {s.x, s.y, s.z, s.w};
+            for (int i = 0; i < 4; ++i)
+              sing |= (m[i] == d.x) | (m[i] == d.y) | (m[i] == d.z) | (m[i] == d.w);
+          }
+          if (sing) continue;
+          const double xi[3] = {X[3 * (size_t)row], X[3 * (size_t)row + 1], X[3 * (size_t)row + 2]};
+          const double li = lam[row], phii = phi[row];
+          double grow[3] = {0.0, 0.0, 0.0};
+          for (int q = 0; q < NQ; ++q) adj_point_terms(pc + q * kPt, q, xi, li, phii, g64, grow);
+          for (int e = 0; e < 3; ++e) sgrow[j][e][tid] += grow[e];
+        }
+        for (int t = 0; t < 12; ++t) {
+          double s = g64[t];
+          for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+          if (lane == 0) wnear[warp][k][t] = s;
+        }
+      } else if (lane == 0) {
+        for (int t = 0; t < 12; ++t) wnear[warp][k][t] = 0.0;
+      }
+    }
+    __syncthreads();
+    for (int t = tid; t < cnt * 24; t += 128) {
+      const int k = t / 24, m = t - 24 * k;
+      smom[k][m] = ((double)wmom[0][k][m] + (double)wmom[1][k][m]) +
+                   ((double)wmom[2][k][m] + (double)wmom[3][k][m]);
+    }
+    __syncthreads();
+    for (int t = tid; t < cnt * 12; t += 128) {
+      const int k = t / 12, o = t - 12 * k, w = o / 3, e = o - 3 * w;
+      const int e1 = e == 2 ? 0 : e + 1, e2 = e == 0 ? 2 : e - 1;
+      const double* G = pgeo + (size_t)(cb + k) * 12;  // E0, E1, F0, F1
+      const double* D = &smom[k][12];                  // D_i at D[3 i]
+      // X-part: E0 x D_i + E1 x D_{i+1}, i = 0 (vertices 0, 1) or 2 (vertices 2, 3)
+      const int ix = w < 2 ? 0 : 2;
+      const double xs = G[e1] * D[3 * ix + e2] - G[e2] * D[3 * ix + e1] +
+                        G[3 + e1] * D[3 * ix + 3 + e2] - G[3 + e2] * D[3 * ix + 3 + e1];
+      // Y-part: D_i x F0 + D_{i+2} x F1, i = 0 (vertices 0, 2) or 1 (vertices 1, 3)
+      const int iy = w & 1;
+      const double ys = D[3 * iy + e1] * G[6 + e2] - D[3 * iy + e2] * G[6 + e1] +
+                        D[3 * iy + 6 + e1] * G[9 + e2] - D[3 * iy + 6 + e2] * G[9 + e1];
+      double val = smom[k][o] + ((w & 1) ? xs : -xs) + (w >= 2 ? ys : -ys);
+      val += (wnear[0][k][o] + wnear[1][k][o]) + (wnear[2][k][o] + wnear[3][k][o]);
+      gcell_part[((size_t)blockIdx.y * C + cb + k) * 12 + o] = val;
+    }
+  }
+  // each thread reads back only the entries of sgrow it wrote itself
+#pragma unroll
+  for (int j = 0; j < kAdjRpt; ++j) {
+    const int row = rbase + j;
+    if (row < N)
+      for (int e = 0; e < 3; ++e)
+        grow_part[((size_t)blockIdx.x * N + row) * 3 + e] = sgrow[j][e][tid];
+  }
 }
 
 // Singular panels of each row (FP64, vertex rule): row part into grow_sing,
@@ -409,14 +677,28 @@ __global__ void k_gb(int N, const uint8_t* __restrict__ mask, const double* __re
   gb[i] = v;
 }
 
-template <int Q1, bool MIXED>
+template <int Q1>
 static cudaError_t launch_adj_tile_t(int N, int C, const double* X, const int* dnset,
-                                     const int4* cd, const float4* geo, const double* lam,
-                                     const double* phi, const double* dn, double* grow_part,
-                                     double* gcell_part, int cpb, cudaStream_t s) {
+                                     const int4* cd, const double* lam, const double* phi,
+                                     const double* dn, double* grow_part, double* gcell_part,
+                                     int cpb, cudaStream_t s) {
   dim3 grid((C + cpb - 1) / cpb, (N + 127) / 128);
-  k_adj_tile<Q1, MIXED><<<grid, 128, 0, s>>>(N, C, X, dnset, cd, geo, lam, phi, dn, grow_part,
-                                             gcell_part, cpb);
+  k_adj_tile<Q1><<<grid, 128, 0, s>>>(N, C, X, dnset, cd, lam, phi, dn, grow_part, gcell_part,
+                                      cpb);
+  return cudaGetLastError();
+}
+
+template <int Q1>
+static cudaError_t launch_adj_mixed_t(int N, int C, const double* X, const int* dnset,
+                                      const int4* cd, const float4* geo, const double* lam,
+                                      const double* phi, const double* dn, double* recd,
+                                      float4* recf, double* pgeo, double* grow_part,
+                                      double* gcell_part, int cpb, cudaStream_t s) {
+  constexpr int NQ = Q1 * Q1;
+  k_adj_points<Q1><<<(C * NQ + 255) / 256, 256, 0, s>>>(C, X, cd, phi, dn, recd, recf, pgeo);
+  dim3 grid((C + cpb - 1) / cpb, (N + kAdjRowsCta - 1) / kAdjRowsCta);
+  k_adj_tile_mixed<Q1><<<grid, 128, 0, s>>>(N, C, X, dnset, cd, geo, recf, recd, pgeo, lam, phi,
+                                            grow_part, gcell_part, cpb);
   return cudaGetLastError();
 }
 
@@ -436,9 +718,14 @@ int adjoint_force(wbem_context* h, const int* hull_cells, int n_hull, const doub
   for (int k = 0; k < n_hull; ++k) hoc[hull_ids[k]] = k;
   int* d_hoc = nullptr;
   double *d_ghull = nullptr, *d_gph = nullptr, *d_gpn = nullptr;
-  const int cpb = 64;
-  const int n_cb = (C + cpb - 1) / cpb, n_rb = (N + 127) / 128;
+  // panels per CTA column and rows per CTA of the tile kernel
+  const int cpb = mixed ? 128 : 64;
+  const int rows_cta = mixed ? kAdjRowsCta : 128;
+  const int n_cb = (C + cpb - 1) / cpb, n_rb = (N + rows_cta - 1) / rows_cta;
+  const size_t npts = (size_t)C * q1 * q1;
   double *grow_part = nullptr, *gcell_part = nullptr, *grow_sing = nullptr, *gpair = nullptr;
+  double *recd = nullptr, *pgeo = nullptr;
+  float4* recf = nullptr;
   int *d_cpptr = nullptr, *d_cpidx = nullptr;
   double* d_out = nullptr;
   double* d_nph = nullptr;
@@ -471,6 +758,11 @@ int adjoint_force(wbem_context* h, const int* hull_cells, int n_hull, const doub
     if ((st = dev_alloc(h, &gpair, (size_t)std::max<size_t>(1, scell.size()) * 12)) != WBEM_OK) break;
     if ((st = dev_alloc(h, &d_out, (size_t)N * 3)) != WBEM_OK) break;
     if ((st = dev_alloc(h, &d_nph, (size_t)N * 2)) != WBEM_OK) break;
+    if (mixed) {
+      if ((st = dev_alloc(h, &recd, npts * kPt)) != WBEM_OK) break;
+      if ((st = dev_alloc(h, &recf, npts * 3)) != WBEM_OK) break;
+      if ((st = dev_alloc(h, &pgeo, (size_t)C * 12)) != WBEM_OK) break;
+    }
     double* phi = h->d_vec[3];
     double* dn = h->d_vec[4];
     double* gx = h->d_vec[5];
@@ -498,20 +790,21 @@ int adjoint_force(wbem_context* h, const int* hull_cells, int n_hull, const doub
     const float4* geo = reinterpret_cast<const float4*>(h->d_cellgeo);
     cudaError_t e;
     if (mixed) {
+      const int4* cd = h->d_cell_dofs;
       switch (q1) {
-        case 2: e = launch_adj_tile_t<2, true>(N, C, h->d_X, h->d_dnset, h->d_cell_dofs, geo, lamu, phi, dn, grow_part, gcell_part, cpb, h->stream); break;
-        case 3: e = launch_adj_tile_t<3, true>(N, C, h->d_X, h->d_dnset, h->d_cell_dofs, geo, lamu, phi, dn, grow_part, gcell_part, cpb, h->stream); break;
-        case 4: e = launch_adj_tile_t<4, true>(N, C, h->d_X, h->d_dnset, h->d_cell_dofs, geo, lamu, phi, dn, grow_part, gcell_part, cpb, h->stream); break;
-        case 5: e = launch_adj_tile_t<5, true>(N, C, h->d_X, h->d_dnset, h->d_cell_dofs, geo, lamu, phi, dn, grow_part, gcell_part, cpb, h->stream); break;
-        default: e = launch_adj_tile_t<6, true>(N, C, h->d_X, h->d_dnset, h->d_cell_dofs, geo, lamu, phi, dn, grow_part, gcell_part, cpb, h->stream); break;
+        case 2: e = launch_adj_mixed_t<2>(N, C, h->d_X, h->d_dnset, cd, geo, lamu, phi, dn, recd, recf, pgeo, grow_part, gcell_part, cpb, h->stream); break;
+        case 3: e = launch_adj_mixed_t<3>(N, C, h->d_X, h->d_dnset, cd, geo, lamu, phi, dn, recd, recf, pgeo, grow_part, gcell_part, cpb, h->stream); break;
+        case 4: e = launch_adj_mixed_t<4>(N, C, h->d_X, h->d_dnset, cd, geo, lamu, phi, dn, recd, recf, pgeo, grow_part, gcell_part, cpb, h->stream); break;
+        case 5: e = launch_adj_mixed_t<5>(N, C, h->d_X, h->d_dnset, cd, geo, lamu, phi, dn, recd, recf, pgeo, grow_part, gcell_part, cpb, h->stream); break;
+        default: e = launch_adj_mixed_t<6>(N, C, h->d_X, h->d_dnset, cd, geo, lamu, phi, dn, recd, recf, pgeo, grow_part, gcell_part, cpb, h->stream); break;
       }
     } else {
       switch (q1) {
-        case 2: e = launch_adj_tile_t<2, false>(N, C, h->d_X, h->d_dnset, h->d_cell_dofs, geo, lamu, phi, dn, grow_part, gcell_part, cpb, h->stream); break;
-        case 3: e = launch_adj_tile_t<3, false>(N, C, h->d_X, h->d_dnset, h->d_cell_dofs, geo, lamu, phi, dn, grow_part, gcell_part, cpb, h->stream); break;
-        case 4: e = launch_adj_tile_t<4, false>(N, C, h->d_X, h->d_dnset, h->d_cell_dofs, geo, lamu, phi, dn, grow_part, gcell_part, cpb, h->stream); break;
-        case 5: e = launch_adj_tile_t<5, false>(N, C, h->d_X, h->d_dnset, h->d_cell_dofs, geo, lamu, phi, dn, grow_part, gcell_part, cpb, h->stream); break;
-        default: e = launch_adj_tile_t<6, false>(N, C, h->d_X, h->d_dnset, h->d_cell_dofs, geo, lamu, phi, dn, grow_part, gcell_part, cpb, h->stream); break;
+        case 2: e = launch_adj_tile_t<2>(N, C, h->d_X, h->d_dnset, h->d_cell_dofs, lamu, phi, dn, grow_part, gcell_part, cpb, h->stream); break;
+        case 3: e = launch_adj_tile_t<3>(N, C, h->d_X, h->d_dnset, h->d_cell_dofs, lamu, phi, dn, grow_part, gcell_part, cpb, h->stream); break;
+        case 4: e = launch_adj_tile_t<4>(N, C, h->d_X, h->d_dnset, h->d_cell_dofs, lamu, phi, dn, grow_part, gcell_part, cpb, h->stream); break;
+        case 5: e = launch_adj_tile_t<5>(N, C, h->d_X, h->d_dnset, h->d_cell_dofs, lamu, phi, dn, grow_part, gcell_part, cpb, h->stream); break;
+        default: e = launch_adj_tile_t<6>(N, C, h->d_X, h->d_dnset, h->d_cell_dofs, lamu, phi, dn, grow_part, gcell_part, cpb, h->stream); break;
       }
     }
     WB_CU(e);
@@ -531,7 +824,7 @@ int adjoint_force(wbem_context* h, const int* hull_cells, int n_hull, const doub
     double* gb = h->d_vec[0];
     k_gb<<<nb, bs, 0, h->stream>>>(N, h->d_mask, nph, npn, bt, h->d_alpha, lamu, gb);
     WB_CU(cudaGetLastError());
-    h->launches += 12;
+    h->launches += mixed ? 13 : 12;
     WB_CHK(check_device_error(h, "adjoint"));
     // back to the caller's order; constraint inhomogeneities tied to b
     std::vector<double> gXi(3 * (size_t)N), gbi(N), li(N);
@@ -564,7 +857,7 @@ int adjoint_force(wbem_context* h, const int* hull_cells, int n_hull, const doub
     h->stats.t_adjoint_ms = tm.ms();
   } while (0);
   void* fr[] = {hd, d_hoc, d_ghull, d_gph, d_gpn, grow_part, gcell_part, grow_sing, gpair,
-                d_cpptr, d_cpidx, d_out, d_nph};
+                d_cpptr, d_cpidx, d_out, d_nph, recd, recf, pgeo};
   for (void* p : fr)
     if (p) cudaFree(p);
   return st;

@@ -124,18 +124,5 @@ cudaError_t launch_hull_force_grad(int nh, const int4* hull_dofs, const double* 
                                    const double* U, int dir, const double* phi, const double* dphi,
                                    double* gX_cell, double* gphi_cell, double* gdphi_cell,
                                    cudaStream_t s);
-cudaError_t launch_adjoint_tiles(int N, int q1, const double* X, const int* dnset, int C,
-                                 const int4* cell_dofs, const double* lambda, const double* phi,
-                                 const double* dphi, const uint8_t* rowmask, double* gX_row,
-                                 double* gX_cell_part, int row_blocks, DevErr* err,
-                                 cudaStream_t s);
-cudaError_t launch_adjoint_singular(int N, const double* X, const int* dnset, const int* sptr,
-                                    const int* scell, const int4* cell_dofs,
-                                    const double* lambda, const double* phi, const double* dphi,
-                                    const uint8_t* rowmask, double* gX_row, double* gX_sing,
-                                    DevErr* err, cudaStream_t s);
-cudaError_t launch_reduce_cell_grad(int N, int C, int row_blocks, const double* gX_cell_part,
-                                    const double* gX_sing, const int* ncptr, const int* ncent,
-                                    const double* gX_row, double* gX, cudaStream_t s);
 
 }  // namespace wbem
