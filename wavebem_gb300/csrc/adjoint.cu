@@ -158,6 +158,37 @@ __device__ __forceinline__ void adj_point_terms(const double* p, int q, const do
       g[3 * v + e] += c_qa.phi[q][v] * aR[e] + Ns[v] * gjx[e] + Nt[v] * gje[e];
 }
 
+// FP64 terms of one near (row, regular point) pair of the mixed form, in the
+// moment form of the far field (B_v += N4_v aR, D_v += N4_v ac, row part into
+// grow). p: x (3), c = jx x je (3), w'phi(q), w'dn(q) |c|, w'dn(q) / |c|;
+// lpw = lambda_i phi_i / (4 pi).
+__device__ __forceinline__ void adj_near_moments(const double* __restrict__ p, int q,
+                                                 const double xi[3], double li, double lpw,
+                                                 double B[12], double D[12], double grow[3]) {
+  const double R[3] = {p[0] - xi[0], p[1] - xi[1], p[2] - xi[2]};
+  const double c[3] = {p[3], p[4], p[5]};
+  const double r2 = R[0] * R[0] + R[1] * R[1] + R[2] * R[2];
+  const double ri = rsqrt(r2), ri2 = ri * ri, ri3 = ri2 * ri;
+  const double u = R[0] * c[0] + R[1] * c[1] + R[2] * c[2];
+  const double s1 = li * p[6] - lpw * c_qa.gp[q][2];
+  const double a = s1 * ri3;
+  const double kr = 3.0 * s1 * u * ri3 * ri2 + li * p[7] * ri3;
+  const double kc = li * p[8] * ri;
+  double aR[3], ac[3];
+  for (int e = 0; e < 3; ++e) {
+    aR[e] = kr * R[e] - a * c[e];
+    ac[e] = -a * R[e] - kc * c[e];
+    grow[e] -= aR[e];
+  }
+  for (int v = 0; v < 4; ++v) {
+    const double nv = c_qa.phi[q][v];
+    for (int e = 0; e < 3; ++e) {
+      B[3 * v + e] += nv * aR[e];
+      D[3 * v + e] += nv * ac[e];
+    }
+  }
+}
+
 // Plain form. One CTA: 128 rows x a range of panels, FP64 throughout.
 template <int Q1>
 __global__ void __launch_bounds__(128)
@@ -237,13 +268,13 @@ __global__ void __launch_bounds__(128)
 // B and D are linear in the rows, so each thread sums them over its rows,
 // the warp reduces them once per panel and the cross products are taken
 // once per (CTA, panel) in FP64.
-constexpr int kAdjRpt = 4;                  // rows per thread
-constexpr int kAdjRowsCta = 128 * kAdjRpt;  // rows per CTA (consecutive, 128 per warp)
+constexpr int kAdjRpt = 4;                  // rows per thread: r0 + 128 j + tid, j < kAdjRpt
+constexpr int kAdjRowsCta = 128 * kAdjRpt;  // rows per CTA
 static_assert(kMaxSet % 4 == 0, "double-node sets are read as int4");
 static_assert(kAdjRpt * kAdjChunk <= 32, "near mask of a chunk in one word");
 
 // Per (panel, regular point), once per adjoint call:
-//   recd (12 doubles): the FP64 point data of adj_point (near pairs);
+//   recd (12 doubles): x, c = jx x je, w'phi, w'dn |c|, w'dn / |c| (near pairs);
 //   recf (3 float4):   (x_hi, c.x), (x_lo, c.y), (c.z, w'phi, w'dn |c|, w'dn / |c|)
 //                      with x = x_hi + x_lo and c = jx x je;
 // per panel pgeo (12 doubles): E0, E1, F0, F1.
@@ -259,10 +290,11 @@ __global__ void k_adj_points(int C, const double* __restrict__ X,
   const int4 d = cell_dofs[cell];
   double p[kPt];
   adj_point(X, d, q, phi, dn, p);
-  double* pd = recd + (size_t)t * kPt;
-  for (int e = 0; e < kPt; ++e) pd[e] = p[e];
   const double c0 = p[4] * p[8] - p[5] * p[7], c1 = p[5] * p[6] - p[3] * p[8],
                c2 = p[3] * p[7] - p[4] * p[6];
+  const double rd[kPt] = {p[0], p[1], p[2], c0, c1, c2, p[10], p[11] * p[9], p[11] / p[9], 0.0, 0.0, 0.0};
+  double* pd = recd + (size_t)t * kPt;
+  for (int e = 0; e < kPt; ++e) pd[e] = rd[e];
   float hi[3], lo[3];
   for (int e = 0; e < 3; ++e) {
     hi[e] = (float)p[e];
@@ -289,33 +321,35 @@ __global__ void k_adj_points(int C, const double* __restrict__ X,
 
 // Sum of v[0..23] over the 32 lanes of the warp by reduce-scatter (27
 // shuffles): lane l returns the sums of v[3 (l >> 2) + i], i = 0..2.
-__device__ __forceinline__ void warp_sum24(const float v[24], int lane, float out[3]) {
+template <typename T>
+__device__ __forceinline__ void warp_sum24(const T v[24], int lane, T out[3]) {
   const bool h1 = lane & 16, h2 = lane & 8, h3 = lane & 4;
-  float w[12], x[6];
+  T w[12], x[6];
 #pragma unroll
   for (int i = 0; i < 12; ++i) {
-    const float keep = h1 ? v[12 + i] : v[i], send = h1 ? v[i] : v[12 + i];
+    const T keep = h1 ? v[12 + i] : v[i], send = h1 ? v[i] : v[12 + i];
     w[i] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
   }
 #pragma unroll
   for (int i = 0; i < 6; ++i) {
-    const float keep = h2 ? w[6 + i] : w[i], send = h2 ? w[i] : w[6 + i];
+    const T keep = h2 ? w[6 + i] : w[i], send = h2 ? w[i] : w[6 + i];
     x[i] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
   }
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    const float keep = h3 ? x[3 + i] : x[i], send = h3 ? x[i] : x[3 + i];
-    float y = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    const T keep = h3 ? x[3 + i] : x[i], send = h3 ? x[i] : x[3 + i];
+    T y = keep + __shfl_xor_sync(0xffffffffu, send, 4);
     y += __shfl_xor_sync(0xffffffffu, y, 2);
     y += __shfl_xor_sync(0xffffffffu, y, 1);
     out[i] = y;
   }
 }
 
-// One CTA: kAdjRowsCta rows (kAdjRpt consecutive rows per thread) x a range
-// of panels, in chunks of kAdjChunk panels whose FP32 point data (offsets from
-// the CTA's first row, so that the FP32 differences stay accurate) sit in
-// shared memory.
+// One CTA: kAdjRowsCta consecutive rows (kAdjRpt per thread, 128 apart, so
+// that the near rows of a panel fall on different lanes) x a range of panels,
+// in chunks of kAdjChunk panels whose FP32 point data (offsets from the CTA's
+// first row, so that the FP32 differences stay accurate) sit in shared memory.
+// Near pairs add their FP64 moments to the same per-panel sums.
 template <int Q1>
 __global__ void __launch_bounds__(128, 4)
     k_adj_tile_mixed(int N, int C, const double* __restrict__ X, const int* __restrict__ dnset,
@@ -327,7 +361,7 @@ __global__ void __launch_bounds__(128, 4)
   constexpr int NQ = Q1 * Q1;
   __shared__ __align__(16) float sp[kAdjChunk][NQ][12];
   __shared__ float wmom[4][kAdjChunk][24];
-  __shared__ double wnear[4][kAdjChunk][12];
+  __shared__ double wnmom[4][kAdjChunk][24];  // near-pair moments per warp
   __shared__ double smom[kAdjChunk][24];
   __shared__ double sgrow[kAdjRpt][3][128];
   __shared__ float sxf[kAdjRpt][3][128];
@@ -337,7 +371,6 @@ __global__ void __launch_bounds__(128, 4)
   __shared__ float cTs[6];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int r0 = blockIdx.y * kAdjRowsCta;
-  const int rbase = r0 + kAdjRpt * tid;
   if (tid < 3) {
     const double c = X[3 * (size_t)r0 + tid];
     const float hi = (float)c;
@@ -350,7 +383,7 @@ __global__ void __launch_bounds__(128, 4)
   unsigned live = 0;
 #pragma unroll
   for (int j = 0; j < kAdjRpt; ++j) {
-    const int row = rbase + j;
+    const int row = r0 + 128 * j + tid;
     double x[3] = {cTd[0], cTd[1], cTd[2]}, li = 0, ph = 0;
     if (row < N) {
       for (int e = 0; e < 3; ++e) x[e] = X[3 * (size_t)row + e];
@@ -455,7 +488,7 @@ __global__ void __launch_bounds__(128, 4)
         }
       }
       float o3[3];
-      warp_sum24(v, lane, o3);
+      warp_sum24<float>(v, lane, o3);
       if ((lane & 3) == 0)
         for (int i = 0; i < 3; ++i) wmom[warp][k][3 * (lane >> 2) + i] = o3[i];
     }
@@ -466,14 +499,14 @@ __global__ void __launch_bounds__(128, 4)
     for (int k = 0; k < cnt; ++k) {
       unsigned nm = (nmask >> (kAdjRpt * k)) & ((1u << kAdjRpt) - 1u);
       if (__any_sync(0xffffffffu, nm != 0u)) {
-        double g64[12];
-        for (int t = 0; t < 12; ++t) g64[t] = 0.0;
+        double m64[24];
+        for (int t = 0; t < 24; ++t) m64[t] = 0.0;
         const int4 d = sdofs[k];
         const double* pc = recd + (size_t)(cb + k) * NQ * kPt;
         while (nm) {
           const int j = __ffs(nm) - 1;
           nm &= nm - 1u;
-          const int row = rbase + j;
+          const int row = r0 + 128 * j + tid;
           const int4* s4 = reinterpret_cast<const int4*>(dnset + (size_t)row * kMaxSet);
           bool sing = false;
           for (int h = 0; h < kMaxSet / 4; ++h) {
@@ -484,25 +517,26 @@ __global__ void __launch_bounds__(128, 4)
           }
           if (sing) continue;
           const double xi[3] = {X[3 * (size_t)row], X[3 * (size_t)row + 1], X[3 * (size_t)row + 2]};
-          const double li = lam[row], phii = phi[row];
+          const double li = lam[row], lpw = li * phi[row] * kI4P;
           double grow[3] = {0.0, 0.0, 0.0};
-          for (int q = 0; q < NQ; ++q) adj_point_terms(pc + q * kPt, q, xi, li, phii, g64, grow);
+          for (int q = 0; q < NQ; ++q)
+            adj_near_moments(pc + q * kPt, q, xi, li, lpw, m64, m64 + 12, grow);
           for (int e = 0; e < 3; ++e) sgrow[j][e][tid] += grow[e];
         }
-        for (int t = 0; t < 12; ++t) {
-          double s = g64[t];
-          for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-          if (lane == 0) wnear[warp][k][t] = s;
-        }
-      } else if (lane == 0) {
-        for (int t = 0; t < 12; ++t) wnear[warp][k][t] = 0.0;
+        double n3[3];
+        warp_sum24<double>(m64, lane, n3);
+        if ((lane & 3) == 0)
+          for (int i = 0; i < 3; ++i) wnmom[warp][k][3 * (lane >> 2) + i] = n3[i];
+      } else if (lane < 24) {
+        wnmom[warp][k][lane] = 0.0;
       }
     }
     __syncthreads();
     for (int t = tid; t < cnt * 24; t += 128) {
       const int k = t / 24, m = t - 24 * k;
       smom[k][m] = ((double)wmom[0][k][m] + (double)wmom[1][k][m]) +
-                   ((double)wmom[2][k][m] + (double)wmom[3][k][m]);
+                   ((double)wmom[2][k][m] + (double)wmom[3][k][m]) +
+                   ((wnmom[0][k][m] + wnmom[1][k][m]) + (wnmom[2][k][m] + wnmom[3][k][m]));
     }
     __syncthreads();
     for (int t = tid; t < cnt * 12; t += 128) {
@@ -518,15 +552,14 @@ __global__ void __launch_bounds__(128, 4)
       const int iy = w & 1;
       const double ys = D[3 * iy + e1] * G[6 + e2] - D[3 * iy + e2] * G[6 + e1] +
                         D[3 * iy + 6 + e1] * G[9 + e2] - D[3 * iy + 6 + e2] * G[9 + e1];
-      double val = smom[k][o] + ((w & 1) ? xs : -xs) + (w >= 2 ? ys : -ys);
-      val += (wnear[0][k][o] + wnear[1][k][o]) + (wnear[2][k][o] + wnear[3][k][o]);
+      const double val = smom[k][o] + ((w & 1) ? xs : -xs) + (w >= 2 ? ys : -ys);
       gcell_part[((size_t)blockIdx.y * C + cb + k) * 12 + o] = val;
     }
   }
   // each thread reads back only the entries of sgrow it wrote itself
 #pragma unroll
   for (int j = 0; j < kAdjRpt; ++j) {
-    const int row = rbase + j;
+    const int row = r0 + 128 * j + tid;
     if (row < N)
       for (int e = 0; e < 3; ++e)
         grow_part[((size_t)blockIdx.x * N + row) * 3 + e] = sgrow[j][e][tid];
