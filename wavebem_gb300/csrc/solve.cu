@@ -186,11 +186,6 @@ template <>
 __device__ __forceinline__ double load_entry<double>(const double* p) {
   return __ldcs(p);
 }
-template <>
-__device__ __forceinline__ double load_entry<float2>(const float2* p) {
-  const float2 v = __ldcs(p);
-  return (double)v.x + (double)v.y;
-}
 
 // sel: the column mask that picks N or -D (NULL: Nm already holds the
 // selected operator)
@@ -230,10 +225,48 @@ cudaError_t launch_matvec_t_fp64(int N, const double* Nm, const double* Dm, cons
   return cudaGetLastError();
 }
 
+// Transposed operator with (hi, lo) float pairs (P = A2 or B2, selection
+// applied at assembly): threads own columns, blocks own a column strip and a
+// slice of rows; the slice's x is split into float pairs in shared memory and
+// products and sums run in double-float on FP32 units, as in k_matvec_mixed.
+constexpr int kMvtChunk = 256;
+__global__ void __launch_bounds__(kMvtCols)
+    k_matvec_t_mixed(int N, const float2* __restrict__ P, const double* __restrict__ x,
+                     double* __restrict__ part) {
+  __shared__ float2 xs[kMvtChunk];
+  const int col = blockIdx.x * kMvtCols + threadIdx.x;
+  const int slice = blockIdx.y;
+  const int rows_per = (N + kMvtSlices - 1) / kMvtSlices;
+  const int r0 = slice * rows_per, r1 = min(N, r0 + rows_per);
+  const bool active = col < N;
+  df acc = {0.f, 0.f};
+  for (int i0 = r0; i0 < r1; i0 += kMvtChunk) {
+    const int n = min(kMvtChunk, r1 - i0);
+    __syncthreads();
+    for (int k = threadIdx.x; k < n; k += kMvtCols) {
+      const df v = df_from_double(x[i0 + k]);
+      xs[k] = make_float2(v.hi, v.lo);
+    }
+    __syncthreads();
+    if (active) {
+      const float2* a_col = P + (size_t)i0 * N + col;
+#pragma unroll 8
+      for (int k = 0; k < n; ++k) {
+        const float2 a = __ldcs(a_col + (size_t)k * N);
+        const float2 xv = xs[k];
+        df p = two_prod(a.x, xv.x);
+        p.lo = __fmaf_rn(a.x, xv.y, __fmaf_rn(a.y, xv.x, p.lo));
+        acc = df_add(acc, p);
+      }
+    }
+  }
+  if (active) part[(size_t)slice * N + col] = df_to_double(acc);
+}
+
 cudaError_t launch_matvec_t_mixed(int N, const float2* P, const uint8_t* mask, const double* alpha,
                                   const double* x, double* y, double* part, cudaStream_t s) {
   dim3 g((N + kMvtCols - 1) / kMvtCols, kMvtSlices);
-  k_matvec_t<float2><<<g, kMvtCols, 0, s>>>(N, P, P, nullptr, x, part);
+  k_matvec_t_mixed<<<g, kMvtCols, 0, s>>>(N, P, x, part);
   k_matvec_t_finish<<<(N + 255) / 256, 256, 0, s>>>(N, mask, alpha, x, part, y);
   return cudaGetLastError();
 }
