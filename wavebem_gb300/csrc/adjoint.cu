@@ -55,15 +55,14 @@ static int hull_dofs_upload(wbem_context* h, const int* hull_cells, int n_hull, 
 int hull_force_dev(wbem_context* h, const int* hull_cells, int n_hull, const double* U, int dir,
                    const double* d_phi, const double* d_dphi, double* force) {
   int4* hd = nullptr;
-  WB_CHK(hull_dofs_upload(h, hull_cells, n_hull, &hd));
   double* part = nullptr;
+  DeviceFreeGuard scratch{{reinterpret_cast<void**>(&hd), reinterpret_cast<void**>(&part)}};
+  WB_CHK(hull_dofs_upload(h, hull_cells, n_hull, &hd));
   cudaError_t e = cudaMalloc(&part, sizeof(double) * (n_hull + 1));
   if (e == cudaSuccess) e = launch_hull_force(n_hull, hd, h->d_X, U, dir, d_phi, d_dphi, part, h->stream);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(force, part + n_hull, sizeof(double), cudaMemcpyDeviceToHost, h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-  if (part) cudaFree(part);
-  cudaFree(hd);
   if (e != cudaSuccess) return fail(h, WBEM_ERR_CUDA, cudaGetErrorString(e));
   return WBEM_OK;
 }
@@ -743,25 +742,32 @@ int adjoint_force(wbem_context* h, const int* hull_cells, int n_hull, const doub
   const bool mixed = h->assembled_prec == WBEM_PREC_MIXED;
   WB_CHK(ensure_vectors(h, h->opt.gmres_restart));
   EvTimer tm(h->stream);
+  int4* hd = nullptr;
+  int *d_hoc = nullptr, *d_cpptr = nullptr, *d_cpidx = nullptr;
+  double *d_ghull = nullptr, *d_gph = nullptr, *d_gpn = nullptr;
+  double *grow_part = nullptr, *gcell_part = nullptr, *grow_sing = nullptr, *gpair = nullptr;
+  double *recd = nullptr, *pgeo = nullptr;
+  float4* recf = nullptr;
+  double *d_out = nullptr, *d_nph = nullptr;
+  DeviceFreeGuard scratch{{reinterpret_cast<void**>(&hd), reinterpret_cast<void**>(&d_hoc),
+                           reinterpret_cast<void**>(&d_cpptr), reinterpret_cast<void**>(&d_cpidx),
+                           reinterpret_cast<void**>(&d_ghull), reinterpret_cast<void**>(&d_gph),
+                           reinterpret_cast<void**>(&d_gpn), reinterpret_cast<void**>(&grow_part),
+                           reinterpret_cast<void**>(&gcell_part),
+                           reinterpret_cast<void**>(&grow_sing), reinterpret_cast<void**>(&gpair),
+                           reinterpret_cast<void**>(&recd), reinterpret_cast<void**>(&pgeo),
+                           reinterpret_cast<void**>(&recf), reinterpret_cast<void**>(&d_out),
+                           reinterpret_cast<void**>(&d_nph)}};
   // hull panel data
   std::vector<int> hull_ids;
-  int4* hd = nullptr;
   WB_CHK(hull_dofs_upload(h, hull_cells, n_hull, &hd, &hull_ids));
   std::vector<int> hoc(C, -1);
   for (int k = 0; k < n_hull; ++k) hoc[hull_ids[k]] = k;
-  int* d_hoc = nullptr;
-  double *d_ghull = nullptr, *d_gph = nullptr, *d_gpn = nullptr;
   // panels per CTA column and rows per CTA of the tile kernel
   const int cpb = mixed ? 128 : 64;
   const int rows_cta = mixed ? kAdjRowsCta : 128;
   const int n_cb = (C + cpb - 1) / cpb, n_rb = (N + rows_cta - 1) / rows_cta;
   const size_t npts = (size_t)C * q1 * q1;
-  double *grow_part = nullptr, *gcell_part = nullptr, *grow_sing = nullptr, *gpair = nullptr;
-  double *recd = nullptr, *pgeo = nullptr;
-  float4* recf = nullptr;
-  int *d_cpptr = nullptr, *d_cpidx = nullptr;
-  double* d_out = nullptr;
-  double* d_nph = nullptr;
   int st = WBEM_OK;
   // cell -> singular pair index lists (inverse of the per-row singular lists)
   std::vector<int> sptr(N + 1), scell;
@@ -889,10 +895,6 @@ int adjoint_force(wbem_context* h, const int* hull_cells, int n_hull, const doub
     (void)tmp_rhs;
     h->stats.t_adjoint_ms = tm.ms();
   } while (0);
-  void* fr[] = {hd, d_hoc, d_ghull, d_gph, d_gpn, grow_part, gcell_part, grow_sing, gpair,
-                d_cpptr, d_cpidx, d_out, d_nph, recd, recf, pgeo};
-  for (void* p : fr)
-    if (p) cudaFree(p);
   return st;
 }
 

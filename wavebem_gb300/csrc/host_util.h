@@ -42,6 +42,18 @@ int upload(wbem_context* h, T** p, const std::vector<T>& v) {
 
 int check_device_error(wbem_context* h, const char* what);
 
+// Frees the device pointers held in the listed variables when it goes out of
+// scope. The variables are read at that point, so buffers allocated after the
+// guard was set up are freed on every return path, early error returns
+// included.
+struct DeviceFreeGuard {
+  std::vector<void**> slots;
+  ~DeviceFreeGuard() {
+    for (void** s : slots)
+      if (*s) cudaFree(*s);
+  }
+};
+
 struct EvTimer {
   cudaEvent_t a, b;
   cudaStream_t s;
