@@ -377,7 +377,7 @@ def run_gpu(args, rank, world, local):
     g.close()
     del g
 
-    # configs[3]-style adjoint workload: N = 8,192 with shape parameters
+    # shape-parameter adjoint workload: N = 8,192 Wigley hull with 8 seeded shape parameters
     rng = np.random.default_rng(7)
     m8 = M.wigley_mesh(8192, a=rng.normal(0.0, 1e-3, 8))
     p8, i8 = M.double_nodes(m8.X, m8.cells)

@@ -1,7 +1,7 @@
 """Adjoint of assemble + solve + hull force against central finite
 differences (h = 1e-6) of the FP64 forward map, and mixed against FP64.
 
-The configs[3]-style check: Wigley hull offset perturbed by
+The shape-parameter check: Wigley hull offset perturbed by
 sum_j a_j sin(j pi (x + 0.5)) (1 - (z/T)^2); gradient with respect to the a_j
 through X(a) and the Neumann data b(a) = -U . n(a), chained in a
 torch.autograd.Function wrapper (test harness only)."""

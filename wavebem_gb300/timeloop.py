@@ -1,4 +1,5 @@
-"""Stand-in for the reference's time-integrated run (configs[4]).
+"""Stand-in for the reference's time-integrated run (100 BDF steps of the
+Wigley tank at N = 12,000).
 
 The reference integrates its free-surface DAE with SUNDIALS IDA (BDF,
 `source/dae_time_integrator.cc:212-305`). Each residual evaluation of the
