@@ -155,6 +155,15 @@ int wbem_hull_force(wbem_handle h, const int* hull_cells, int n_hull, const doub
 int wbem_force_adjoint(wbem_handle h, const int* hull_cells, int n_hull, const double* U, int dir,
                        const double* tmp_rhs, double* dF_dX, double* dF_drhs);
 
+/* Adjoint of assemble + solve_system for any objective J(phi, dphi_dn) of the
+ * last solution (J with no direct dependence on the node positions): given
+ * dJ/dphi and dJ/d(dphi_dn) per node (N each, caller order, both the known and
+ * the solved entries), returns dJ/dX (N x 3, tmp_rhs held fixed) and
+ * dJ/dtmp_rhs (N). Same transposed solve and tile recomputation as
+ * wbem_force_adjoint. No counterpart in the reference. */
+int wbem_adjoint(wbem_handle h, const double* dJ_dphi, const double* dJ_ddn, double* dJ_dX,
+                 double* dJ_drhs);
+
 int wbem_get_stats(wbem_handle h, wbem_stats* st);
 
 #ifdef __cplusplus

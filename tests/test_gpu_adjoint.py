@@ -185,3 +185,36 @@ def test_adjoint_matches_oracle_directional_differences(prec):
     # ~1e-9 and its gradient by <= 1e-6 (test_adjoint_mixed_matches_fp64)
     tol = 1e-6 if prec == PREC_FP64 else 2e-6
     assert abs(ad - fd) <= tol * abs(fd), (ad, fd)
+
+
+def test_adjoint_of_a_linear_objective_fp64_and_mixed():
+    """wbem_adjoint for J = c . phi + d . dphi_dn (all entries, known and
+    solved) against central differences, along a smooth displacement of every
+    node (coincident double-node copies move together) and along the known
+    data; the mixed form against the FP64 form."""
+    m, ptr, idx, _ = _setup(800, None)
+    b = M.wigley_bc(m, seed=3)
+    rng = np.random.default_rng(11)
+    c = rng.normal(size=m.n_dofs)
+    dd = rng.normal(size=m.n_dofs)
+
+    def J(X, bb, prec=PREC_FP64):
+        g = BEMProblem(X, m.cells, m.dirichlet, ptr, idx, precision=prec, tolerance=1e-14)
+        phi, dphi = bb.copy(), bb.copy()
+        g.solve(phi, dphi, bb)
+        return g, float(c @ phi + dd @ dphi)
+
+    g, _ = J(m.X, b)
+    gX, gb = g.adjoint(c, dd)
+    A = rng.normal(size=(3, 3))
+    d = 0.1 * np.sin(m.X @ A + rng.uniform(0, 2 * np.pi, 3))
+    h = 1e-6
+    fd = (J(m.X + h * d, b)[1] - J(m.X - h * d, b)[1]) / (2 * h)
+    assert abs(float(np.sum(gX * d)) - fd) <= 1e-6 * abs(fd), (float(np.sum(gX * d)), fd)
+    db = rng.normal(size=len(b))
+    fd = (J(m.X, b + h * db)[1] - J(m.X, b - h * db)[1]) / (2 * h)
+    assert abs(float(gb @ db) - fd) <= 1e-6 * abs(fd), (float(gb @ db), fd)
+    gm, _ = J(m.X, b, PREC_MIXED)
+    gXm, gbm = gm.adjoint(c, dd)
+    assert rel2(gXm, gX) <= 1e-6
+    assert rel2(gbm, gb) <= 1e-6

@@ -32,7 +32,7 @@ EXPORTS = ["wbem_default_options", "wbem_create", "wbem_destroy", "wbem_last_err
            "wbem_set_geometry", "wbem_update_nodes", "wbem_set_bc", "wbem_assemble",
            "wbem_solve_system", "wbem_solve", "wbem_get_alpha", "wbem_get_matrices",
            "wbem_vmult", "wbem_compute_rhs", "wbem_residual", "wbem_hull_force", "wbem_force_adjoint",
-           "wbem_get_stats"]
+           "wbem_adjoint", "wbem_get_stats"]
 
 
 class WBEMError(RuntimeError):
@@ -96,6 +96,7 @@ def load_library(path: str = LIB_PATH):
     L.wbem_residual.argtypes = [H, dp, dp, dp]
     L.wbem_hull_force.argtypes = [H, ip, C.c_int, dp, C.c_int, dp, dp, C.POINTER(C.c_double)]
     L.wbem_force_adjoint.argtypes = [H, ip, C.c_int, dp, C.c_int, dp, dp, dp]
+    L.wbem_adjoint.argtypes = [H, dp, dp, dp, dp]
     L.wbem_get_stats.argtypes = [H, C.POINTER(Stats)]
     L.wbem_test_lu_factors.argtypes = [H, C.c_void_p, C.c_void_p, C.c_void_p]
     L.wbem_test_lu_apply.argtypes = [H, dp, dp, C.c_int]
@@ -251,6 +252,17 @@ class BEMProblem:
         hc = np.ascontiguousarray(hull_cells, np.int32)
         self._check(self.L.wbem_force_adjoint(self.h, hc, hc.size, _f64(U), int(direction),
                                               _f64(tmp_rhs), gX, gb))
+        return gX.reshape(-1, 3), gb
+
+    def adjoint(self, dJ_dphi, dJ_ddn):
+        """dJ/dX (N,3) with tmp_rhs fixed, and dJ/dtmp_rhs (N,), at the last solve,
+        for an objective J(phi, dphi_dn) with the given partial derivatives."""
+        a, c = _f64(dJ_dphi).ravel(), _f64(dJ_ddn).ravel()
+        if a.size != self.n_dofs or c.size != self.n_dofs:
+            raise ValueError("dJ_dphi and dJ_ddn need one entry per dof")
+        gX = np.zeros(3 * self.n_dofs)
+        gb = np.zeros(self.n_dofs)
+        self._check(self.L.wbem_adjoint(self.h, a, c, gX, gb))
         return gX.reshape(-1, 3), gb
 
     def lu_factors(self):

@@ -734,8 +734,13 @@ static cudaError_t launch_adj_mixed_t(int N, int C, const double* X, const int* 
   return cudaGetLastError();
 }
 
-int adjoint_force(wbem_context* h, const int* hull_cells, int n_hull, const double* U, int dir,
-                  const double* tmp_rhs, double* dF_dX, double* dF_drhs) {
+// Adjoint of assemble + solve_system for an objective J(X, phi, dphi_dn). Its
+// direct partial derivatives come either from the hull force (hull_cells
+// given: dF/dphi, dF/ddn and dF/dX|direct of the hull panels) or from the
+// caller (dJ_dphi, dJ_ddn per node in caller order, no direct X term).
+static int adjoint_run(wbem_context* h, const int* hull_cells, int n_hull, const double* U, int dir,
+                       const double* dJ_dphi, const double* dJ_ddn, double* dF_dX,
+                       double* dF_drhs) {
   const int N = h->N, C = h->C;
   const int q1 = h->opt.quadrature_order;
   if (q1 < 2 || q1 > 6) return fail(h, WBEM_ERR_ARG, "adjoint supports quadrature orders 2..6");
@@ -811,8 +816,18 @@ int adjoint_force(wbem_context* h, const int* hull_cells, int n_hull, const doub
     const int bs = 256, nb = (N + bs - 1) / bs;
     // fields and direct force derivatives
     k_fields<<<nb, bs, 0, h->stream>>>(N, h->d_mask, h->d_sol, h->d_b, phi, dn);
-    WB_CU(launch_hull_force_grad(n_hull, hd, h->d_X, U, dir, phi, dn, d_ghull, d_gph, d_gpn, h->stream));
-    k_hull_node_sum<<<nb, bs, 0, h->stream>>>(N, h->d_ncptr, h->d_ncent, d_hoc, d_gph, d_gpn, nph, npn);
+    if (hull_cells) {
+      WB_CU(launch_hull_force_grad(n_hull, hd, h->d_X, U, dir, phi, dn, d_ghull, d_gph, d_gpn, h->stream));
+      k_hull_node_sum<<<nb, bs, 0, h->stream>>>(N, h->d_ncptr, h->d_ncent, d_hoc, d_gph, d_gpn, nph, npn);
+    } else {
+      std::vector<double> dj(2 * (size_t)N);
+      for (int i = 0; i < N; ++i) {
+        dj[i] = dJ_dphi[h->perm[i]];
+        dj[N + i] = dJ_ddn[h->perm[i]];
+      }
+      WB_CU(cudaMemcpyAsync(d_nph, dj.data(), sizeof(double) * 2 * N, cudaMemcpyHostToDevice, h->stream));
+      WB_CU(cudaStreamSynchronize(h->stream));
+    }
     k_gx<<<nb, bs, 0, h->stream>>>(N, h->d_mask, nph, npn, gx);
     WB_CU(cudaGetLastError());
     // transposed solve A^T lambda = g_x (constrained operator)
@@ -863,7 +878,7 @@ int adjoint_force(wbem_context* h, const int* hull_cells, int n_hull, const doub
     double* gb = h->d_vec[0];
     k_gb<<<nb, bs, 0, h->stream>>>(N, h->d_mask, nph, npn, bt, h->d_alpha, lamu, gb);
     WB_CU(cudaGetLastError());
-    h->launches += mixed ? 13 : 12;
+    h->launches += (mixed ? 13 : 12) - (hull_cells ? 0 : 2);
     WB_CHK(check_device_error(h, "adjoint"));
     // back to the caller's order; constraint inhomogeneities tied to b
     std::vector<double> gXi(3 * (size_t)N), gbi(N), li(N);
@@ -892,10 +907,19 @@ int adjoint_force(wbem_context* h, const int* hull_cells, int n_hull, const doub
         if (o != i && !h->mask[o]) dF_drhs[i] += li[h->iperm[o]];
       }
     }
-    (void)tmp_rhs;
     h->stats.t_adjoint_ms = tm.ms();
   } while (0);
   return st;
+}
+
+int adjoint_force(wbem_context* h, const int* hull_cells, int n_hull, const double* U, int dir,
+                  double* dF_dX, double* dF_drhs) {
+  return adjoint_run(h, hull_cells, n_hull, U, dir, nullptr, nullptr, dF_dX, dF_drhs);
+}
+
+int adjoint_objective(wbem_context* h, const double* dJ_dphi, const double* dJ_ddn, double* dJ_dX,
+                      double* dJ_drhs) {
+  return adjoint_run(h, nullptr, 0, nullptr, 0, dJ_dphi, dJ_ddn, dJ_dX, dJ_drhs);
 }
 
 }  // namespace wbem

@@ -29,7 +29,9 @@ int assemble_mixed(wbem_context* h);
 int factor_mixed(wbem_context* h);
 void free_mixed(wbem_context* h);
 int adjoint_force(wbem_context* h, const int* hull_cells, int n_hull, const double* U, int dir,
-                  const double* tmp_rhs, double* dF_dX, double* dF_drhs);
+                  double* dF_dX, double* dF_drhs);
+int adjoint_objective(wbem_context* h, const double* dJ_dphi, const double* dJ_ddn, double* dJ_dX,
+                      double* dJ_drhs);
 int hull_force_dev(wbem_context* h, const int* hull_cells, int n_hull, const double* U, int dir,
                    const double* d_phi, const double* d_dphi, double* force);
 }  // namespace wbem
@@ -1584,7 +1586,16 @@ int wbem_force_adjoint(wbem_handle h, const int* hull_cells, int n_hull, const d
     return fail(h, WBEM_ERR_ARG, "wbem_force_adjoint: bad argument");
   if (!h->have_solution) return fail(h, WBEM_ERR_STATE, "wbem_force_adjoint: solve first");
   cudaSetDevice(h->device);
-  return adjoint_force(h, hull_cells, n_hull, U, dir, tmp_rhs, dF_dX, dF_drhs);
+  return adjoint_force(h, hull_cells, n_hull, U, dir, dF_dX, dF_drhs);
+}
+
+int wbem_adjoint(wbem_handle h, const double* dJ_dphi, const double* dJ_ddn, double* dJ_dX,
+                 double* dJ_drhs) {
+  if (!h) return WBEM_ERR_ARG;
+  if (!dJ_dphi || !dJ_ddn || !dJ_dX || !dJ_drhs) return fail(h, WBEM_ERR_ARG, "wbem_adjoint: NULL pointer");
+  if (!h->have_solution) return fail(h, WBEM_ERR_STATE, "wbem_adjoint: solve first");
+  cudaSetDevice(h->device);
+  return adjoint_objective(h, dJ_dphi, dJ_ddn, dJ_dX, dJ_drhs);
 }
 
 int wbem_set_profiling(wbem_handle h, int on) {
