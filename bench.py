@@ -55,8 +55,11 @@ def dist_init(args):
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl" if args.impl == "gb300" else "gloo")
+        gpu_arm = args.impl == "gb300"
+        if gpu_arm:
+            torch.cuda.set_device(local)
+        # the reference arm runs on the host cores: gloo, no device
+        dist.init_process_group("nccl" if gpu_arm else "gloo")
     return rank, world, local
 
 
@@ -71,7 +74,8 @@ def allmax(world, v):
         return v
     import torch
     import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
