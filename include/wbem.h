@@ -160,7 +160,9 @@ int wbem_force_adjoint(wbem_handle h, const int* hull_cells, int n_hull, const d
  * dJ/dphi and dJ/d(dphi_dn) per node (N each, caller order, both the known and
  * the solved entries), returns dJ/dX (N x 3, tmp_rhs held fixed) and
  * dJ/dtmp_rhs (N). Same transposed solve and tile recomputation as
- * wbem_force_adjoint. No counterpart in the reference. */
+ * wbem_force_adjoint. No counterpart in the reference.
+ * Array lengths (N = n_dofs of the last wbem_set_geometry): dJ_dphi N,
+ * dJ_ddn N, dJ_dX 3 N, dJ_drhs N doubles; the library cannot check them. */
 int wbem_adjoint(wbem_handle h, const double* dJ_dphi, const double* dJ_ddn, double* dJ_dX,
                  double* dJ_drhs);
 

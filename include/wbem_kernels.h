@@ -79,10 +79,13 @@ int wbem_set_stream(struct wbem_context* h, void* cuda_stream);
  * returns without waiting; *force is valid once that stream has reached it.
  * Per-panel partial sums live in a fixed 512 KB array inside the library, so
  * n_hull is limited to 65536 (WBEM_ERR_ARG beyond). The first call on a device
- * looks up that array's device address (cudaGetSymbolAddress); make the first
- * call before any stream capture. All calls on a device share the array:
+ * looks up that array's device address (cudaGetSymbolAddress, once per device
+ * and thread-safe); make the first call before any stream capture, and reload
+ * the library after a cudaDeviceReset. All calls on a device share the array:
  * calls whose work overlaps on the GPU (other streams, other handles) race and
- * must be serialised by the caller. An out-of-range panel index gives NaN. */
+ * must be serialised by the caller. The quadrature rule is the handle's, the
+ * one wbem_hull_force uses. The calling thread's current device is the same
+ * on return as on entry. An out-of-range panel index gives NaN. */
 int wbem_hull_force_noalloc(struct wbem_context* h, const int* hull_cells, int n_hull,
                             const double* U, int dir, const double* phi, const double* dphi_dn,
                             double* force, void* stream);

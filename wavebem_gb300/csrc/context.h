@@ -57,6 +57,10 @@ struct wbem_context {
   std::string err;
   wbem_stats stats{};
   wbem_options opt{};
+  // the regular Gauss-Legendre line rule on [0,1] of the last quadrature
+  // set-up (the tensor rule of the panels is its product)
+  int gauss_n = 0;
+  double gauss_x[8] = {}, gauss_w[8] = {};
 
   // ---- host topology (caller order)
   int N = 0, C = 0;

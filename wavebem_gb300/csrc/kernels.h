@@ -14,6 +14,7 @@ constexpr int kMaxSet = 8;         // max size of a double-node set
 constexpr int kMaxQ1 = 8;          // max regular quadrature order per direction
 constexpr int kMaxSingular = 2 * 8 * 8;  // max points of a vertex-singular rule
 constexpr int kBJ = 128;           // block-Jacobi block size
+constexpr int kMaxDev = 64;        // devices a process may drive (per-device launch caches)
 
 // per-panel metadata of a staged chunk (tile entry, vertex dofs, near-test data)
 struct ChunkMeta {

@@ -31,6 +31,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <algorithm>
+#include <atomic>
 #include <vector>
 #include "context.h"
 #include "host_util.h"
@@ -866,18 +868,21 @@ static bool encode_cmap(CUtensorMap* map, const float* base, int rows, int cols,
 static cudaError_t run_gemm(const GemmMaps& mp, const CUtensorMap& cmap, int crow0, int ccol0,
                              int arow0, int brow0, int M, int Nc, int K, DevErr* err, cudaStream_t s,
                              int spare_sms = 0) {
-  static bool attr = false;
-  static int sms = 0;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_gemm_bf16x3, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)gemm_smem());
-    if (e != cudaSuccess) return e;
-    int dev = 0;
-    e = cudaGetDevice(&dev);
+  // per device: the shared-memory attribute is set and the SM count read on
+  // the first launch there (both idempotent, so racing first launches agree)
+  static std::atomic<int> sms_of[kMaxDev];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev >= kMaxDev) return cudaErrorInvalidDevice;
+  int sms = sms_of[dev].load(std::memory_order_acquire);
+  if (sms == 0) {
+    e = cudaFuncSetAttribute(k_gemm_bf16x3, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)gemm_smem());
     if (e != cudaSuccess) return e;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
-    attr = true;
+    sms_of[dev].store(sms, std::memory_order_release);
   }
   const int ntiles = ((M + G3M - 1) / G3M) * ((Nc + G3N - 1) / G3N);
   const int grid = std::min(ntiles, std::max(1, sms - spare_sms));
@@ -942,88 +947,95 @@ __global__ void __launch_bounds__(kTriThreads)
   __shared__ int bad;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const bool fwd = (mode == 0 || mode == 2);
-  const int k = fwd ? blockIdx.x : nblk - 1 - blockIdx.x;
-  const int k0 = k * kNB, nb = min(kNB, N - k0);
   const bool vec4 = (ld & 3) == 0;
-  const float* Dk = dinv + (size_t)k * kNB * kNB;
-  for (int idx = tid; idx < kNB * kNB; idx += kTriThreads) sInv[idx] = Dk[idx];
-  if (tid < kNB) acc[tid] = (tid < nb) ? in[k0 + tid] : 0.f;
   if (tid == 0) bad = 0;
-  const int jbeg = fwd ? 0 : nblk - 1, jend = k, jstep = fwd ? 1 : -1;
-  float t[64];
-  if (jbeg != jend) {
-    const int j0 = jbeg * kNB;
-    tri_load(t, mode, LU, ld, k0, nb, j0, min(kNB, N - j0), vec4);
-  }
-  __syncthreads();
-  for (int j = jbeg; j != jend; j += jstep) {
-    const int j0 = j * kNB, jn = min(kNB, N - j0);
-    if (tid == 0 && !bad) {
-      uint32_t it = 0;
-      while (*((volatile unsigned*)&flags[j]) != epoch) {
-        if (++it > (1u << 26)) {
-          bad = 1;
-          dev_fail(err, WBEM_ERR_TIMEOUT, 71, k, j);
-          break;
+  // A CTA takes the block rows blockIdx.x, blockIdx.x + gridDim.x, ... in
+  // sweep order. Block row b waits only for rows earlier in that order, and
+  // the owner of the earliest unfinished row has finished all of its earlier
+  // rows, so the sweep progresses with any grid size that is co-resident.
+  for (int b = blockIdx.x; b < nblk; b += gridDim.x) {
+    const int k = fwd ? b : nblk - 1 - b;
+    const int k0 = k * kNB, nb = min(kNB, N - k0);
+    const float* Dk = dinv + (size_t)k * kNB * kNB;
+    for (int idx = tid; idx < kNB * kNB; idx += kTriThreads) sInv[idx] = Dk[idx];
+    if (tid < kNB) acc[tid] = (tid < nb) ? in[k0 + tid] : 0.f;
+    const int jbeg = fwd ? 0 : nblk - 1, jend = k, jstep = fwd ? 1 : -1;
+    float t[64];
+    if (jbeg != jend) {
+      const int j0 = jbeg * kNB;
+      tri_load(t, mode, LU, ld, k0, nb, j0, min(kNB, N - j0), vec4);
+    }
+    __syncthreads();
+    for (int j = jbeg; j != jend; j += jstep) {
+      const int j0 = j * kNB, jn = min(kNB, N - j0);
+      if (tid == 0 && !bad) {
+        uint32_t it = 0;
+        while (*((volatile unsigned*)&flags[j]) != epoch) {
+          if (++it > (1u << 26)) {
+            bad = 1;
+            dev_fail(err, WBEM_ERR_TIMEOUT, 71, k, j);
+            break;
+          }
         }
+        __threadfence();
       }
-      __threadfence();
-    }
-    __syncthreads();
-    if (bad) break;
-    if (tid < kNB) v[tid] = (tid < jn) ? __ldcg(out + j0 + tid) : 0.f;
-    __syncthreads();
-    if (mode <= 1) {
-      const float4 vv = reinterpret_cast<const float4*>(v)[lane];
+      __syncthreads();
+      if (bad) break;
+      if (tid < kNB) v[tid] = (tid < jn) ? __ldcg(out + j0 + tid) : 0.f;
+      __syncthreads();
+      if (mode <= 1) {
+        const float4 vv = reinterpret_cast<const float4*>(v)[lane];
 #pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        float s2 = t[4 * i] * vv.x;
-        s2 = __fmaf_rn(t[4 * i + 1], vv.y, s2);
-        s2 = __fmaf_rn(t[4 * i + 2], vv.z, s2);
-        s2 = __fmaf_rn(t[4 * i + 3], vv.w, s2);
+        for (int i = 0; i < 16; ++i) {
+          float s2 = t[4 * i] * vv.x;
+          s2 = __fmaf_rn(t[4 * i + 1], vv.y, s2);
+          s2 = __fmaf_rn(t[4 * i + 2], vv.z, s2);
+          s2 = __fmaf_rn(t[4 * i + 3], vv.w, s2);
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s2 += __shfl_xor_sync(0xffffffffu, s2, o);
-        if (lane == 0) acc[warp * 16 + i] -= s2;
+          for (int o = 16; o > 0; o >>= 1) s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+          if (lane == 0) acc[warp * 16 + i] -= s2;
+        }
+      } else {
+        // four independent partial sums (the dot product is on the chain)
+        const int c = tid & (kNB - 1), h = tid >> 7;
+        float q0 = 0.f, q1 = 0.f, q2 = 0.f, q3 = 0.f;
+#pragma unroll
+        for (int i = 0; i < 64; i += 4) {
+          q0 = __fmaf_rn(t[i], v[h + 2 * i], q0);
+          q1 = __fmaf_rn(t[i + 1], v[h + 2 * i + 2], q1);
+          q2 = __fmaf_rn(t[i + 2], v[h + 2 * i + 4], q2);
+          q3 = __fmaf_rn(t[i + 3], v[h + 2 * i + 6], q3);
+        }
+        part[h * kNB + c] = (q0 + q1) + (q2 + q3);
       }
-    } else {
-      // four independent partial sums (the dot product is on the chain)
-      const int c = tid & (kNB - 1), h = tid >> 7;
-      float q0 = 0.f, q1 = 0.f, q2 = 0.f, q3 = 0.f;
-#pragma unroll
-      for (int i = 0; i < 64; i += 4) {
-        q0 = __fmaf_rn(t[i], v[h + 2 * i], q0);
-        q1 = __fmaf_rn(t[i + 1], v[h + 2 * i + 2], q1);
-        q2 = __fmaf_rn(t[i + 2], v[h + 2 * i + 4], q2);
-        q3 = __fmaf_rn(t[i + 3], v[h + 2 * i + 6], q3);
+      // prefetch the next block while the next flag is pending
+      const int jn2 = j + jstep;
+      if (jn2 != jend) {
+        const int j02 = jn2 * kNB;
+        tri_load(t, mode, LU, ld, k0, nb, j02, min(kNB, N - j02), vec4);
       }
-      part[h * kNB + c] = (q0 + q1) + (q2 + q3);
+      __syncthreads();
+      if (mode >= 2 && tid < kNB) acc[tid] -= part[tid] + part[kNB + tid];
+      __syncthreads();
     }
-    // prefetch the next block while the next flag is pending
-    const int jn2 = j + jstep;
-    if (jn2 != jend) {
-      const int j02 = jn2 * kNB;
-      tri_load(t, mode, LU, ld, k0, nb, j02, min(kNB, N - j02), vec4);
-    }
-    __syncthreads();
-    if (mode >= 2 && tid < kNB) acc[tid] -= part[tid] + part[kNB + tid];
-    __syncthreads();
-  }
-  // diagonal block (four independent partial sums: this is on the chain)
-  if (tid < kNB) {
-    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    // diagonal block (four independent partial sums: this is on the chain)
+    if (tid < kNB) {
+      float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
 #pragma unroll 4
-    for (int c = 0; c < kNB; c += 4) {
-      s0 = __fmaf_rn(sInv[c * kNB + tid], acc[c], s0);
-      s1 = __fmaf_rn(sInv[(c + 1) * kNB + tid], acc[c + 1], s1);
-      s2 = __fmaf_rn(sInv[(c + 2) * kNB + tid], acc[c + 2], s2);
-      s3 = __fmaf_rn(sInv[(c + 3) * kNB + tid], acc[c + 3], s3);
+      for (int c = 0; c < kNB; c += 4) {
+        s0 = __fmaf_rn(sInv[c * kNB + tid], acc[c], s0);
+        s1 = __fmaf_rn(sInv[(c + 1) * kNB + tid], acc[c + 1], s1);
+        s2 = __fmaf_rn(sInv[(c + 2) * kNB + tid], acc[c + 2], s2);
+        s3 = __fmaf_rn(sInv[(c + 3) * kNB + tid], acc[c + 3], s3);
+      }
+      if (tid < nb) out[k0 + tid] = (s0 + s1) + (s2 + s3);
     }
-    if (tid < nb) out[k0 + tid] = (s0 + s1) + (s2 + s3);
-  }
-  __syncthreads();
-  if (tid == 0) {
-    __threadfence();
-    atomicExch(&flags[k], epoch);
+    __syncthreads();
+    if (tid == 0) {
+      __threadfence();
+      atomicExch(&flags[k], epoch);
+    }
+    if (bad) break;  // a wait gave up: the status word has it; stop this CTA
   }
 }
 
@@ -1102,24 +1114,31 @@ static int tri_sweep(wbem_context* h, LuState& L, int mode, const float* in, flo
   unsigned* flags = L.flags + (size_t)mode * nblk;
   unsigned epoch = ++L.epoch;
   const size_t smem = (size_t)(kNB * kNB + 4 * kNB) * sizeof(float);
-  static bool attr = false;
-  if (!attr) {
-    WB_CU(cudaFuncSetAttribute(k_trsv_wave, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
-  int dev = 0, sms = 0, per_sm = 0;
+  // per device: attribute and co-resident grid size on the first sweep there
+  static std::atomic<int> grid_of[kMaxDev];
+  int dev = 0;
   WB_CU(cudaGetDevice(&dev));
-  WB_CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  WB_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trsv_wave, kTriThreads, smem));
-  if ((long long)per_sm * sms < nblk)
-    return fail(h, WBEM_ERR_ARG, "triangular sweep: too many blocks to be co-resident");
+  if (dev >= kMaxDev) return fail(h, WBEM_ERR_CUDA, "triangular sweep: device index beyond 64");
+  int cap = grid_of[dev].load(std::memory_order_acquire);
+  if (cap == 0) {
+    int sms = 0, per_sm = 0;
+    WB_CU(cudaFuncSetAttribute(k_trsv_wave, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    WB_CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    WB_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trsv_wave, kTriThreads, smem));
+    cap = per_sm * sms;
+    if (cap < 1) return fail(h, WBEM_ERR_CUDA, "triangular sweep: kernel does not fit on an SM");
+    grid_of[dev].store(cap, std::memory_order_release);
+  }
+  // more block rows than co-resident CTAs: each CTA takes block rows
+  // blockIdx.x, blockIdx.x + grid, ... in sweep order (no size limit)
+  const int grid = std::min(nblk, cap);
   const float* LU = h->d_lu;
   DevErr* err = h->d_err;
   const int ld = L.ld;
   void* args[] = {(void*)&N, (void*)&ld, (void*)&nblk, (void*)&mode, (void*)&LU, (void*)&dinv,
                   (void*)&in, (void*)&out, (void*)&flags, (void*)&epoch, (void*)&err};
   if (h->profiling) h->prof_trsv.begin(h->stream);
-  WB_CU(cudaLaunchCooperativeKernel((const void*)k_trsv_wave, dim3(nblk), dim3(kTriThreads), args,
+  WB_CU(cudaLaunchCooperativeKernel((const void*)k_trsv_wave, dim3(grid), dim3(kTriThreads), args,
                                     smem, h->stream));
   if (h->profiling) h->prof_trsv.end(h->stream, 2.0 * (double)N * N);
   return WBEM_OK;

@@ -9,7 +9,9 @@
 // takes device pointers only and keeps its partial sums in a fixed array in
 // the library's own device memory, so it never calls the allocator.
 #include <cuda_runtime.h>
+#include <atomic>
 #include <cmath>
+#include <mutex>
 #include <string>
 #include "context.h"
 
@@ -27,33 +29,6 @@ struct GaussLine {
   double w[8];
 };
 
-// Host-side Gauss-Legendre rule on [0,1] (Newton iteration on the Legendre
-// recurrence), the same rule as the regular panel quadrature.
-GaussLine gauss_line(int n) {
-  GaussLine g{};
-  g.n = n;
-  const long double pi = 3.141592653589793238462643383279502884L;
-  for (int i = 0; i < n; ++i) {
-    long double z = cosl(pi * (i + 0.75L) / (n + 0.5L)), dp = 1;
-    for (int it = 0; it < 100; ++it) {
-      long double pn = z, pm = 1;
-      for (int k = 2; k <= n; ++k) {
-        const long double pk = ((2 * k - 1) * z * pn - (k - 1) * pm) / k;
-        pm = pn;
-        pn = pk;
-      }
-      if (n == 1) pm = 1;
-      dp = n * (z * pn - pm) / (z * z - 1);
-      const long double dz = pn / dp;
-      z -= dz;
-      if (fabsl(dz) < 1e-20L) break;
-    }
-    g.x[i] = (double)((1 - z) / 2);
-    g.w[i] = (double)(1 / ((1 - z * z) * dp * dp));
-  }
-  return g;
-}
-
 }  // namespace
 
 // Partial sums of the last call (shared by every call on a device).
@@ -62,9 +37,45 @@ static __device__ __align__(256) double g_hull_partials[kNoAllocMaxPanels];
 // Host-side copies of the device address of g_hull_partials, one per device.
 // The name g_hull_partials in host code is only a stand-in for the device
 // symbol, so the address is looked up once per device with that device
-// current and passed to the kernels.
-static double* s_partials[kMaxDevices];
-static bool s_ready[kMaxDevices];
+// current and passed to the kernels. The lookup is serialised by a mutex;
+// later calls read the cached address without locking. A device reset
+// (cudaDeviceReset) invalidates the cached addresses: reload the library
+// after one.
+static std::atomic<double*> s_partials[kMaxDevices];
+static std::mutex s_partials_lock;
+
+// Device address of g_hull_partials on the current device `dev`.
+static cudaError_t partials_address(int dev, double** out) {
+  double* p = s_partials[dev].load(std::memory_order_acquire);
+  if (!p) {
+    std::lock_guard<std::mutex> g(s_partials_lock);
+    p = s_partials[dev].load(std::memory_order_relaxed);
+    if (!p) {
+      void* q = nullptr;
+      const cudaError_t e = cudaGetSymbolAddress(&q, g_hull_partials);
+      if (e != cudaSuccess) return e;
+      if (!q) return cudaErrorInvalidSymbol;
+      p = static_cast<double*>(q);
+      s_partials[dev].store(p, std::memory_order_release);
+    }
+  }
+  *out = p;
+  return cudaSuccess;
+}
+
+// Makes `dev` current for the lifetime of the guard and gives the caller's
+// current device back on every return path.
+struct DeviceScope {
+  int prev = -1;
+  bool ok = false;
+  explicit DeviceScope(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) return;
+    ok = prev == dev || cudaSetDevice(dev) == cudaSuccess;
+  }
+  ~DeviceScope() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
 
 // One thread per hull panel: F_panel = sum_q p n_dir JxW with
 // p = -(U . grad phi + |grad phi|^2 / 2), grad phi = tangential gradient of
@@ -159,26 +170,38 @@ extern "C" int wbem_hull_force_noalloc(wbem_handle h, const int* hull_cells, int
     h->err = "wbem_hull_force_noalloc: set the geometry first";
     return WBEM_ERR_STATE;
   }
-  if (h->device < 0 || h->device >= kMaxDevices || cudaSetDevice(h->device) != cudaSuccess) {
+  if (h->device < 0 || h->device >= kMaxDevices) {
+    h->err = "wbem_hull_force_noalloc: device index beyond the library's table of 64";
+    return WBEM_ERR_CUDA;
+  }
+  if (h->gauss_n < 1 || h->gauss_n > 8) {
+    h->err = "wbem_hull_force_noalloc: no quadrature rule (set the geometry first)";
+    return WBEM_ERR_STATE;
+  }
+  // the handle's device is current from here on; the caller's is restored
+  DeviceScope scope(h->device);
+  if (!scope.ok) {
     h->err = "wbem_hull_force_noalloc: cannot select the handle's device";
     return WBEM_ERR_CUDA;
   }
-  // one-time set-up per device (the handle's device is current here)
-  if (!s_ready[h->device]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_hull_partials);
-    if (e != cudaSuccess || !p) {
+  // one-time set-up per device (the first call on a device)
+  double* partials = nullptr;
+  {
+    const cudaError_t e = partials_address(h->device, &partials);
+    if (e != cudaSuccess) {
       h->err = std::string("wbem_hull_force_noalloc: cudaGetSymbolAddress failed: ") +
                cudaGetErrorString(e);
       return WBEM_ERR_CUDA;
     }
-    s_partials[h->device] = static_cast<double*>(p);
-    s_ready[h->device] = true;
   }
-  double* partials = s_partials[h->device];
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : h->stream;
-  const int q1 = h->opt.quadrature_order;
-  const GaussLine g = gauss_line(q1 >= 1 && q1 <= 8 ? q1 : 4);
+  // the same line rule as the panels' tensor rule of the allocating path
+  GaussLine g{};
+  g.n = h->gauss_n;
+  for (int a = 0; a < g.n; ++a) {
+    g.x[a] = h->gauss_x[a];
+    g.w[a] = h->gauss_w[a];
+  }
   if (n_hull > 0)
     k_hull_partials_noalloc<<<(n_hull + 127) / 128, 128, 0, s>>>(
         n_hull, h->C, hull_cells, h->d_cell_dofs, h->d_perm, h->d_X, U[0], U[1], U[2], dir, phi,

@@ -104,6 +104,11 @@ static int build_quadrature(wbem_context* h, int q1, int sorder) {
   t.q1 = q1;
   std::vector<double> x, w;
   gauss_legendre01(q1, x, w);
+  h->gauss_n = q1;
+  for (int a = 0; a < q1; ++a) {
+    h->gauss_x[a] = x[a];
+    h->gauss_w[a] = w[a];
+  }
   for (int b = 0; b < q1; ++b)
     for (int a = 0; a < q1; ++a) {
       const int q = a + q1 * b;
