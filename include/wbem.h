@@ -142,6 +142,17 @@ int wbem_compute_rhs(wbem_handle h, const double* src, double* dst);
  * constraint inhomogeneities from the known data, as a solve does. */
 int wbem_residual(wbem_handle h, const double* phi, const double* dphi_dn, double* res);
 
+/* ComputationalDomain::compute_normals (source/computational_domain.cc:1525-1620):
+ * the L2 projection onto Q1 of the panel normals (consistent mass matrix),
+ * normalised per node. normals: N x 3, caller order. Needs only the geometry. */
+int wbem_node_normals(wbem_handle h, double* normals);
+/* BEMProblem::compute_surface_gradients (source/bem_problem.cc:1153-1293): the
+ * L2 projection onto Q1 of the surface gradient of tmp_rhs * surface_nodes
+ * (the Dirichlet data, zero elsewhere). tmp_rhs: N; gradients: N x 3, caller
+ * order. These two projections give the inhomogeneities of the sharp
+ * Dirichlet-Dirichlet constraint lines. */
+int wbem_surface_gradients(wbem_handle h, const double* tmp_rhs, double* gradients);
+
 /* Hull force F = sum over cells hull_cells[k] of  int p n_dir dS,
  * p = -(U . grad phi + |grad phi|^2 / 2) (steady, rho = 1, g = 0 form of
  * source/free_surface.cc:6936-6942); dir = 0,1,2 selects the force component. */
@@ -151,7 +162,10 @@ int wbem_hull_force(wbem_handle h, const int* hull_cells, int n_hull, const doub
 /* Adjoint of assemble + solve_system + hull force, at the current solution of
  * the last wbem_solve / wbem_solve_system with tmp_rhs: returns dF/dX (N x 3,
  * with tmp_rhs held fixed) and dF/dtmp_rhs (N). Reuses the factors for the
- * transposed solve and recomputes matrix tiles (no dG/dX storage). */
+ * transposed solve and recomputes matrix tiles (no dG/dX storage). The
+ * constraint rows are differentiated too: a Dirichlet-Neumann line through
+ * its datum, a sharp Dirichlet-Dirichlet line through the projected normals
+ * and surface gradients (node positions and Dirichlet data). */
 int wbem_force_adjoint(wbem_handle h, const int* hull_cells, int n_hull, const double* U, int dir,
                        const double* tmp_rhs, double* dF_dX, double* dF_drhs);
 

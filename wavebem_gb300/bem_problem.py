@@ -31,8 +31,9 @@ SOLVER_AUTO, SOLVER_GMRES, SOLVER_LU, SOLVER_GMRES_IR = 0, 1, 2, 3
 EXPORTS = ["wbem_default_options", "wbem_create", "wbem_destroy", "wbem_last_error",
            "wbem_set_geometry", "wbem_update_nodes", "wbem_set_bc", "wbem_assemble",
            "wbem_solve_system", "wbem_solve", "wbem_get_alpha", "wbem_get_matrices",
-           "wbem_vmult", "wbem_compute_rhs", "wbem_residual", "wbem_hull_force", "wbem_force_adjoint",
-           "wbem_adjoint", "wbem_get_stats"]
+           "wbem_vmult", "wbem_compute_rhs", "wbem_residual", "wbem_node_normals",
+           "wbem_surface_gradients", "wbem_hull_force", "wbem_force_adjoint", "wbem_adjoint",
+           "wbem_get_stats"]
 
 
 class WBEMError(RuntimeError):
@@ -94,6 +95,8 @@ def load_library(path: str = LIB_PATH):
     L.wbem_vmult.argtypes = [H, dp, dp]
     L.wbem_compute_rhs.argtypes = [H, dp, dp]
     L.wbem_residual.argtypes = [H, dp, dp, dp]
+    L.wbem_node_normals.argtypes = [H, dp]
+    L.wbem_surface_gradients.argtypes = [H, dp, dp]
     L.wbem_hull_force.argtypes = [H, ip, C.c_int, dp, C.c_int, dp, dp, C.POINTER(C.c_double)]
     L.wbem_force_adjoint.argtypes = [H, ip, C.c_int, dp, C.c_int, dp, dp, dp]
     L.wbem_adjoint.argtypes = [H, dp, dp, dp, dp]
@@ -220,6 +223,19 @@ class BEMProblem:
         self._check(self.L.wbem_residual(self.h, _f64(phi), _f64(dphi_dn), out))
         res[:] = out
         return res
+
+    def compute_normals(self):
+        """ComputationalDomain::compute_normals: L2-projected node normals (N, 3)."""
+        n = np.zeros(3 * self.n_dofs)
+        self._check(self.L.wbem_node_normals(self.h, n))
+        return n.reshape(-1, 3)
+
+    def compute_surface_gradients(self, tmp_rhs):
+        """BEMProblem::compute_surface_gradients: L2-projected surface gradients
+        (N, 3) of tmp_rhs on the Dirichlet nodes (zero elsewhere)."""
+        g = np.zeros(3 * self.n_dofs)
+        self._check(self.L.wbem_surface_gradients(self.h, _f64(tmp_rhs), g))
+        return g.reshape(-1, 3)
 
     def matrices(self, neumann=True, dirichlet=True):
         N = self.n_dofs

@@ -738,6 +738,9 @@ static cudaError_t launch_adj_mixed_t(int N, int C, const double* X, const int* 
 // direct partial derivatives come either from the hull force (hull_cells
 // given: dF/dphi, dF/ddn and dF/dX|direct of the hull panels) or from the
 // caller (dJ_dphi, dJ_ddn per node in caller order, no direct X term).
+void constraints_adjoint(wbem_context* h, const double* tmp_rhs, const double* lam, double* dJ_dX,
+                         double* dJ_db);
+
 static int adjoint_run(wbem_context* h, const int* hull_cells, int n_hull, const double* U, int dir,
                        const double* dJ_dphi, const double* dJ_ddn, double* dF_dX,
                        double* dF_drhs) {
@@ -891,22 +894,12 @@ static int adjoint_run(wbem_context* h, const int* hull_cells, int n_hull, const
       for (int d = 0; d < 3; ++d) dF_dX[3 * (size_t)p + d] = gXi[3 * (size_t)i + d];
       dF_drhs[p] = gbi[i];
     }
-    // Dirichlet-Neumann lines x_m = b_first: -lambda_m * d(-b_first)/db = +lambda_m
-    const auto& P = h->dn_ptr;
-    const auto& I = h->dn_idx;
-    for (int i = 0; i < N; ++i) {
-      int first = I[P[i]];
-      for (int k = P[i]; k < P[i + 1]; ++k)
-        if (h->mask[I[k]]) {
-          first = I[k];
-          break;
-        }
-      if (i != first || !h->mask[i]) continue;
-      for (int k = P[i]; k < P[i + 1]; ++k) {
-        const int o = I[k];
-        if (o != i && !h->mask[o]) dF_drhs[i] += li[h->iperm[o]];
-      }
-    }
+    // constraint inhomogeneities: a Dirichlet-Neumann line carries the datum
+    // of its Dirichlet copy; a sharp Dirichlet-Dirichlet line carries a value
+    // of the projected normals and surface gradients, i.e. of X and b
+    std::vector<double> lc(N);
+    for (int i = 0; i < N; ++i) lc[h->perm[i]] = li[i];
+    constraints_adjoint(h, h->sol_b.data(), lc.data(), dF_dX, dF_drhs);
     h->stats.t_adjoint_ms = tm.ms();
   } while (0);
   return st;

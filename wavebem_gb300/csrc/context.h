@@ -174,6 +174,7 @@ struct wbem_context {
   double* d_rhs = nullptr;
   double* d_b = nullptr;   // known data (internal order)
   bool have_solution = false;
+  std::vector<double> sol_b;  // known data (tmp_rhs) of the last solve, caller order
 
   wbem::DevErr* d_err = nullptr;
   int launches = 0;

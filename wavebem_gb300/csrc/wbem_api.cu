@@ -409,298 +409,12 @@ static int build_topology(wbem_context* h) {
 }
 
 // ------------------------------------------------------------ constraints
-// BEMProblem<3>::compute_constraints (source/bem_problem.cc:990-1105) with
-// deal.II ConstraintMatrix semantics (add_line is idempotent, close() resolves
-// entries that point at constrained dofs). Caller order in, internal order
-// uploaded. Normals and surface gradients (L2 projections) are only needed
-// for Dirichlet-Dirichlet double nodes.
-namespace {
-struct Lines {
-  std::map<int, std::vector<std::pair<int, double>>> l;
-  std::map<int, double> inh;
-  void add_line(int i) {
-    if (!l.count(i)) {
-      l[i] = {};
-      inh[i] = 0;
-    }
-  }
-  void add_entry(int i, int j, double v) {
-    for (auto& e : l[i])
-      if (e.first == j) return;
-    l[i].push_back({j, v});
-  }
-  void close() {
-    for (int pass = 0; pass < 64; ++pass) {
-      bool changed = false;
-      for (auto& kv : l) {
-        std::vector<std::pair<int, double>> out;
-        double v = inh[kv.first];
-        for (auto& e : kv.second) {
-          auto it = l.find(e.first);
-          if (it != l.end() && e.first != kv.first) {
-            changed = true;
-            v += e.second * inh[e.first];
-            for (auto& e2 : it->second) out.push_back({e2.first, e.second * e2.second});
-          } else {
-            out.push_back(e);
-          }
-        }
-        std::map<int, double> m;
-        for (auto& e : out) m[e.first] += e.second;
-        kv.second.assign(m.begin(), m.end());
-        inh[kv.first] = v;
-      }
-      if (!changed) break;
-    }
-  }
-};
-
-// L2 projection onto Q1 with the consistent mass matrix (CG to round-off).
-void l2_project(int N, const double* X, int C, const int* cells, int q1,
-                const std::vector<std::vector<double>>& cellval /*C x q x 3*/,
-                std::vector<double>& out /*N x 3*/) {
-  std::vector<double> x, w;
-  gauss_legendre01(q1, x, w);
-  std::vector<std::map<int, double>> M(N);
-  std::vector<double> rhs(3 * (size_t)N, 0.0);
-  for (int c = 0; c < C; ++c) {
-    const int* cc = cells + 4 * c;
-    for (int b = 0; b < q1; ++b)
-      for (int a = 0; a < q1; ++a) {
-        const int q = a + q1 * b;
-        double s = x[a], u = x[b];
-        double ph[4] = {(1 - s) * (1 - u), s * (1 - u), (1 - s) * u, s * u};
-        double jx[3], je[3];
-        for (int d = 0; d < 3; ++d) {
-          jx[d] = (1 - u) * (X[3 * cc[1] + d] - X[3 * cc[0] + d]) + u * (X[3 * cc[3] + d] - X[3 * cc[2] + d]);
-          je[d] = (1 - s) * (X[3 * cc[2] + d] - X[3 * cc[0] + d]) + s * (X[3 * cc[3] + d] - X[3 * cc[1] + d]);
-        }
-        double cr[3] = {jx[1] * je[2] - jx[2] * je[1], jx[2] * je[0] - jx[0] * je[2],
-                        jx[0] * je[1] - jx[1] * je[0]};
-        double jxw = std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]) * w[a] * w[b];
-        for (int i = 0; i < 4; ++i) {
-          for (int j = 0; j < 4; ++j) M[cc[i]][cc[j]] += ph[i] * ph[j] * jxw;
-          for (int d = 0; d < 3; ++d) rhs[(size_t)d * N + cc[i]] += ph[i] * cellval[c][3 * q + d] * jxw;
-        }
-      }
-  }
-  out.assign(3 * (size_t)N, 0.0);
-  for (int d = 0; d < 3; ++d) {
-    std::vector<double> xs(N, 0.0), r(rhs.begin() + (size_t)d * N, rhs.begin() + (size_t)(d + 1) * N), z(N), p(N), Ap(N), dinv(N);
-    double bn = 0;
-    for (int i = 0; i < N; ++i) {
-      dinv[i] = 1.0 / M[i][i];
-      bn += r[i] * r[i];
-    }
-    bn = std::sqrt(bn);
-    if (bn > 0) {
-      for (int i = 0; i < N; ++i) z[i] = dinv[i] * r[i];
-      p = z;
-      double rz = 0;
-      for (int i = 0; i < N; ++i) rz += r[i] * z[i];
-      for (int it = 0; it < 10 * N + 100; ++it) {
-        for (int i = 0; i < N; ++i) {
-          double s = 0;
-          for (auto& kv : M[i]) s += kv.second * p[kv.first];
-          Ap[i] = s;
-        }
-        double pAp = 0;
-        for (int i = 0; i < N; ++i) pAp += p[i] * Ap[i];
-        double al = rz / pAp, rn = 0;
-        for (int i = 0; i < N; ++i) {
-          xs[i] += al * p[i];
-          r[i] -= al * Ap[i];
-          rn += r[i] * r[i];
-        }
-        if (std::sqrt(rn) < 1e-15 * bn) break;
-        double rz2 = 0;
-        for (int i = 0; i < N; ++i) {
-          z[i] = dinv[i] * r[i];
-          rz2 += r[i] * z[i];
-        }
-        for (int i = 0; i < N; ++i) p[i] = z[i] + rz2 / rz * p[i];
-        rz = rz2;
-      }
-    }
-    for (int i = 0; i < N; ++i) out[3 * (size_t)i + d] = xs[i];
-  }
-}
-}  // namespace
-
-static int build_constraints(wbem_context* h, const double* tmp_rhs) {
-  const int N = h->N;
-  const auto& m = h->mask;
-  const auto& P = h->dn_ptr;
-  const auto& I = h->dn_idx;
-  bool need_geo = false;
-  for (int i = 0; i < N && !need_geo; ++i)
-    if (m[i])
-      for (int k = P[i]; k < P[i + 1]; ++k)
-        if (I[k] != i && m[I[k]]) need_geo = true;
-  std::vector<double> nn, gg;
-  if (need_geo) {
-    const int q1 = h->opt.quadrature_order;
-    std::vector<double> x, w;
-    gauss_legendre01(q1, x, w);
-    std::vector<std::vector<double>> cn(h->C), cg(h->C);
-    for (int c = 0; c < h->C; ++c) {
-      const int* cc = &h->cells[4 * c];
-      cn[c].resize(3 * q1 * q1);
-      cg[c].resize(3 * q1 * q1);
-      double f[4];
-      for (int k = 0; k < 4; ++k) f[k] = m[cc[k]] ? tmp_rhs[cc[k]] : 0.0;
-      for (int b = 0; b < q1; ++b)
-        for (int a = 0; a < q1; ++a) {
-          const int q = a + q1 * b;
-          double s = x[a], u = x[b];
-          double jx[3], je[3];
-          const double* X = h->X.data();
-          for (int d = 0; d < 3; ++d) {
-            jx[d] = (1 - u) * (X[3 * cc[1] + d] - X[3 * cc[0] + d]) + u * (X[3 * cc[3] + d] - X[3 * cc[2] + d]);
-            je[d] = (1 - s) * (X[3 * cc[2] + d] - X[3 * cc[0] + d]) + s * (X[3 * cc[3] + d] - X[3 * cc[1] + d]);
-          }
-          double cr[3] = {jx[1] * je[2] - jx[2] * je[1], jx[2] * je[0] - jx[0] * je[2],
-                          jx[0] * je[1] - jx[1] * je[0]};
-          double l = std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
-          double gx = -(1 - u) * f[0] + (1 - u) * f[1] - u * f[2] + u * f[3];
-          double ge = -(1 - s) * f[0] - s * f[1] + (1 - s) * f[2] + s * f[3];
-          double g11 = 0, g12 = 0, g22 = 0;
-          for (int d = 0; d < 3; ++d) {
-            g11 += jx[d] * jx[d];
-            g12 += jx[d] * je[d];
-            g22 += je[d] * je[d];
-          }
-          double det = g11 * g22 - g12 * g12;
-          double c1 = (g22 * gx - g12 * ge) / det, c2 = (-g12 * gx + g11 * ge) / det;
-          for (int d = 0; d < 3; ++d) {
-            cn[c][3 * q + d] = cr[d] / l;
-            cg[c][3 * q + d] = c1 * jx[d] + c2 * je[d];
-          }
-        }
-    }
-    l2_project(N, h->X.data(), h->C, h->cells.data(), q1, cn, nn);
-    l2_project(N, h->X.data(), h->C, h->cells.data(), q1, cg, gg);
-    for (int i = 0; i < N; ++i) {
-      double l = std::sqrt(nn[3 * i] * nn[3 * i] + nn[3 * i + 1] * nn[3 * i + 1] + nn[3 * i + 2] * nn[3 * i + 2]);
-      for (int d = 0; d < 3; ++d) nn[3 * i + d] /= l;
-    }
-  }
-  auto dot3 = [](const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
-  Lines c;
-  for (int i = 0; i < N; ++i) {
-    int first = I[P[i]];
-    for (int k = P[i]; k < P[i + 1]; ++k)
-      if (m[I[k]] == 1) {
-        first = I[k];
-        break;
-      }
-    if (i != first) continue;
-    for (int k = P[i]; k < P[i + 1]; ++k) {
-      const int o = I[k];
-      if (o == i) continue;
-      if (m[i] == 1) {
-        if (m[o] == 1) {
-          const double* ni = &nn[3 * i];
-          const double* no = &nn[3 * o];
-          double dd = std::sqrt((ni[0] - no[0]) * (ni[0] - no[0]) + (ni[1] - no[1]) * (ni[1] - no[1]) +
-                                (ni[2] - no[2]) * (ni[2] - no[2]));
-          if (dd < 1e-4) {
-            c.add_line(o);
-            c.add_entry(o, i, 1.0);
-          } else {
-            c.add_line(o);
-            const double* gi = &gg[3 * i];
-            const double* go = &gg[3 * o];
-            double cij = dot3(ni, no);
-            double this_g = (1.0 / (1.0 - cij * cij)) * (dot3(go, ni) + dot3(gi, no) * cij);
-            double other_g = (1.0 / (1.0 - cij * cij)) * (dot3(gi, no) + dot3(go, ni) * cij);
-            c.add_line(i);
-            c.inh[i] = this_g;
-            c.add_line(o);
-            c.inh[o] = other_g;
-          }
-        } else {
-          c.add_line(o);
-          c.inh[o] = tmp_rhs[i];
-        }
-      } else {
-        c.add_line(o);
-        c.add_entry(o, i, 1.0);
-      }
-    }
-  }
-  c.close();
-  // internal order, rows sorted
-  const auto& ip = h->iperm;
-  std::vector<std::pair<int, int>> rows;  // (internal row, caller row)
-  for (auto& kv : c.l) rows.push_back({ip[kv.first], kv.first});
-  std::sort(rows.begin(), rows.end());
-  std::vector<int> crow, cptr{0}, ccol;
-  std::vector<double> cval, cinh;
-  for (auto& r : rows) {
-    crow.push_back(r.first);
-    cinh.push_back(c.inh[r.second]);
-    for (auto& e : c.l[r.second]) {
-      ccol.push_back(ip[e.first]);
-      cval.push_back(e.second);
-    }
-    cptr.push_back((int)ccol.size());
-  }
-  h->n_crows = (int)crow.size();
-  if (h->d_cinh && h->d_cflag && crow == h->c_crow && cptr == h->c_cptr && ccol == h->c_ccol &&
-      cval == h->c_cval) {
-    // same lines and entries as the last upload (the usual case from one
-    // solve_system to the next): only the inhomogeneities change
-    if (!cinh.empty())
-      CU(copy_sync(h, h->d_cinh, cinh.data(), sizeof(double) * cinh.size(), cudaMemcpyHostToDevice));
-    return WBEM_OK;
-  }
-  std::vector<uint8_t> cflag(N, 0);
-  std::vector<int> cptr_full(N + 1, 0), ccol_full;
-  std::vector<double> cval_full;
-  std::vector<std::vector<std::pair<int, double>>> byrow(N);
-  for (size_t k = 0; k < crow.size(); ++k) {
-    cflag[crow[k]] = 1;
-    for (int e = cptr[k]; e < cptr[k + 1]; ++e) byrow[crow[k]].push_back({ccol[e], cval[e]});
-  }
-  for (int i = 0; i < N; ++i) {
-    for (auto& e : byrow[i]) {
-      ccol_full.push_back(e.first);
-      cval_full.push_back(e.second);
-    }
-    cptr_full[i + 1] = (int)ccol_full.size();
-  }
-  // transposed entries: for column j, the constrained rows i with entry c_ij
-  std::vector<int> tptr(N + 1, 0), tsrc;
-  std::vector<double> tval;
-  std::vector<std::vector<std::pair<int, double>>> bycol(N);
-  for (int i = 0; i < N; ++i)
-    for (auto& e : byrow[i]) bycol[e.first].push_back({i, e.second});
-  for (int j = 0; j < N; ++j) {
-    for (auto& e : bycol[j]) {
-      tsrc.push_back(e.first);
-      tval.push_back(e.second);
-    }
-    tptr[j + 1] = (int)tsrc.size();
-  }
-  CHK(upload(h, &h->d_crow, crow));
-  CHK(upload(h, &h->d_cptr, cptr));
-  CHK(upload(h, &h->d_ccol, ccol));
-  CHK(upload(h, &h->d_cval, cval));
-  CHK(upload(h, &h->d_cinh, cinh));
-  CHK(upload(h, &h->d_cflag, cflag));
-  CHK(upload(h, &h->d_cptr_full, cptr_full));
-  CHK(upload(h, &h->d_ccol_full, ccol_full));
-  CHK(upload(h, &h->d_cval_full, cval_full));
-  CHK(upload(h, &h->d_tptr, tptr));
-  CHK(upload(h, &h->d_tsrc, tsrc));
-  CHK(upload(h, &h->d_tval, tval));
-  h->c_crow.swap(crow);
-  h->c_cptr.swap(cptr);
-  h->c_ccol.swap(ccol);
-  h->c_cval.swap(cval);
-  return WBEM_OK;
-}
+// (constraints.cu: compute_constraints, the L2 projections, their adjoint)
+namespace wbem {
+int build_constraints(wbem_context* h, const double* tmp_rhs);
+void node_normals(wbem_context* h, std::vector<double>& n);
+void surface_gradients(wbem_context* h, const double* tmp_rhs, std::vector<double>& g);
+}  // namespace wbem
 
 // ------------------------------------------------------------- workspaces
 namespace wbem {
@@ -1436,6 +1150,7 @@ int wbem_solve_system(wbem_handle h, const double* tmp_rhs, double* phi, double*
     if (h->mask[p] == 0) phi[p] = si[i];
     else dphi_dn[p] = si[i];
   }
+  h->sol_b.assign(tmp_rhs, tmp_rhs + N);
   h->have_solution = true;
   h->stats.kernel_launches = h->launches;
   return WBEM_OK;
@@ -1562,7 +1277,37 @@ int wbem_residual(wbem_handle h, const double* phi, const double* dphi_dn, doubl
     for (int i = 0; i < N; ++i) res[i] -= sn;
   }
   for (int i = 0; i < N; ++i) res[h->perm[i]] -= ri[i];
-  return check_device_error(h, "wbem_residual");
+  CHK(check_device_error(h, "wbem_residual"));
+  if (h->have_solution) {
+    // the adjoint reads the known data of the last solve from d_b
+    std::vector<double> bi(N);
+    for (int i = 0; i < N; ++i) bi[i] = h->sol_b[h->perm[i]];
+    CU(copy_sync(h, h->d_b, bi.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+  }
+  return WBEM_OK;
+}
+
+int wbem_node_normals(wbem_handle h, double* normals) {
+  if (!h) return WBEM_ERR_ARG;
+  if (!normals) return fail(h, WBEM_ERR_ARG, "wbem_node_normals: NULL pointer");
+  if (h->N == 0) return fail(h, WBEM_ERR_STATE, "wbem_node_normals: set the geometry first");
+  std::vector<double> n;
+  node_normals(h, n);
+  std::copy(n.begin(), n.end(), normals);
+  return WBEM_OK;
+}
+
+int wbem_surface_gradients(wbem_handle h, const double* tmp_rhs, double* gradients) {
+  if (!h) return WBEM_ERR_ARG;
+  if (!tmp_rhs || !gradients) return fail(h, WBEM_ERR_ARG, "wbem_surface_gradients: NULL pointer");
+  if (h->N == 0) return fail(h, WBEM_ERR_STATE, "wbem_surface_gradients: set the geometry first");
+  if (!h->have_mask) return fail(h, WBEM_ERR_STATE, "wbem_surface_gradients: set the boundary conditions first");
+  for (int i = 0; i < h->N; ++i)
+    if (!std::isfinite(tmp_rhs[i])) return fail(h, WBEM_ERR_NONFINITE, "wbem_surface_gradients: non-finite tmp_rhs");
+  std::vector<double> g;
+  surface_gradients(h, tmp_rhs, g);
+  std::copy(g.begin(), g.end(), gradients);
+  return WBEM_OK;
 }
 
 int wbem_hull_force(wbem_handle h, const int* hull_cells, int n_hull, const double* U, int dir,
