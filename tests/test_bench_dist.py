@@ -3,7 +3,8 @@
 bench.py runs N independent replicas (one process per GPU, no data-path
 collective); what the ranks share is the barrier around the timed region, the
 maximum of the per-rank times and the rule that rank 0 alone runs the CPU
-reference arm. Those host-side pieces are exercised here with world size 2."""
+reference arm (here on a small tank) while the other ranks return at once.
+Those host-side pieces are exercised here with world size 2."""
 import os
 import socket
 import sys
@@ -23,6 +24,10 @@ def _free_port():
 
 class _Args:
     impl = "reference"
+    n = 300      # a small tank, so that the oracle runs in about a second
+    steps = 2
+    warmup = 1
+    gpus = 2
 
 
 def _rank(rank, world, port, q):
@@ -35,9 +40,11 @@ def _rank(rank, world, port, q):
     bench.barrier(w)
     t_max = bench.allmax(w, 0.5 * (r + 1))
     # only rank 0 runs (and prints) the reference arm; the others return at once
-    skipped = bench.run_reference(_Args, r, w) is None if r != 0 else True
+    line = bench.run_reference(_Args, r, w)
     bench.barrier(w)
-    q.put((r, w, dist.get_backend(), t_max, skipped))
+    ran = None if line is None else (line["impl"], line["steps"], line["value"] > 0,
+                                     line["measured"]["gmres_iterations"] > 0)
+    q.put((r, w, dist.get_backend(), t_max, ran))
     dist.destroy_process_group()
 
 
@@ -53,4 +60,4 @@ def test_two_ranks_share_barrier_and_max_time():
         p.join(180)
     assert all(p.exitcode == 0 for p in procs), [p.exitcode for p in procs]
     got = sorted(q.get(timeout=10) for _ in procs)
-    assert got == [(0, 2, "gloo", 1.0, True), (1, 2, "gloo", 1.0, True)]
+    assert got == [(0, 2, "gloo", 1.0, ("reference", 2, True, True)), (1, 2, "gloo", 1.0, None)]
