@@ -99,3 +99,27 @@ def test_sphere_exact_normal_derivative():
     g.solve(phi, dphi, p)
     # discretisation error of the Q1 collocation BEM on a coarse sphere
     assert rel2(dphi, dpdn) < 0.01
+
+
+@pytest.mark.parametrize("prec,tol", [(0, 1e-12), (1, 2e-8)])
+def test_vmult_all_neumann_norm_shift(prec, tol):
+    """vmult with no Dirichlet node subtracts ||dst||_2 from every entry
+    (source/bem_problem.cc:667-668), like the oracle's; a solve of that
+    singular system is refused with an argument error."""
+    import oracle as O
+    from wavebem_gb300.bem_problem import WBEMError
+    P, m, b = oracle_problem("wigley", 2000)
+    g = _gpu(m, P.dn_ptr, P.dn_idx, precision=prec)
+    g.assemble_system()
+    neu = np.zeros(P.N, np.uint8)
+    g.set_bc(neu)
+    P0 = O.Problem(m.X, m.cells, P.dn_ptr, P.dn_idx, neu)
+    P0.Nm, P0.Dm, P0.alpha = P.Nm, P.Dm, P.alpha
+    v = np.random.default_rng(7).normal(size=P.N)
+    ref = P0.vmult(v)
+    assert rel2(g.vmult(v), ref) <= tol
+    # without the shift the two would differ by ||dst|| in every entry
+    assert np.abs(ref - (P.Nm @ v + P.alpha * v)).max() > 1e-3 * np.abs(ref).max()
+    phi, dphi = b.copy(), b.copy()
+    with pytest.raises(WBEMError):
+        g.solve_system(phi, dphi, b)
