@@ -92,15 +92,20 @@ __device__ __forceinline__ bool in_set(const int set[kMaxSet], int v) {
 
 constexpr int kChunk = 6;  // panels per staged chunk
 
+// Two threads per row (2 * kRowsF64 threads): each takes every other
+// quadrature point of a panel; the partial sums are combined through a lane
+// shuffle, then one thread adds the N entries and the other the D entries.
+constexpr int kF64Threads = 2 * kRowsF64;
+
 template <int Q1>
-__global__ void __launch_bounds__(kRowsPerTile)
+__global__ void __launch_bounds__(kF64Threads)
     k_tile_fp64(int N, const double* __restrict__ X, const int* __restrict__ dnset,
                 const int* __restrict__ tile_ptr, const int2* __restrict__ tile_ent,
                 const int4* __restrict__ cell_dofs, const double* __restrict__ rec,
                 double* __restrict__ Nm, double* __restrict__ Dm, DevErr* err) {
   constexpr int NQ = Q1 * Q1;
   constexpr int RECD = NQ * 8;  // doubles per panel record
-  constexpr int RT = kRowsPerTile, CT = kColsPerTile, LDA = RT + 1;
+  constexpr int RT = kRowsF64, CT = kColsPerTileF64, LDA = RT + 1;
   extern __shared__ __align__(128) unsigned char smem[];
   double* stage = reinterpret_cast<double*>(smem);  // [2][kChunk][RECD], 128-byte aligned
   double* accN = stage + 2 * kChunk * RECD;         // [CT][LDA]
@@ -109,9 +114,10 @@ __global__ void __launch_bounds__(kRowsPerTile)
   uint64_t* bar = reinterpret_cast<uint64_t*>(meta + 2 * kChunk);
 
   const int tid = threadIdx.x;
+  const int rt = tid >> 1, half = tid & 1;  // row in the tile, point parity
   const int tile = blockIdx.x;
   const int row0 = blockIdx.y * RT;
-  const int row = row0 + tid;
+  const int row = row0 + rt;
   const bool active = row < N;
   double xi = 0, yi = 0, zi = 0;
   int set[kMaxSet];
@@ -124,7 +130,7 @@ __global__ void __launch_bounds__(kRowsPerTile)
 #pragma unroll
     for (int k = 0; k < kMaxSet; ++k) set[k] = dnset[(size_t)row * kMaxSet + k];
   }
-  for (int k = tid; k < CT * LDA; k += RT) {
+  for (int k = tid; k < CT * LDA; k += kF64Threads) {
     accN[k] = 0.0;
     accD[k] = 0.0;
   }
@@ -189,11 +195,14 @@ __global__ void __launch_bounds__(kRowsPerTile)
       const uint32_t slots = mt.slots;
       const int4 d = mt.dofs;
       const bool sing = in_set(set, d.x) || in_set(set, d.y) || in_set(set, d.z) || in_set(set, d.w);
-      if (!active || sing) continue;
+      // a skipped row (inactive, or the panel is singular for it) runs no
+      // points but still takes part in the shuffle below: every lane of the
+      // warp reaches it
+      const bool skip = !active || sing;
       const double* r = stage + (size_t)((c & 1) * kChunk + k) * RECD;
       double ln0 = 0, ln1 = 0, ln2 = 0, ln3 = 0, ld0 = 0, ld1 = 0, ld2 = 0, ld3 = 0;
 #pragma unroll 4
-      for (int q = 0; q < NQ; ++q) {
+      for (int q = skip ? NQ : half; q < NQ; q += 2) {
         const double2 p01 = *reinterpret_cast<const double2*>(r + q * 8);
         const double2 p23 = *reinterpret_cast<const double2*>(r + q * 8 + 2);
         const double2 p45 = *reinterpret_cast<const double2*>(r + q * 8 + 4);
@@ -213,14 +222,21 @@ __global__ void __launch_bounds__(kRowsPerTile)
         ld2 = fma(sq, c_q.phi[q][2], ld2);
         ld3 = fma(sq, c_q.phi[q][3], ld3);
       }
-      const double lnv[4] = {ln0, ln1, ln2, ln3}, ldv[4] = {ld0, ld1, ld2, ld3};
+      // the row's sums: even points + odd points (the same on both threads)
+      double lnv[4] = {ln0, ln1, ln2, ln3}, ldv[4] = {ld0, ld1, ld2, ld3};
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const double on = __shfl_xor_sync(0xffffffffu, lnv[j], 1);
+        const double od = __shfl_xor_sync(0xffffffffu, ldv[j], 1);
+        lnv[j] = half ? on + lnv[j] : lnv[j] + on;
+        ldv[j] = half ? od + ldv[j] : ldv[j] + od;
+      }
+      if (skip) continue;
+      double* acc = half ? accD : accN;
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const uint32_t sl = (slots >> (8 * j)) & 255u;
-        if (sl != 255u) {
-          accN[sl * LDA + tid] += lnv[j];
-          accD[sl * LDA + tid] += ldv[j];
-        }
+        if (sl != 255u) acc[sl * LDA + rt] += half ? ldv[j] : lnv[j];
       }
     }
     __syncthreads();
@@ -229,7 +245,7 @@ __global__ void __launch_bounds__(kRowsPerTile)
   // coalesced write-out of the tile (row-major N x N); the tile's columns:
   // tile_ptr[gridDim.x + 1 + tile] .. (+ 1)
   const int col0 = tile_ptr[gridDim.x + 1 + tile], ncol = tile_ptr[gridDim.x + 2 + tile] - col0;
-  for (int idx = tid; idx < RT * CT; idx += RT) {
+  for (int idx = tid; idx < RT * CT; idx += kF64Threads) {
     const int rr = idx / CT, cc = idx % CT;
     const int gr = row0 + rr, gc = col0 + cc;
     if (gr < N && cc < ncol) {
@@ -246,13 +262,13 @@ static cudaError_t launch_tile_fp64_t(int N, const double* X, const int* dnset, 
                                       double* Dm, DevErr* err, cudaStream_t s) {
   constexpr int RECD = Q1 * Q1 * 8;
   const size_t smem = (size_t)2 * kChunk * RECD * 8 +
-                      (size_t)2 * kColsPerTile * (kRowsPerTile + 1) * 8 +
+                      (size_t)2 * kColsPerTileF64 * (kRowsF64 + 1) * 8 +
                       2 * kChunk * sizeof(ChunkMeta) + 2 * sizeof(uint64_t);
   cudaError_t e = cudaFuncSetAttribute(k_tile_fp64<Q1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return e;
-  dim3 grid(n_tiles, (N + kRowsPerTile - 1) / kRowsPerTile);
-  k_tile_fp64<Q1><<<grid, kRowsPerTile, smem, s>>>(N, X, dnset, tile_ptr, tile_ent, cell_dofs, rec,
+  dim3 grid(n_tiles, (N + kRowsF64 - 1) / kRowsF64);
+  k_tile_fp64<Q1><<<grid, kF64Threads, smem, s>>>(N, X, dnset, tile_ptr, tile_ent, cell_dofs, rec,
                                                    Nm, Dm, err);
   return cudaGetLastError();
 }

@@ -77,8 +77,11 @@ struct wbem_context {
   double* d_X = nullptr;        // N x 3
   int4* d_cell_dofs = nullptr;  // C
   int* d_dnset = nullptr;       // N x kMaxSet
-  int* d_tile_ptr = nullptr;    // n_tiles + 1
+  int* d_tile_ptr = nullptr;    // n_tiles + 1 (+ the tiles' first columns)
   int2* d_tile_ent = nullptr;
+  int n_tiles64 = 0;            // FP64 column tiles: groups of consecutive patches
+  int* d_tile_ptr64 = nullptr;
+  int2* d_tile_ent64 = nullptr;
   int* d_sptr = nullptr;        // singular panels per row (CSR)
   int* d_scell = nullptr;
   int* d_perm = nullptr;        // internal -> caller

@@ -9,7 +9,10 @@
 namespace wbem {
 
 constexpr int kRowsPerTile = 128;  // collocation rows per assembly CTA (one per thread)
-constexpr int kColsPerTile = 48;   // matrix columns (dofs) per assembly CTA
+constexpr int kColsPerTile = 20;   // dofs per surface patch: the column tile of the mixed far field
+constexpr int kTileGroupF64 = 4;   // consecutive patches per column tile of the FP64 far field
+constexpr int kColsPerTileF64 = kColsPerTile * kTileGroupF64;
+constexpr int kRowsF64 = 64;       // collocation rows per CTA of the FP64 far field
 constexpr int kMaxSet = 8;         // max size of a double-node set
 constexpr int kMaxQ1 = 8;          // max regular quadrature order per direction
 constexpr int kMaxSingular = 2 * 8 * 8;  // max points of a vertex-singular rule

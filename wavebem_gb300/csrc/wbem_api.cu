@@ -254,9 +254,11 @@ static void morton_order(int N, const double* X, std::vector<int>& perm, std::ve
 // Internal dof order in surface patches of at most ct nodes: each patch
 // grows breadth-first over the mesh graph (nodes sharing a cell) from the
 // first node not yet taken in the Morton order, so consecutive patches stay
-// close in space. A patch is a column tile of the assembly: BFS patches are
-// rounder than runs of the Morton order, so fewer panels straddle two tiles
-// (measured on the 32,768-dof tank: 1.33 tiles per panel against 1.47).
+// close in space. A patch is a column tile of the mixed far-field assembly,
+// and groups of consecutive patches are the tiles of the FP64 one: BFS
+// patches are rounder than runs of the Morton order, so fewer panels straddle
+// two tiles (32,768-dof tank, 48-node tiles: 1.33 tiles per panel against
+// 1.47; 20-node patches: 1.50; groups of four of them: 1.34).
 // tstart[t] is the first internal dof of patch t, tstart[T] = N.
 static void patch_order(int N, const double* X, int C, const int* cells, int ct, std::vector<int>& perm,
                         std::vector<int>& iperm, std::vector<int>& tstart) {
@@ -317,44 +319,57 @@ static int build_topology(wbem_context* h) {
   for (int c = 0; c < C; ++c)
     cd[c] = make_int4(ip[h->cells[4 * c]], ip[h->cells[4 * c + 1]], ip[h->cells[4 * c + 2]],
                       ip[h->cells[4 * c + 3]]);
-  // column tiles = the patches
-  h->n_tiles = (int)tstart.size() - 1;
-  std::vector<int> tile_of(N);
-  for (int t = 0; t < h->n_tiles; ++t)
-    for (int i = tstart[t]; i < tstart[t + 1]; ++i) tile_of[i] = t;
-  std::vector<std::vector<int2>> tl(h->n_tiles);
-  for (int c = 0; c < C; ++c) {
-    const int d[4] = {cd[c].x, cd[c].y, cd[c].z, cd[c].w};
-    int tiles[4];
-    int nt = 0;
-    for (int k = 0; k < 4; ++k) {
-      int t = tile_of[d[k]];
-      bool seen = false;
-      for (int u = 0; u < nt; ++u) seen |= tiles[u] == t;
-      if (!seen) tiles[nt++] = t;
-    }
-    const int owner = tile_of[d[0]];
-    for (int u = 0; u < nt; ++u) {
-      uint32_t slots = 0;
+  // column tiles: the patches (mixed far field) and groups of kTileGroupF64
+  // consecutive patches (FP64 far field). Per tile, the panels touching it as
+  // (panel | owner bit, 4 slot bytes: the column of each vertex in the tile,
+  // 255 outside); tile_ptr: [0, T] entry offsets, then [T + 1, 2T + 1] the
+  // tiles' first columns (the tile kernels find them at gridDim.x + 1).
+  auto tile_lists = [&](const std::vector<int>& ts, std::vector<int>& tptr, std::vector<int2>& tent) {
+    const int T = (int)ts.size() - 1;
+    std::vector<int> tile_of(N);
+    for (int t = 0; t < T; ++t)
+      for (int i = ts[t]; i < ts[t + 1]; ++i) tile_of[i] = t;
+    std::vector<std::vector<int2>> tl(T);
+    for (int c = 0; c < C; ++c) {
+      const int d[4] = {cd[c].x, cd[c].y, cd[c].z, cd[c].w};
+      int tiles[4];
+      int nt = 0;
       for (int k = 0; k < 4; ++k) {
-        uint32_t sl = (tile_of[d[k]] == tiles[u]) ? (uint32_t)(d[k] - tstart[tiles[u]]) : 255u;
-        slots |= sl << (8 * k);
+        int t = tile_of[d[k]];
+        bool seen = false;
+        for (int u = 0; u < nt; ++u) seen |= tiles[u] == t;
+        if (!seen) tiles[nt++] = t;
       }
-      int2 e;
-      e.x = c | (tiles[u] == owner ? (int)0x80000000u : 0);
-      e.y = (int)slots;
-      tl[tiles[u]].push_back(e);
+      const int owner = tile_of[d[0]];
+      for (int u = 0; u < nt; ++u) {
+        uint32_t slots = 0;
+        for (int k = 0; k < 4; ++k) {
+          uint32_t sl = (tile_of[d[k]] == tiles[u]) ? (uint32_t)(d[k] - ts[tiles[u]]) : 255u;
+          slots |= sl << (8 * k);
+        }
+        int2 e;
+        e.x = c | (tiles[u] == owner ? (int)0x80000000u : 0);
+        e.y = (int)slots;
+        tl[tiles[u]].push_back(e);
+      }
     }
-  }
-  // tile_ptr: [0, T] entry offsets, then [T + 1, 2T + 1] the tiles' first
-  // columns (tstart); the tile kernels find the second half at gridDim.x + 1
-  std::vector<int> tptr(h->n_tiles + 1, 0);
-  std::vector<int2> tent;
-  for (int t = 0; t < h->n_tiles; ++t) {
-    tent.insert(tent.end(), tl[t].begin(), tl[t].end());
-    tptr[t + 1] = (int)tent.size();
-  }
-  tptr.insert(tptr.end(), tstart.begin(), tstart.end());
+    tptr.assign(T + 1, 0);
+    tent.clear();
+    for (int t = 0; t < T; ++t) {
+      tent.insert(tent.end(), tl[t].begin(), tl[t].end());
+      tptr[t + 1] = (int)tent.size();
+    }
+    tptr.insert(tptr.end(), ts.begin(), ts.end());
+  };
+  h->n_tiles = (int)tstart.size() - 1;
+  std::vector<int> tptr, tptr64;
+  std::vector<int2> tent, tent64;
+  tile_lists(tstart, tptr, tent);
+  std::vector<int> tstart64;
+  for (size_t t = 0; t < tstart.size(); t += kTileGroupF64) tstart64.push_back(tstart[t]);
+  if (tstart64.back() != N) tstart64.push_back(N);
+  h->n_tiles64 = (int)tstart64.size() - 1;
+  tile_lists(tstart64, tptr64, tent64);
   // double-node sets (internal)
   std::vector<int> dnset((size_t)N * kMaxSet, -1);
   for (int p = 0; p < N; ++p) {
@@ -399,6 +414,8 @@ static int build_topology(wbem_context* h) {
   CHK(upload(h, &h->d_dnset, dnset));
   CHK(upload(h, &h->d_tile_ptr, tptr));
   CHK(upload(h, &h->d_tile_ent, tent));
+  CHK(upload(h, &h->d_tile_ptr64, tptr64));
+  CHK(upload(h, &h->d_tile_ent64, tent64));
   CHK(upload(h, &h->d_sptr, sptr));
   CHK(upload(h, &h->d_scell, scell));
   CHK(upload(h, &h->d_perm, h->perm));
@@ -840,7 +857,7 @@ static void release_mesh_buffers(wbem_context* h) {
   cudaStreamSynchronize(h->stream);
   free_lu(h);
   void** ptrs[] = {(void**)&h->d_X, (void**)&h->d_cell_dofs, (void**)&h->d_dnset, (void**)&h->d_tile_ptr,
-                   (void**)&h->d_tile_ent, (void**)&h->d_sptr, (void**)&h->d_scell, (void**)&h->d_perm,
+                   (void**)&h->d_tile_ent, (void**)&h->d_tile_ptr64, (void**)&h->d_tile_ent64, (void**)&h->d_sptr, (void**)&h->d_scell, (void**)&h->d_perm,
                    (void**)&h->d_iperm, (void**)&h->d_ncptr, (void**)&h->d_ncent, (void**)&h->d_mask,
                    (void**)&h->d_rec, (void**)&h->d_rec32, (void**)&h->d_cellc, (void**)&h->d_cellgeo,
                    (void**)&h->d_N, (void**)&h->d_D, (void**)&h->d_A2, (void**)&h->d_B2,
@@ -1064,8 +1081,8 @@ int wbem_assemble(wbem_handle h, const wbem_options* opt) {
     }
     CU(launch_cell_records_fp64(h->C, h->d_X, h->d_cell_dofs, h->d_rec, o.quadrature_order, h->stream));
     h->stats.t_geometry_ms = tm.ms();
-    CU(launch_tile_fp64(N, o.quadrature_order, h->d_X, h->d_dnset, h->n_tiles, h->d_tile_ptr,
-                        h->d_tile_ent, h->d_cell_dofs, h->d_rec, h->d_N, h->d_D, h->d_err, h->stream));
+    CU(launch_tile_fp64(N, o.quadrature_order, h->d_X, h->d_dnset, h->n_tiles64, h->d_tile_ptr64,
+                        h->d_tile_ent64, h->d_cell_dofs, h->d_rec, h->d_N, h->d_D, h->d_err, h->stream));
     h->stats.t_assemble_ms = tm.ms();
     CU(launch_singular_fp64(N, h->d_X, h->d_dnset, h->d_sptr, h->d_scell, h->d_cell_dofs, h->d_N,
                             h->d_D, h->d_err, h->stream));
