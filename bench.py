@@ -263,7 +263,7 @@ def run_reference(args, rank, world):
 # move O(N^2) bytes per launch, so a launch at N dofs is scaled by
 # (N / 8192)^2.
 NCU_TRAFFIC = {
-    "k_tile_mixed": 15.2704e6 + 1294.491e6,
+    "k_tile_mixed": 17.5424e6 + 1314.548e6,
     "k_matvec_mixed": 537.038080e6 + 3.272192e6,
     "k_trsv_wave": 136.424192e6 + 3.058176e6,
 }
@@ -272,7 +272,13 @@ NCU_TRAFFIC = {
 # Warp instructions of one far-field assembly launch at N = 8,192 (ncu
 # smsp__inst_executed.sum); they scale with the (row, panel) pairs, i.e. with
 # N^2 on the same family of meshes.
-NCU_TILE_INSTR = 2677553771.0
+NCU_TILE_INSTR = 2949815885.0
+
+# DRAM bytes of a trailing-update launch over its algorithmic C traffic
+# (8 bytes per element of C, read and written once): 2.114 GB against
+# 2.010 GB for the largest launch at N = 16,384 (15,872 x 15,360, K = 512),
+# from one ncu capture; the operands add the rest.
+NCU_GEMM_TRAFFIC_RATIO = (1.218723e9 + 0.895937e9) / (8.0 * 15872 * 15360)
 
 
 def ncu_traffic(kernel, n):
@@ -481,11 +487,16 @@ def run_gpu(args, rank, world, local):
         kernels = []
         if kprof["gemm_ms"] > 0:
             a = kprof["gemm_flop"] / (kprof["gemm_ms"] / 1e3) / 1e12
+            # sum of M x Nc over the launches (every trailing update has K = 512)
+            mn = kprof["gemm_flop"] / (6.0 * 512)
             kernels.append({"kernel": "k_gemm_bf16x3", "bound": "tensor", "ms": kprof["gemm_ms"],
                             "launches": kprof["gemm_launches"], "achieved": a, "peak": tc,
                             "unit": "TFLOP/s", "frac": a / tc,
                             "work": "3 x 2 M N K per launch (BF16x3 products of the trailing updates)",
-                            "peak_source": f"MEASURED_PEAKS.json bf16_tflops_sustained ({src})"})
+                            "peak_source": f"MEASURED_PEAKS.json bf16_tflops_sustained ({src})",
+                            "traffic_per_launch": NCU_GEMM_TRAFFIC_RATIO * 8.0 * mn / kprof["gemm_launches"],
+                            "traffic_source": "8 bytes per C element per launch (the average launch) times "
+                                              "the DRAM / C-traffic ratio of one ncu capture at N = 16384"})
         # the far-field assembly: bound by FP32 arithmetic (the survey's
         # convention: 36 flop per regular kernel evaluation, 16 evaluations per
         # (row, panel) pair); its HBM figure is reported beside it
@@ -532,9 +543,10 @@ def run_gpu(args, rank, world, local):
         kernels.append({"kernel": "k_panel_small", "ms": kprof["panel_ms"],
                         "launches": kprof["panel_launches"]})
         for k in kernels:
-            tb, _ = ncu_traffic(k["kernel"], N)
+            tb, ts = ncu_traffic(k["kernel"], N)
             if tb is not None:
                 k["traffic_per_launch"] = tb
+                k["traffic_source"] = ts
         if "fp64_phases_ms" in extra and fp64_peak:
             # the plain FP64 form's far-field assembly against the FP64 FMA rate:
             # ~30 FP64 flop per regular evaluation, 16 N C evaluations
@@ -549,8 +561,8 @@ def run_gpu(args, rank, world, local):
         per_launch = dom["ms"] / max(1, dom["launches"])
         roof = {"bound": dom["bound"], "kernel": dom["kernel"], "achieved": dom["achieved"],
                 "peak": dom["peak"], "unit": dom["unit"], "frac": dom["frac"],
-                "traffic": ncu_traffic(dom["kernel"], N)[0],
-                "traffic_source": ncu_traffic(dom["kernel"], N)[1], "ms_per_launch": per_launch,
+                "traffic": dom.get("traffic_per_launch"),
+                "traffic_source": dom.get("traffic_source"), "ms_per_launch": per_launch,
                 "peak_source": dom["peak_source"],
                 "timing": "CUDA events around each launch on its own stream, in an instrumented "
                           "pass after the timed region (factorisation serialised on one stream)"}
