@@ -61,6 +61,14 @@ extern "C" {
                                   inner block-Jacobi GMRES on the FP32 system matrix, run to a
                                   relative residual of 10^-inner_digits */
 
+/* solution methods ("Solution method" of the reference, source/bem_problem.cc:87) */
+#define WBEM_METHOD_DIRECT 0 /* dense N and D (either precision form) */
+#define WBEM_METHOD_FMA 1    /* fast multipole operators: octree, exact near field (FP64 within
+                                two panel diameters, FP32 beyond), Chebyshev-interpolation
+                                expansions of order fma_order for the far field; O(N) memory
+                                and mat-vec; FP64 GMRES with block-Jacobi on the near field.
+                                No matrices to export and no adjoint in this method. */
+
 typedef struct wbem_context* wbem_handle;
 
 typedef struct {
@@ -74,7 +82,10 @@ typedef struct {
   double near_field_ratio;       /* MIXED: a panel is near when |x_i - centre| < ratio * diameter */
   int keep_matrices;             /* keep FP64 N (dG/dn) and D (G) for wbem_get_matrices */
   int inner_digits;              /* GMRES_IR: inner relative tolerance 10^-inner_digits, 0 -> 4 */
-  int reserved[6];
+  int method;                    /* WBEM_METHOD_* ("Solution method"), DIRECT by default */
+  int fma_order;                 /* FMA: Chebyshev points per direction of the expansions, 3..8
+                                    (6 by default; the far field's error falls about 4x per step) */
+  int reserved[4];
 } wbem_options;
 
 typedef struct {

@@ -26,6 +26,7 @@ STATUS = {1: "ERR_ARG", 2: "ERR_STATE", 3: "ERR_CUDA", 4: "ERR_NOMEM", 5: "ERR_S
           6: "ERR_NOCONV", 7: "ERR_NONFINITE", 8: "ERR_TIMEOUT"}
 PREC_FP64, PREC_MIXED = 0, 1
 SOLVER_AUTO, SOLVER_GMRES, SOLVER_LU, SOLVER_GMRES_IR = 0, 1, 2, 3
+METHOD_DIRECT, METHOD_FMA = 0, 1
 
 # every entry point declared in include/wbem.h
 EXPORTS = ["wbem_default_options", "wbem_create", "wbem_destroy", "wbem_last_error",
@@ -51,7 +52,8 @@ class Options(C.Structure):
                 ("singular_quadrature_order", C.c_int), ("gmres_restart", C.c_int),
                 ("max_steps", C.c_int), ("tolerance", C.c_double),
                 ("near_field_ratio", C.c_double), ("keep_matrices", C.c_int),
-                ("inner_digits", C.c_int), ("reserved", C.c_int * 6)]
+                ("inner_digits", C.c_int), ("method", C.c_int), ("fma_order", C.c_int),
+                ("reserved", C.c_int * 4)]
 
 
 class Stats(C.Structure):

@@ -14,7 +14,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libwbem.so")
 PEAKS_LIB = os.path.join(HERE, "libwbem_peaks.so")
 SOURCES = ["wbem_api.cu", "assemble_fp64.cu", "solve.cu", "mixed.cu", "lu.cu", "force.cu", "adjoint.cu", "noalloc.cu",
-           "constraints.cu"]
+           "constraints.cu", "fma.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-Xptxas", "-warn-spills"]

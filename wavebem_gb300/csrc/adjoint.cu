@@ -746,6 +746,8 @@ static int adjoint_run(wbem_context* h, const int* hull_cells, int n_hull, const
                        double* dF_drhs) {
   const int N = h->N, C = h->C;
   const int q1 = h->opt.quadrature_order;
+  if (h->assembled_prec == kAssembledFma)
+    return fail(h, WBEM_ERR_STATE, "the adjoint needs the direct method (no FMA adjoint)");
   if (q1 < 2 || q1 > 6) return fail(h, WBEM_ERR_ARG, "adjoint supports quadrature orders 2..6");
   const bool mixed = h->assembled_prec == WBEM_PREC_MIXED;
   WB_CHK(ensure_vectors(h, h->opt.gmres_restart));

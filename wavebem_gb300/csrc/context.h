@@ -8,6 +8,7 @@
 #include "kernels.h"
 
 constexpr int kNumVec = 10;
+constexpr int kAssembledFma = 2;  // assembled_prec of the FMA method
 
 // Event-bracketed intervals of one kernel class on one stream (kernel
 // profiling mode): begin/end around each launch, summed after the work.
@@ -178,6 +179,12 @@ struct wbem_context {
   double* d_b = nullptr;   // known data (internal order)
   bool have_solution = false;
   std::vector<double> sol_b;  // known data (tmp_rhs) of the last solve, caller order
+
+  // FMA method (fma.cu): octree, near field and expansion buffers; rebuilt
+  // when the nodes or the order change
+  void* fma_state = nullptr;
+  bool fma_geometry_stale = true;
+  wbem::QuadTables quad{};  // the quadrature tables of the last set-up
 
   wbem::DevErr* d_err = nullptr;
   int launches = 0;

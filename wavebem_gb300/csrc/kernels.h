@@ -96,8 +96,10 @@ cudaError_t launch_matvec_s32(int N, int ld, const float* S, const double* x, do
                               cudaStream_t s);
 cudaError_t launch_matvec_s32_t(int N, int ld, const float* S, const double* x, double* y,
                                 double* part, cudaStream_t s);
+// block-Jacobi of the system operator, from N and D (FP64), from the selected
+// pairs A2 (mixed) or from precomputed diagonal blocks (FMA near field)
 cudaError_t launch_bj_build(int N, const double* Nm, const double* Dm, const float2* A2,
-                            const uint8_t* mask, const double* alpha,
+                            const double* blocks, const uint8_t* mask, const double* alpha,
                             const uint8_t* cflag, const int* cptr_full, const int* ccol_full,
                             const double* cval_full, double* binv, DevErr* err, cudaStream_t s);
 cudaError_t launch_bj_apply(int N, const double* binv, const double* x, double* y, int transpose,

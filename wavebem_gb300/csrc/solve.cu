@@ -367,7 +367,8 @@ cudaError_t launch_set_rows(int nrows, const int* crow, const double* val, doubl
 // (column k of the inverse contiguous) for coalesced application.
 __global__ void __launch_bounds__(kBJ)
     k_bj_build(int N, const double* __restrict__ Nm, const double* __restrict__ Dm,
-               const float2* __restrict__ A2, const uint8_t* __restrict__ mask,
+               const float2* __restrict__ A2, const double* __restrict__ blocks,
+               const uint8_t* __restrict__ mask,
                const double* __restrict__ alpha,
                const uint8_t* __restrict__ cflag, const int* __restrict__ cptr,
                const int* __restrict__ ccol, const double* __restrict__ cval,
@@ -390,6 +391,8 @@ __global__ void __launch_bounds__(kBJ)
       v = (r == c) ? 1.0 : 0.0;
     } else if (cflag[i]) {
       v = (r == c) ? 1.0 : 0.0;
+    } else if (blocks) {  // the system's diagonal block, free term included
+      v = blocks[((size_t)b * kBJ + r) * kBJ + c];
     } else {
       const size_t o = (size_t)i * N + j;
       if (Nm) v = mask[j] ? -Dm[o] : Nm[o];
@@ -462,7 +465,7 @@ __global__ void __launch_bounds__(kBJ)
 }
 
 cudaError_t launch_bj_build(int N, const double* Nm, const double* Dm, const float2* A2,
-                            const uint8_t* mask, const double* alpha,
+                            const double* blocks, const uint8_t* mask, const double* alpha,
                             const uint8_t* cflag, const int* cptr_full, const int* ccol_full,
                             const double* cval_full, double* binv, DevErr* err, cudaStream_t s) {
   const size_t smem = (size_t)kBJ * (kBJ + 1) * sizeof(double);
@@ -470,7 +473,7 @@ cudaError_t launch_bj_build(int N, const double* Nm, const double* Dm, const flo
                                        (int)smem);
   if (e != cudaSuccess) return e;
   const int nb = (N + kBJ - 1) / kBJ;
-  k_bj_build<<<nb, kBJ, smem, s>>>(N, Nm, Dm, A2, mask, alpha, cflag, cptr_full, ccol_full,
+  k_bj_build<<<nb, kBJ, smem, s>>>(N, Nm, Dm, A2, blocks, mask, alpha, cflag, cptr_full, ccol_full,
                                    cval_full, binv, err);
   return cudaGetLastError();
 }

@@ -32,6 +32,10 @@ int adjoint_force(wbem_context* h, const int* hull_cells, int n_hull, const doub
                   double* dF_dX, double* dF_drhs);
 int adjoint_objective(wbem_context* h, const double* dJ_dphi, const double* dJ_ddn, double* dJ_dX,
                       double* dJ_drhs);
+int assemble_fma(wbem_context* h, const QuadTables& qt);
+int fma_apply(wbem_context* h, int mode, const double* x, double* y);
+int fma_near_blocks(wbem_context* h, double** blocks);
+void free_fma(wbem_context* h);
 int hull_force_dev(wbem_context* h, const int* hull_cells, int n_hull, const double* U, int dir,
                    const double* d_phi, const double* d_dphi, double* force);
 }  // namespace wbem
@@ -152,6 +156,7 @@ static int build_quadrature(wbem_context* h, int q1, int sorder) {
   CU(upload_quadrature_fp64(t));
   CU(upload_quadrature_mixed(t));
   CU(upload_quadrature_adjoint(t));
+  h->quad = t;
   return WBEM_OK;
 }
 
@@ -454,7 +459,9 @@ int ensure_vectors(wbem_context* h, int restart) {
 
 // y = A x (constrained system operator), FP64 or mixed storage.
 int apply_system(wbem_context* h, const double* x, double* y) {
-  if (h->assembled_prec == WBEM_PREC_FP64)
+  if (h->assembled_prec == kAssembledFma)
+    CHK(fma_apply(h, 0, x, y));
+  else if (h->assembled_prec == WBEM_PREC_FP64)
     CU(launch_matvec_fp64(h->N, 0, h->d_N, h->d_D, h->d_mask, h->d_alpha, x, y, h->stream));
   else {
     if (h->profiling) h->prof_matvec.begin(h->stream);
@@ -468,6 +475,8 @@ int apply_system(wbem_context* h, const double* x, double* y) {
 
 // y = A^T x for the constrained operator.
 int apply_system_t(wbem_context* h, const double* x, double* y) {
+  if (h->assembled_prec == kAssembledFma)
+    return fail(h, WBEM_ERR_STATE, "the FMA method has no transposed operator");
   // x with its constrained entries zeroed feeds the unconstrained rows
   double* xz = h->d_vec[7];
   CU(cudaMemcpyAsync(xz, x, sizeof(double) * h->N, cudaMemcpyDeviceToDevice, h->stream));
@@ -646,9 +655,12 @@ int build_block_jacobi(wbem_context* h) {
   const int nb = (h->N + kBJ - 1) / kBJ;
   CHK(dev_alloc(h, &h->d_binv, (size_t)nb * kBJ * kBJ));
   const bool fp64 = h->assembled_prec == WBEM_PREC_FP64;
-  CU(launch_bj_build(h->N, fp64 ? h->d_N : nullptr, fp64 ? h->d_D : nullptr, h->d_A2,
-                     h->d_mask, h->d_alpha, h->d_cflag, h->d_cptr_full, h->d_ccol_full,
-                     h->d_cval_full, h->d_binv, h->d_err, h->stream));
+  double* blocks = nullptr;  // FMA: the near field's diagonal blocks
+  if (h->assembled_prec == kAssembledFma) CHK(fma_near_blocks(h, &blocks));
+  CU(launch_bj_build(h->N, fp64 ? h->d_N : nullptr, fp64 ? h->d_D : nullptr,
+                     blocks ? nullptr : h->d_A2, blocks, h->d_mask, h->d_alpha, h->d_cflag,
+                     h->d_cptr_full, h->d_ccol_full, h->d_cval_full, h->d_binv, h->d_err,
+                     h->stream));
   h->launches++;
   return check_device_error(h, "block-Jacobi");
 }
@@ -735,6 +747,8 @@ int build_constraint_structure(wbem_context* h) {
 // The solver an assembly uses (the AUTO choice resolved), or -1 if the
 // option does not apply to the assembled precision.
 int resolved_solver(const wbem_context* h) {
+  if (h->assembled_prec == kAssembledFma)
+    return (h->opt.solver == WBEM_SOLVER_AUTO || h->opt.solver == WBEM_SOLVER_GMRES) ? WBEM_SOLVER_GMRES : -1;
   const bool fp64 = h->assembled_prec == WBEM_PREC_FP64;
   switch (h->opt.solver) {
     case WBEM_SOLVER_AUTO:
@@ -822,6 +836,8 @@ int wbem_default_options(wbem_options* o) {
   o->tolerance = 1e-12;
   o->near_field_ratio = 2.0;
   o->keep_matrices = 1;
+  o->method = WBEM_METHOD_DIRECT;
+  o->fma_order = 6;
   return WBEM_OK;
 }
 
@@ -856,6 +872,7 @@ int wbem_create(wbem_handle* out, int device) {
 static void release_mesh_buffers(wbem_context* h) {
   cudaStreamSynchronize(h->stream);
   free_lu(h);
+  free_fma(h);
   void** ptrs[] = {(void**)&h->d_X, (void**)&h->d_cell_dofs, (void**)&h->d_dnset, (void**)&h->d_tile_ptr,
                    (void**)&h->d_tile_ent, (void**)&h->d_tile_ptr64, (void**)&h->d_tile_ent64, (void**)&h->d_sptr, (void**)&h->d_scell, (void**)&h->d_perm,
                    (void**)&h->d_iperm, (void**)&h->d_ncptr, (void**)&h->d_ncent, (void**)&h->d_mask,
@@ -925,8 +942,6 @@ int wbem_set_geometry(wbem_handle h, const double* X, int n_dofs, const int* cel
   if (!h) return WBEM_ERR_ARG;
   if (!X || !cells || n_dofs < 1 || n_cells < 1)
     return fail(h, WBEM_ERR_ARG, "wbem_set_geometry: empty mesh or NULL pointer");
-  if ((long long)n_dofs * n_dofs > (1LL << 34))
-    return fail(h, WBEM_ERR_ARG, "wbem_set_geometry: n_dofs too large for a dense N x N matrix");
   if ((dn_ptr == nullptr) != (dn_idx == nullptr))
     return fail(h, WBEM_ERR_ARG, "wbem_set_geometry: dn_ptr and dn_idx must both be given or both NULL");
   for (long long k = 0; k < 3LL * n_dofs; ++k)
@@ -973,6 +988,7 @@ int wbem_set_geometry(wbem_handle h, const double* X, int n_dofs, const int* cel
   h->assembled_prec = -1;
   h->factors_valid = false;
   h->have_solution = false;
+  h->fma_geometry_stale = true;
   CHK(build_quadrature(h, h->opt.quadrature_order, h->opt.singular_quadrature_order));
   CHK(build_topology(h));
   if (h->have_mask && (int)h->mask.size() == n_dofs) {
@@ -996,6 +1012,7 @@ int wbem_update_nodes(wbem_handle h, const double* X) {
   for (int i = 0; i < h->N; ++i)
     for (int d = 0; d < 3; ++d) Xi[3 * (size_t)i + d] = X[3 * (size_t)h->perm[i] + d];
   CU(copy_sync(h, h->d_X, Xi.data(), Xi.size() * sizeof(double), cudaMemcpyHostToDevice));
+  h->fma_geometry_stale = true;  // the octree follows the nodes
   h->assembled_prec = -1;
   h->factors_valid = false;
   h->have_solution = false;
@@ -1052,6 +1069,10 @@ int wbem_assemble(wbem_handle h, const wbem_options* opt) {
     return fail(h, WBEM_ERR_ARG, "wbem_assemble: gmres_restart must be in [1,250]");
   if (o.max_steps < 1) return fail(h, WBEM_ERR_ARG, "wbem_assemble: max_steps must be >= 1");
   if (!(o.tolerance >= 0)) return fail(h, WBEM_ERR_ARG, "wbem_assemble: tolerance must be >= 0");
+  if (o.method != WBEM_METHOD_DIRECT && o.method != WBEM_METHOD_FMA)
+    return fail(h, WBEM_ERR_ARG, "wbem_assemble: unknown method");
+  if (o.method == WBEM_METHOD_DIRECT && (long long)h->N * h->N > (1LL << 34))
+    return fail(h, WBEM_ERR_ARG, "wbem_assemble: n_dofs too large for dense N x N matrices (use the FMA method)");
   h->opt = o;
   cudaSetDevice(h->device);
   CHK(build_quadrature(h, o.quadrature_order, o.singular_quadrature_order));
@@ -1063,7 +1084,16 @@ int wbem_assemble(wbem_handle h, const wbem_options* opt) {
   h->have_solution = false;
   const int N = h->N;
   Timer tm(h->stream);
-  if (o.precision == WBEM_PREC_FP64) {
+  if (o.method == WBEM_METHOD_FMA) {
+    // no dense matrices in this method
+    free_mixed(h);
+    free_lu(h);
+    if (h->d_N) { cudaFree(h->d_N); h->d_N = nullptr; }
+    if (h->d_D) { cudaFree(h->d_D); h->d_D = nullptr; }
+    h->mat_elems = 0;
+    CHK(assemble_fma(h, h->quad));
+    h->assembled_prec = kAssembledFma;
+  } else if (o.precision == WBEM_PREC_FP64) {
     free_mixed(h);
     const size_t nn = (size_t)N * N;
     if (!h->d_N || h->mat_elems != nn || h->d_A2) {
@@ -1121,7 +1151,13 @@ static int prepare_rhs(wbem_handle h, const double* tmp_rhs, bool beside = false
     CU(cudaStreamWaitEvent(h->rhs_stream, h->ev_rhs, 0));
     rs = h->rhs_stream;
   }
-  if (h->assembled_prec == WBEM_PREC_FP64)
+  if (h->assembled_prec == kAssembledFma) {
+    if (rs != h->stream) {  // the FMA product runs on the handle's stream
+      CU(cudaStreamWaitEvent(h->stream, h->ev_rhs, 0));
+      rs = h->stream;
+    }
+    CHK(fma_apply(h, 1, h->d_b, h->d_rhs));
+  } else if (h->assembled_prec == WBEM_PREC_FP64)
     CU(launch_matvec_fp64(N, 1, h->d_N, h->d_D, h->d_mask, h->d_alpha, h->d_b, h->d_rhs, rs));
   else
     CU(launch_matvec_mixed(N, 1, h->d_B2, h->d_mask, h->d_alpha, h->d_b, h->d_rhs, rs));
@@ -1193,6 +1229,8 @@ int wbem_get_alpha(wbem_handle h, double* alpha) {
 int wbem_get_matrices(wbem_handle h, double* neumann, double* dirichlet) {
   if (!h) return WBEM_ERR_ARG;
   if (h->assembled_prec < 0) return fail(h, WBEM_ERR_STATE, "wbem_get_matrices: assemble first");
+  if (h->assembled_prec == kAssembledFma)
+    return fail(h, WBEM_ERR_STATE, "wbem_get_matrices: the FMA method keeps no dense matrices");
   cudaSetDevice(h->device);
   const int N = h->N;
   const int rows_per = std::max(1, (int)std::min<size_t>((size_t)N, (size_t)(64u << 20) / (8 * (size_t)N)));
@@ -1233,7 +1271,9 @@ static int op_caller(wbem_handle h, int mode, const double* src, double* dst) {
   std::vector<double> xi(N), yi(N);
   for (int i = 0; i < N; ++i) xi[i] = src[h->perm[i]];
   CU(copy_sync(h, h->d_vec[3], xi.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
-  if (h->assembled_prec == WBEM_PREC_FP64)
+  if (h->assembled_prec == kAssembledFma)
+    CHK(fma_apply(h, mode, h->d_vec[3], h->d_vec[4]));
+  else if (h->assembled_prec == WBEM_PREC_FP64)
     CU(launch_matvec_fp64(N, mode, h->d_N, h->d_D, h->d_mask, h->d_alpha, h->d_vec[3], h->d_vec[4], h->stream));
   else
     CU(launch_matvec_mixed(N, mode, mode == 0 ? h->d_A2 : h->d_B2, h->d_mask, h->d_alpha, h->d_vec[3],
