@@ -325,8 +325,8 @@ def run_gpu(args, rank, world, local):
     import ctypes
     import torch
     from wavebem_gb300 import meshes as M
-    from wavebem_gb300.bem_problem import (PREC_FP64, PREC_MIXED, SOLVER_GMRES_IR, SOLVER_LU,
-                                           BEMProblem, load_library)
+    from wavebem_gb300.bem_problem import (METHOD_FMA, PREC_FP64, PREC_MIXED, SOLVER_GMRES_IR,
+                                           SOLVER_LU, BEMProblem, load_library)
 
     torch.cuda.set_device(local)
     L = load_library()
@@ -420,6 +420,40 @@ def run_gpu(args, rank, world, local):
     g.close()
     del g
 
+    # the FMA method on the same workload (O(N) memory and mat-vec), and on a
+    # 135,002-node cube-sphere whose dense N and D would need 290 GB
+    gf = BEMProblem(m.X, m.cells, m.dirichlet, ptr, idx, device=local, method=METHOD_FMA, fma_order=6)
+    assert L.wbem_set_stream(gf.h, ctypes.c_void_p(stream.cuda_stream)) == 0
+    phi_f, dphi_f = b.copy(), b.copy()
+    gf.solve(phi_f, dphi_f, b)
+    fma_s = timed(stream, lambda: gf.solve(phi_f, dphi_f, b), 2)
+    st_f = gf.stats()
+    F_f = gf.hull_force(hull, phi_f, dphi_f)
+    vm_s = timed(stream, lambda: gf.vmult(b), 5)
+    variants["fma"] = {"s": fma_s, "order": 6, "iterations": st_f["iterations"],
+                       "assemble_ms": st_f["t_geometry_ms"] + st_f["t_singular_ms"] + st_f["t_alpha_ms"],
+                       "vmult_ms_host": vm_s * 1e3,
+                       "what": "octree + Chebyshev far field (order 6) + on-the-fly near field with FP64 "
+                               "close-pair corrections, FP64 GMRES with near-field block-Jacobi"}
+    gf.close()
+    del gf
+    ms_ = M.cube_sphere_mesh(150)
+    ps_, is_ = M.double_nodes(ms_.X, ms_.cells)
+    p_s, dp_s = M.sphere_harmonics(ms_.X, seed=1)
+    for order in (6, 8):
+        gs = BEMProblem(ms_.X, ms_.cells, ms_.dirichlet, ps_, is_, device=local, method=METHOD_FMA,
+                        fma_order=order, max_steps=2000)
+        assert L.wbem_set_stream(gs.h, ctypes.c_void_p(stream.cuda_stream)) == 0
+        ph_s, dph_s = p_s.copy(), np.zeros_like(p_s)
+        gs.solve(ph_s, dph_s, p_s)
+        s_s = timed(stream, lambda: gs.solve(ph_s, dph_s, p_s), 1)
+        variants[f"fma_sphere_order{order}"] = {
+            "s": s_s, "n_dofs": ms_.n_dofs, "iterations": gs.stats()["iterations"],
+            "rel_err_vs_exact": float(np.linalg.norm(dph_s - dp_s) / np.linalg.norm(dp_s)),
+            "what": "all-Dirichlet cube-sphere (harmonic polynomial data), dphi/dn against the exact one"}
+        gs.close()
+        del gs
+
     # shape-parameter adjoint workload: N = 8,192 Wigley hull with 8 seeded
     # shape parameters (the configuration's seeds)
     m8, p8, i8, b8 = M.config_case("c3")
@@ -450,6 +484,8 @@ def run_gpu(args, rank, world, local):
                                      "hull_force": abs(F_mx - F64) / abs(F64)},
                  "fp64_phases_ms": {k: st64[k] for k in phase}}
         variants["gmres_ir"]["rel_err_vs_fp64"] = {"phi": nrm(phi_ir, p64), "dphi_dn": nrm(dphi_ir, d64)}
+        variants["fma"]["rel_err_vs_fp64"] = {"phi": nrm(phi_f, p64), "dphi_dn": nrm(dphi_f, d64),
+                                              "hull_force": abs(F_f - F64) / abs(F64)}
         g64.close()
         del g64
 
@@ -471,7 +507,9 @@ def run_gpu(args, rank, world, local):
                              f"({full['gmres_iterations']} its) on {threads} host threads"}
             errs = {"mixed": {"phi": nrm(phi_mx, phi_o), "dphi_dn": nrm(dphi_mx, dphi_o),
                               "hull_force": abs(F_mx - F_o) / abs(F_o)},
-                    "gmres_ir": {"phi": nrm(phi_ir, phi_o), "dphi_dn": nrm(dphi_ir, dphi_o)}}
+                    "gmres_ir": {"phi": nrm(phi_ir, phi_o), "dphi_dn": nrm(dphi_ir, dphi_o)},
+                    "fma": {"phi": nrm(phi_f, phi_o), "dphi_dn": nrm(dphi_f, dphi_o),
+                            "hull_force": abs(F_f - F_o) / abs(F_o)}}
             if fp64 is not None:
                 errs["fp64"] = {"phi": nrm(fp64[0], phi_o), "dphi_dn": nrm(fp64[1], dphi_o),
                                 "hull_force": abs(fp64[2] - F_o) / abs(F_o)}
