@@ -1066,12 +1066,14 @@ struct LuState {
   cudaStream_t s_panel = nullptr;
   cudaStream_t s_row = nullptr;
   cudaStream_t s_inrow = nullptr;      // in-panel row panel, beside the column panel
+  cudaStream_t s_col2 = nullptr;       // column panel and in-panel update below the next block
   cudaStream_t s_trail = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_row = nullptr, ev_trail = nullptr, ev_join = nullptr;
   cudaEvent_t ev_next_rows = nullptr;  // bulk update of the next panel's rows done
   cudaEvent_t ev_blk = nullptr;        // diagonal block ready for its row panel
   cudaEvent_t ev_inrow = nullptr;      // in-panel row panel done
   cudaEvent_t ev_u12 = nullptr;        // row panel of the outer panel done
+  cudaEvent_t ev_col2[2] = {nullptr, nullptr};  // s_col2 work of block k done (k % 2)
   float* w = nullptr;         // 2 x N ping-pong vectors
   unsigned* flags = nullptr;  // 4 x nblk publication flags
   unsigned epoch = 0;
@@ -1098,8 +1100,9 @@ void free_lu(wbem_context* h) {
   if (L.s_trail) cudaStreamDestroy(L.s_trail);
   if (L.s_row) cudaStreamDestroy(L.s_row);
   if (L.s_inrow) cudaStreamDestroy(L.s_inrow);
+  if (L.s_col2) cudaStreamDestroy(L.s_col2);
   for (cudaEvent_t e : {L.ev_fork, L.ev_row, L.ev_trail, L.ev_join, L.ev_next_rows, L.ev_blk, L.ev_u12,
-                        L.ev_inrow})
+                        L.ev_inrow, L.ev_col2[0], L.ev_col2[1]})
     if (e) cudaEventDestroy(e);
   if (L.w) cudaFree(L.w);
   if (L.flags) cudaFree(L.flags);
@@ -1258,8 +1261,9 @@ int factor_mixed(wbem_context* h) {
     WB_CU(cudaStreamCreateWithPriority(&L.s_trail, cudaStreamNonBlocking, lo));
     WB_CU(cudaStreamCreateWithPriority(&L.s_row, cudaStreamNonBlocking, hi < lo ? hi + 1 : hi));
     WB_CU(cudaStreamCreateWithPriority(&L.s_inrow, cudaStreamNonBlocking, hi));
+    WB_CU(cudaStreamCreateWithPriority(&L.s_col2, cudaStreamNonBlocking, hi));
     for (cudaEvent_t* e : {&L.ev_fork, &L.ev_row, &L.ev_trail, &L.ev_join, &L.ev_next_rows, &L.ev_blk,
-                           &L.ev_u12, &L.ev_inrow})
+                           &L.ev_u12, &L.ev_inrow, &L.ev_col2[0], &L.ev_col2[1]})
       WB_CU(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
   }
   EvTimer tm(h->stream);
@@ -1274,6 +1278,13 @@ int factor_mixed(wbem_context* h) {
   //     panel's columns [p1, p2).
   //   s_inrow: the in-panel row panel of block k (U_kj for the panel's
   //     columns right of the block), beside the column panel of block k.
+  //   s_col2: the column panel and the in-panel update of block k for the
+  //     rows below block k + 1, beside the diagonal block k + 1; s_panel
+  //     does them for the rows of block k + 1 only (the strip the next
+  //     diagonal block and the next strip need), so the chain of diagonal
+  //     blocks does not wait for the full-height panel products. Block k's
+  //     diagonal block needs the s_col2 work of block k - 2 (its rows lie
+  //     below block k - 1), the strip of block k that of block k - 1.
   //   s_row: the row panel U12 of P (rows [p0, p1), columns [p1, N)), block
   //     row k as soon as diagonal block k is factored, beside the column work.
   //   s_trail: the trailing update of the columns [p2, N): first the next
@@ -1288,6 +1299,7 @@ int factor_mixed(wbem_context* h) {
   cudaStream_t sp = prof ? h->stream : L.s_panel, st = prof ? h->stream : L.s_trail;
   cudaStream_t su = prof ? h->stream : L.s_row;
   cudaStream_t sr = prof ? h->stream : L.s_inrow;
+  cudaStream_t sc = prof ? h->stream : L.s_col2;
   if (prof) {
     h->prof_gemm.reset();
     h->prof_diag.reset();
@@ -1307,6 +1319,8 @@ int factor_mixed(wbem_context* h) {
   WB_CU(cudaStreamWaitEvent(st, L.ev_fork, 0));
   WB_CU(cudaStreamWaitEvent(su, L.ev_fork, 0));
   WB_CU(cudaStreamWaitEvent(sr, L.ev_fork, 0));
+  WB_CU(cudaStreamWaitEvent(sc, L.ev_fork, 0));
+  for (int e = 0; e < 2; ++e) WB_CU(cudaEventRecord(L.ev_col2[e], sc));
   bool trail_pending = false;  // a trailing update was queued on s_trail
   for (int p0 = 0; p0 < N; p0 += kNB2) {
     const int p1 = std::min(N, p0 + kNB2);
@@ -1316,6 +1330,7 @@ int factor_mixed(wbem_context* h) {
     for (int k0 = p0; k0 < p1; k0 += kNB) {
       const int k = k0 / kNB, nb = std::min(kNB, N - k0), k1 = k0 + nb;
       const size_t bo = (size_t)k * kNB * kNB;
+      WB_CU(cudaStreamWaitEvent(sp, L.ev_col2[k & 1], 0));  // s_col2 work of block k - 2
       pb(h->prof_diag, sp);
       k_diag_block<<<1, kDiagThreads, kDiagSmem, sp>>>(ld, k0, nb, A, L.linv + bo, L.uinv + bo,
                                                         L.linvT + bo, L.uinvT + bo, h->d_err);
@@ -1356,27 +1371,53 @@ int factor_mixed(wbem_context* h) {
       }
       if (k1 >= N) break;
       const int m = N - k1;
+      const int sh = std::min(kNB, m);  // the strip: rows of block k + 1
       const SplitOut L21{b2, b2 + rows * kNB2, p1, kNB2, k0 - p0};
-      // column panel (full height), inner split + outer L21 split
-      // L_ik = A_ik inv(U_kk) for rows k1.., in place
+      const SplitOut l21 = p1 < N ? L21 : none;
+      // column panel L_ik = A_ik inv(U_kk), in place, with the outer L21
+      // split: the strip on s_panel (after the s_col2 work of block k - 1,
+      // which updated these rows), the rows below on s_col2
+      WB_CU(cudaStreamWaitEvent(sp, L.ev_col2[(k + 1) & 1], 0));
       const PanelArgs pc{A + (size_t)k1 * ld + k0, ld, L.uinv + bo, kNB, A + (size_t)k1 * ld + k0,
-                         ld, m, kNB, kNB, k1, k0, 0, 0};
+                         ld, sh, kNB, kNB, k1, k0, 0, 0};
       pb(h->prof_panel, sp);
-      WB_CU((run_panel_small<64, 128, false>(pc, none, p1 < N ? L21 : none, sp)));
+      WB_CU((run_panel_small<64, 128, false>(pc, none, l21, sp)));
       pe(h->prof_panel, sp, 0.0);
       h->launches++;
+      if (m > sh) {
+        WB_CU(cudaStreamWaitEvent(sc, L.ev_blk, 0));
+        const int k2 = k1 + sh;
+        const PanelArgs pc2{A + (size_t)k2 * ld + k0, ld, L.uinv + bo, kNB, A + (size_t)k2 * ld + k0,
+                            ld, m - sh, kNB, kNB, k2, k0, 0, 0};
+        pb(h->prof_panel, sc);
+        WB_CU((run_panel_small<64, 128, false>(pc2, none, l21, sc)));
+        pe(h->prof_panel, sc, 0.0);
+        h->launches++;
+      }
       if (k1 < p1) {
         const int w = p1 - k1;
-        // inner update A[k1:, k1:p1] -= L_ik U_kj in FP32 (small footprint, so
-        // it runs beside the previous outer panel's bulk update)
+        // in-panel update A[k1:, k1:p1] -= L_ik U_kj in FP32 (small footprint,
+        // so it runs beside the previous outer panel's bulk update): the strip
+        // on s_panel, the rows below on s_col2
         WB_CU(cudaStreamWaitEvent(sp, L.ev_inrow, 0));
         const PanelArgs pi{A + (size_t)k1 * ld + k0, ld, A + (size_t)k0 * ld + k1, ld,
-                           A + (size_t)k1 * ld + k1, ld, m, w, kNB, k1, k1, 1, 0};
+                           A + (size_t)k1 * ld + k1, ld, sh, w, kNB, k1, k1, 1, 0};
         pb(h->prof_panel, sp);
         WB_CU((run_panel_small<64, 128, false>(pi, none, none, sp)));
         pe(h->prof_panel, sp, 0.0);
         h->launches++;
+        if (m > sh) {
+          const int k2 = k1 + sh;
+          WB_CU(cudaStreamWaitEvent(sc, L.ev_inrow, 0));
+          const PanelArgs pi2{A + (size_t)k2 * ld + k0, ld, A + (size_t)k0 * ld + k1, ld,
+                              A + (size_t)k2 * ld + k1, ld, m - sh, w, kNB, k2, k1, 1, 0};
+          pb(h->prof_panel, sc);
+          WB_CU((run_panel_small<64, 128, false>(pi2, none, none, sc)));
+          pe(h->prof_panel, sc, 0.0);
+          h->launches++;
+        }
       }
+      WB_CU(cudaEventRecord(L.ev_col2[k & 1], sc));
       WB_CU(cudaGetLastError());
     }
     if (p1 >= N) break;
@@ -1385,6 +1426,8 @@ int factor_mixed(wbem_context* h) {
     const int p2 = std::min(N, p1 + kNB2);
     WB_CU(cudaEventRecord(L.ev_u12, su));
     WB_CU(cudaStreamWaitEvent(sp, L.ev_u12, 0));
+    WB_CU(cudaEventRecord(L.ev_join, sc));  // every column panel's rows below the strips
+    WB_CU(cudaStreamWaitEvent(sp, L.ev_join, 0));
     if (trail_pending) WB_CU(cudaStreamWaitEvent(sp, L.ev_trail, 0));
     pb(h->prof_gemm, sp);
     WB_CU(run_gemm(L.maps2[buf], L.cmap, p1, p1, 0, 0, n, p2 - p1, p1 - p0, h->d_err, sp));
@@ -1414,6 +1457,8 @@ int factor_mixed(wbem_context* h) {
   }
   // join the streams back into the handle's stream
   WB_CU(cudaEventRecord(L.ev_join, sr));
+  WB_CU(cudaStreamWaitEvent(h->stream, L.ev_join, 0));
+  WB_CU(cudaEventRecord(L.ev_join, sc));
   WB_CU(cudaStreamWaitEvent(h->stream, L.ev_join, 0));
   WB_CU(cudaEventRecord(L.ev_join, su));
   WB_CU(cudaStreamWaitEvent(h->stream, L.ev_join, 0));
