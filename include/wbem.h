@@ -47,14 +47,14 @@ extern "C" {
 #define WBEM_PREC_FP64 0  /* plain: FP64 everywhere */
 #define WBEM_PREC_MIXED 1 /* FP32 far field (double-float panel base + FP32 quadrature deltas),
                              FP64 singular/near field and alpha; (hi, lo) FP32 storage;
-                             FP32 LU (BF16x3 tensor-core updates) or FP32 inner GMRES,
+                             FP32 LU (TF32 tensor-core updates) or FP32 inner GMRES,
                              refined to full accuracy in FP64 */
 
 /* linear solvers */
 #define WBEM_SOLVER_AUTO 0     /* FP64 -> GMRES; MIXED -> LU */
 #define WBEM_SOLVER_GMRES 1    /* FP64 GMRES(restart) on the assembled operator, block-Jacobi
                                   preconditioner (either precision) */
-#define WBEM_SOLVER_LU 2       /* MIXED only: FP32 dense LU (BF16x3 tensor-core updates) as the
+#define WBEM_SOLVER_LU 2       /* MIXED only: FP32 dense LU (TF32 tensor-core updates) as the
                                   preconditioner of FP64 GMRES; the factors are reused by every
                                   solve until the next assembly */
 #define WBEM_SOLVER_GMRES_IR 3 /* MIXED only: FP64 iterative refinement; each correction is an

@@ -19,6 +19,11 @@ extern "C" {
  * synchronizes. Returns a wbem.h status. */
 int wbem_test_gemm_bf16x3(int M, int Nc, int K, const float* dA, const float* dB, float* dC);
 
+/* The same update as one TF32 product (kind::tf32 tcgen05.mma on the FP32
+ * operands, FP32 accumulation in TMEM): the LU's trailing update. Same
+ * arguments, conditions and synchronisation as wbem_test_gemm_bf16x3. */
+int wbem_test_gemm_tf32(int M, int Nc, int K, const float* dA, const float* dB, float* dC);
+
 /* The mixed-precision system matrix and its LU factors, for factor tests.
  * After wbem_assemble (WBEM_PREC_MIXED) and wbem_set_bc: forms the FP32
  * system matrix S (the constrained operator with alpha on its diagonal, rows
@@ -44,8 +49,8 @@ int wbem_test_lu_apply(struct wbem_context* h, const double* v, double* z, int t
  * pass next to the timed one. The profile covers the last factorisation and
  * the solves since then (reset by each factorisation). */
 typedef struct {
-  double gemm_ms;       /* k_gemm_bf16x3: tensor-core trailing updates */
-  double gemm_flop;     /*   their work: 3 x 2 M N K per launch (three BF16 products) */
+  double gemm_ms;       /* k_gemm_tc<TF32>: tensor-core trailing updates */
+  double gemm_flop;     /*   their work: 2 M N K per launch (one TF32 product) */
   int gemm_launches;
   double diag_ms;       /* k_diag_block: 128 x 128 diagonal LU + triangle inverses */
   int diag_launches;

@@ -26,8 +26,9 @@ def test_lu_factor_residual(factored):
     L = np.tril(LU.astype(np.float64), -1) + np.eye(N)
     U = np.triu(LU.astype(np.float64))
     R = S.astype(np.float64) - L @ U
-    # FP32 factors with BF16x3 (about 17 significant bits) trailing updates
-    assert np.abs(R).max() <= 2e-6 * np.abs(S).max()
+    # FP32 factors with TF32 trailing updates (11 significant bits per
+    # operand, one product): measured 3.0e-5 of the largest entry at N = 2,000
+    assert np.abs(R).max() <= 1e-4 * np.abs(S).max()
     # no pivoting: the diagonal dominates, no growth
     assert np.abs(U).max() <= 1.5 * np.abs(S).max()
 
@@ -49,4 +50,6 @@ def test_lu_sweeps_match_cpu(factored, transpose):
         zc = sla.solve_triangular(U, sla.solve_triangular(L, v, lower=True, unit_diagonal=True))
         Sz = S.astype(np.float64) @ z
     assert np.linalg.norm(z - zc) <= 1e-6 * np.linalg.norm(zc)
-    assert np.linalg.norm(v - Sz) <= 5e-6 * np.linalg.norm(v)
+    # the factors as a preconditioner of S (TF32 trailing updates: measured
+    # 1.0e-4 at N = 2,000; the FP64 GMRES refinement sets the final accuracy)
+    assert np.linalg.norm(v - Sz) <= 3e-4 * np.linalg.norm(v)

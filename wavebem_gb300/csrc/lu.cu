@@ -1,4 +1,4 @@
-// FP32 blocked LU (no pivoting) of the collocation system with BF16x3
+// FP32 blocked LU (no pivoting) of the collocation system with TF32
 // tensor-core trailing updates (tcgen05 + TMEM + TMA), and the FP32 block
 // triangular solves used as the preconditioner of the FP64 GMRES refinement.
 //
@@ -15,17 +15,25 @@
 //   1. k_diag_block: LU of A_kk (one CTA, registers + shared memory), plus
 //      the inverses of its unit-lower and upper factors;
 //   2. k_panel_small: L_ik = A_ik inv(U_kk) and U_kj = inv(L_kk) A_kj (FP32
-//      SIMT), the column panel also writing the BF16 hi/lo split of L21;
-//      then the panel's own trailing update A_ij -= L_ik U_kj (FP32, K = 128).
+//      SIMT); then the panel's own trailing update A_ij -= L_ik U_kj (FP32,
+//      K = 128). Both run first for the next block's 128 rows (the strip the
+//      next diagonal block needs) and then, on a second stream, for the rows
+//      below.
 // Per outer panel P: U12 = inv(L11) A12 for the rest of its rows (FP32, with
 // the earlier blocks' updates first; block row k as soon as A_kk is factored,
-// on its own stream), then the bulk trailing update
-// A22 -= L21 U12 on the tensor cores, k_gemm_bf16x3: Lhi Uhi + Lhi Ulo +
-// Llo Uhi with FP32 accumulation in TMEM, K = 512, persistent 128 x 256
-// tiles. It is split between the next panel's columns (high-priority stream)
-// and the remainder (low-priority stream). The panel kernels have a 13 KB
-// footprint, so the next panel's chain runs beside the remainder's CTAs on
-// every SM (look-ahead); a few SMs stay free for the 200 KB diagonal blocks.
+// on its own stream, writing an FP32 copy of U12^T), then the bulk trailing
+// update A22 -= L21 U12 on the tensor cores, k_gemm_tc<true>: one TF32
+// product (kind::tf32, L21 read in place from the LU buffer, U12^T from the
+// copy) with FP32 accumulation in TMEM, K = 512, persistent 128 x 256 tiles.
+// One TF32 product instead of three BF16 products (hi x hi + hi x lo +
+// lo x hi) leaves the preconditioner about 20x coarser (residual 1e-4 of a
+// vector instead of 5e-6) for one more GMRES iteration, and takes 8% off the
+// update, which streams the same operand bytes per K step either way.
+// The update is split between the next panel's columns (high-priority
+// stream) and the remainder (low-priority stream). The panel kernels have a
+// 13 KB footprint, so the next panel's chain runs beside the remainder's CTAs
+// on every SM (look-ahead); a few SMs stay free for the 200 KB diagonal
+// blocks.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -256,6 +264,7 @@ struct SplitOut {
   int row0;       // absolute matrix index of split row 0
   int ld;         // row length (K of the GEMM that consumes it)
   int coloff;     // column offset inside a row
+  float* f32 = nullptr;  // instead of hi / lo: the FP32 values (TF32 operand copy)
 };
 
 // FP32 SIMT product of the panel work: out = Lft (rows x K) * Rgt (K x cols),
@@ -318,13 +327,20 @@ __device__ __forceinline__ void panel_epilogue(const PanelArgs& pa, const SplitO
       // BF16 splits, 4 consecutive K entries packed into one 8-byte store
       for (int w = 0; w < 2; ++w) {
         const SplitOut& so = w == 0 ? s1 : s2;
-        if (!so.hi) continue;
+        if (!so.hi && !so.f32) continue;
         if (pa.col_split) {
           // split row = absolute column, K index = row (4 rows contiguous)
           for (int v = 0; v < nv; ++v) {
             const int aj = pa.abs_col0 + jb + v;
             if (aj < so.row0) continue;
             const size_t o = (size_t)(aj - so.row0) * so.ld + so.coloff + ib;
+            if (so.f32) {
+              if (nu == 4)
+                *reinterpret_cast<float4*>(so.f32 + o) = make_float4(r[0][v], r[1][v], r[2][v], r[3][v]);
+              else
+                for (int u = 0; u < nu; ++u) so.f32[o + u] = r[u][v];
+              continue;
+            }
             uint16_t hh[4], ll[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) split_bf16(u < nu ? r[u][v] : 0.f, &hh[u], &ll[u]);
@@ -344,6 +360,10 @@ __device__ __forceinline__ void panel_epilogue(const PanelArgs& pa, const SplitO
             const int ai = pa.abs_row0 + ib + u;
             if (ai < so.row0) continue;
             const size_t o = (size_t)(ai - so.row0) * so.ld + so.coloff + jb;
+            if (so.f32) {
+              for (int v = 0; v < nv; ++v) so.f32[o + v] = r[u][v];
+              continue;
+            }
             uint16_t hh[4], ll[4];
 #pragma unroll
             for (int v = 0; v < 4; ++v) split_bf16(v < nv ? r[u][v] : 0.f, &hh[v], &ll[v]);
@@ -483,7 +503,7 @@ static cudaError_t run_panel_small(const PanelArgs& pa, const SplitOut& s1, cons
   return cudaGetLastError();
 }
 
-// ------------------------------------------------------- tcgen05 BF16x3 GEMM
+// ------------------------------------------------------- tcgen05 GEMM (BF16x3 or TF32)
 // rows of padding after each split buffer and each padded test operand
 constexpr int kSplitPad = 128;
 
@@ -505,6 +525,15 @@ __device__ __forceinline__ void umma_bf16(uint32_t tmem, uint64_t a, uint64_t b,
       : "memory");
 }
 
+__device__ __forceinline__ void umma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                          uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, "
+      "%3, p;\n}\n" ::"r"(tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
 __device__ __forceinline__ void umma_commit(uint64_t* bar) {
   asm volatile(
       "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -521,14 +550,16 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int 
 }
 
 // ------------------------------------------------- persistent tcgen05 GEMM
-// C[crow0 + m, ccol0 + n] -= sum_k A[arow0 + m, k] B[brow0 + n, k], BF16x3, for the
+// C[crow0 + m, ccol0 + n] -= sum_k A[arow0 + m, k] B[brow0 + n, k], for the
 // large trailing updates. Persistent CTAs (one per SM) walk 128 x 256 output
 // tiles (M fastest, so the CTAs in flight share B tiles and stream A); warp
 // roles:
-//   warp 0     TMA producer: A hi/lo (128 x 32) and B hi/lo (256 x 32) per
-//              K step into a 3-stage ring of 48 KB (64-byte swizzle);
-//   warp 1     TMEM owner and MMA issuer: 6 tcgen05.mma (M 128, N 256, K 16)
-//              per K step into one of two 256-column FP32 accumulators;
+//   warp 0     TMA producer: per K step of 32, BF16x3: A hi/lo (128 x 32) and
+//              B hi/lo (256 x 32) with 64-byte swizzle; TF32: A and B in
+//              FP32 with 128-byte swizzle; a 3-stage ring of 48 KB either way;
+//   warp 1     TMEM owner and MMA issuer: per K step 6 kind::f16 tcgen05.mma
+//              (M 128, N 256, K 16) or 4 kind::tf32 (K 8) into one of two
+//              256-column FP32 accumulators;
 //   warps 2-5, 6-9  two epilogue groups, one per accumulator (even / odd
 //              tiles of the CTA): per 32-column chunk, the C chunk arrives by
 //              TMA into one of the group's two 16 KB buffers (128-byte
@@ -546,6 +577,13 @@ constexpr uint32_t kB3 = G3N * G3K * 2;                  // 16 KB
 constexpr uint32_t kStage3 = 2 * kA3 + 2 * kB3;          // 48 KB
 constexpr uint32_t kC3 = 128 * 32 * 4;                   // 16 KB C chunk
 constexpr int kG3Threads = 320;
+
+// K-major FP32 operand tile, 128-byte swizzle: rows of 128 B (32 TF32
+// values), 8-row atoms of 1024 B (stride byte offset), layout type 2.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
 
 __device__ __forceinline__ uint64_t smem_desc_sw64(uint32_t saddr) {
   // K-major operand tile, 64-byte swizzle: rows of 64 B, 8-row atoms of
@@ -571,11 +609,15 @@ __device__ __forceinline__ bool named_bar_epi_or(int g, bool v) {
   return r != 0;
 }
 
+// TF32: one kind::tf32 product per K step from FP32 operands (A through mAhi,
+// B through mBhi, both 128-byte swizzled boxes of 32 K; A's K coordinates
+// start at akoff); the stage holds A (16 KB) and B (32 KB), the same 48 KB.
+template <bool TF32>
 __global__ void __launch_bounds__(kG3Threads, 1)
-    k_gemm_bf16x3(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
-            const __grid_constant__ CUtensorMap mBhi, const __grid_constant__ CUtensorMap mBlo,
-            const __grid_constant__ CUtensorMap mC, int crow0, int ccol0, int arow0, int brow0, int M,
-            int Nc, int K, DevErr* err) {
+    k_gemm_tc(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
+              const __grid_constant__ CUtensorMap mBhi, const __grid_constant__ CUtensorMap mBlo,
+              const __grid_constant__ CUtensorMap mC, int crow0, int ccol0, int arow0, int brow0,
+              int akoff, int M, int Nc, int K, DevErr* err) {
   extern __shared__ __align__(1024) uint8_t g3sm[];
   const uint32_t base_s = smem_u32(g3sm);
   const uint32_t pad = (1024 - (base_s & 1023)) & 1023;
@@ -634,10 +676,15 @@ __global__ void __launch_bounds__(kG3Threads, 1)
           }
           const uint32_t st = smem_u32(sm + (size_t)stage * kStage3);
           mbar_arrive_expect_tx(&full[stage], kStage3);
-          tma_load_2d(st, &mAhi, kb * G3K, arow0 + m0, &full[stage]);
-          tma_load_2d(st + kA3, &mAlo, kb * G3K, arow0 + m0, &full[stage]);
-          tma_load_2d(st + 2 * kA3, &mBhi, kb * G3K, brow0 + n0, &full[stage]);
-          tma_load_2d(st + 2 * kA3 + kB3, &mBlo, kb * G3K, brow0 + n0, &full[stage]);
+          if (TF32) {
+            tma_load_2d(st, &mAhi, akoff + kb * G3K, arow0 + m0, &full[stage]);
+            tma_load_2d(st + 2 * kA3, &mBhi, kb * G3K, brow0 + n0, &full[stage]);
+          } else {
+            tma_load_2d(st, &mAhi, kb * G3K, arow0 + m0, &full[stage]);
+            tma_load_2d(st + kA3, &mAlo, kb * G3K, arow0 + m0, &full[stage]);
+            tma_load_2d(st + 2 * kA3, &mBhi, kb * G3K, brow0 + n0, &full[stage]);
+            tma_load_2d(st + 2 * kA3 + kB3, &mBlo, kb * G3K, brow0 + n0, &full[stage]);
+          }
           if (++stage == G3S) {
             stage = 0;
             phase ^= 1u;
@@ -648,8 +695,9 @@ __global__ void __launch_bounds__(kG3Threads, 1)
   } else if (warp == 1) {
     // ------------------------------------------------ MMA issuer
     if (lane == 0) {
-      // D f32, A/B bf16, K-major both, N = 256, M = 128
-      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(G3N >> 3) << 17) |
+      // D f32, A/B bf16 (format 1) or tf32 (format 2), K-major both, N = 256, M = 128
+      const uint32_t fmt = TF32 ? 2u : 1u;
+      const uint32_t idesc = (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(G3N >> 3) << 17) |
                              ((uint32_t)(G3M >> 4) << 24);
       int stage = 0;
       uint32_t phase = 0;
@@ -671,16 +719,28 @@ __global__ void __launch_bounds__(kG3Threads, 1)
           }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint32_t st = smem_u32(sm + (size_t)stage * kStage3);
-          const uint64_t dAh = smem_desc_sw64(st);
-          const uint64_t dAl = smem_desc_sw64(st + kA3);
-          const uint64_t dBh = smem_desc_sw64(st + 2 * kA3);
-          const uint64_t dBl = smem_desc_sw64(st + 2 * kA3 + kB3);
+          if (TF32) {
+            // A: 128 rows x 128 B at st, B: 256 rows x 128 B at st + 16 KB;
+            // K = 8 TF32 (32 bytes) per instruction
+            const uint64_t dA = smem_desc_sw128(st);
+            const uint64_t dB = smem_desc_sw128(st + 2 * kA3);
 #pragma unroll
-          for (int kk = 0; kk < G3K / 16; ++kk) {
-            const uint64_t adv = (uint64_t)(kk * 2);  // 32 bytes along K, in 16-byte units
-            umma_bf16(d, dAh + adv, dBh + adv, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
-            umma_bf16(d, dAh + adv, dBl + adv, idesc, 1u);
-            umma_bf16(d, dAl + adv, dBh + adv, idesc, 1u);
+            for (int kk = 0; kk < G3K / 8; ++kk) {
+              const uint64_t adv = (uint64_t)(kk * 2);
+              umma_tf32(d, dA + adv, dB + adv, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+            }
+          } else {
+            const uint64_t dAh = smem_desc_sw64(st);
+            const uint64_t dAl = smem_desc_sw64(st + kA3);
+            const uint64_t dBh = smem_desc_sw64(st + 2 * kA3);
+            const uint64_t dBl = smem_desc_sw64(st + 2 * kA3 + kB3);
+#pragma unroll
+            for (int kk = 0; kk < G3K / 16; ++kk) {
+              const uint64_t adv = (uint64_t)(kk * 2);  // 32 bytes along K, in 16-byte units
+              umma_bf16(d, dAh + adv, dBh + adv, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+              umma_bf16(d, dAh + adv, dBl + adv, idesc, 1u);
+              umma_bf16(d, dAl + adv, dBh + adv, idesc, 1u);
+            }
           }
           umma_commit(&empty[stage]);
           if (++stage == G3S) {
@@ -837,17 +897,15 @@ static bool encode_ops3(GemmMaps* mp, const uint16_t* ahi, const uint16_t* alo, 
   return one(&mp->Ahi, ahi, rows_a, G3M) && one(&mp->Alo, alo, rows_a, G3M) &&
          one(&mp->Bhi, bhi, rows_b, G3N) && one(&mp->Blo, blo, rows_b, G3N);
 }
-static bool encode_split3(GemmMaps* mp, const uint16_t* base, size_t rows, int kdim) {
-  const size_t plane = rows * (size_t)kdim;
-  return encode_ops3(mp, base, base + plane, rows, base + 2 * plane, base + 3 * plane, rows, kdim);
-}
 
 // FP32 matrix (rows x cols, leading dimension ld floats, ld % 4 == 0) seen by
-// TMA in 128 x 32 boxes with 128-byte swizzle.
-static bool encode_cmap(CUtensorMap* map, const float* base, int rows, int cols, int ld) {
+// TMA in box_rows x 32 boxes with 128-byte swizzle (the C operand, and the
+// TF32 A (128 rows) and B (256 rows) operands).
+static bool encode_cmap(CUtensorMap* map, const float* base, int rows, int cols, int ld,
+                        int box_rows = 128) {
   const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
   const cuuint64_t strides[1] = {(cuuint64_t)ld * 4};
-  const cuuint32_t box[2] = {32u, 128u};
+  const cuuint32_t box[2] = {32u, (cuuint32_t)box_rows};
   const cuuint32_t es[2] = {1, 1};
   PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
   if (!enc || (ld & 3)) return false;
@@ -865,9 +923,10 @@ static bool encode_cmap(CUtensorMap* map, const float* base, int rows, int cols,
 // neither read (zero fill) nor written (clipped), so tiles may overhang M / Nc
 // only where the region ends at the matrix edge.
 // spare_sms: SMs left free of the persistent CTAs (for concurrent panel work)
+template <bool TF32>
 static cudaError_t run_gemm(const GemmMaps& mp, const CUtensorMap& cmap, int crow0, int ccol0,
-                             int arow0, int brow0, int M, int Nc, int K, DevErr* err, cudaStream_t s,
-                             int spare_sms = 0) {
+                             int arow0, int brow0, int akoff, int M, int Nc, int K, DevErr* err,
+                             cudaStream_t s, int spare_sms = 0) {
   // per device: the shared-memory attribute is set and the SM count read on
   // the first launch there (both idempotent, so racing first launches agree)
   static std::atomic<int> sms_of[kMaxDev];
@@ -877,7 +936,7 @@ static cudaError_t run_gemm(const GemmMaps& mp, const CUtensorMap& cmap, int cro
   if (dev >= kMaxDev) return cudaErrorInvalidDevice;
   int sms = sms_of[dev].load(std::memory_order_acquire);
   if (sms == 0) {
-    e = cudaFuncSetAttribute(k_gemm_bf16x3, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    e = cudaFuncSetAttribute(k_gemm_tc<TF32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)gemm_smem());
     if (e != cudaSuccess) return e;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -886,8 +945,8 @@ static cudaError_t run_gemm(const GemmMaps& mp, const CUtensorMap& cmap, int cro
   }
   const int ntiles = ((M + G3M - 1) / G3M) * ((Nc + G3N - 1) / G3N);
   const int grid = std::min(ntiles, std::max(1, sms - spare_sms));
-  k_gemm_bf16x3<<<grid, kG3Threads, gemm_smem(), s>>>(mp.Ahi, mp.Alo, mp.Bhi, mp.Blo, cmap, crow0, ccol0,
-                                                 arow0, brow0, M, Nc, K, err);
+  k_gemm_tc<TF32><<<grid, kG3Threads, gemm_smem(), s>>>(mp.Ahi, mp.Alo, mp.Bhi, mp.Blo, cmap, crow0,
+                                                       ccol0, arow0, brow0, akoff, M, Nc, K, err);
   return cudaGetLastError();
 }
 
@@ -1056,9 +1115,10 @@ struct LuState {
   float* uinv = nullptr;
   float* linvT = nullptr;  // column-major copies
   float* uinvT = nullptr;
-  // outer (K = kNB2) L21hi, L21lo, U12Thi, U12Tlo, two sets: the trailing
-  // update of outer panel P reads set P % 2 while panel P + 1 writes the other
-  uint16_t* split2[2] = {nullptr, nullptr};
+  // the trailing update's TF32 operands: A = L21 in place in the LU buffer,
+  // B = U12^T (K = kNB2 per row) in one of two FP32 copies: the trailing
+  // update of outer panel P reads copy P % 2 while panel P + 1 writes the other
+  float* u12t[2] = {nullptr, nullptr};
   GemmMaps maps2[2];
   // look-ahead: column work and the next panel's columns of the trailing
   // update on a high-priority stream, the row panel one block behind it on a
@@ -1095,7 +1155,7 @@ void free_lu(wbem_context* h) {
   if (L.linvT) cudaFree(L.linvT);
   if (L.uinvT) cudaFree(L.uinvT);
   for (int b = 0; b < 2; ++b)
-    if (L.split2[b]) cudaFree(L.split2[b]);
+    if (L.u12t[b]) cudaFree(L.u12t[b]);
   if (L.s_panel) cudaStreamDestroy(L.s_panel);
   if (L.s_trail) cudaStreamDestroy(L.s_trail);
   if (L.s_row) cudaStreamDestroy(L.s_row);
@@ -1235,6 +1295,7 @@ int factor_mixed(wbem_context* h) {
   h->s32_state = 0;  // the factorisation overwrites the system matrix
   if (!encode_cmap(&L.cmap, h->d_lu, N, N, ld))
     return fail(h, WBEM_ERR_CUDA, "cuTensorMapEncodeTiled (LU buffer) failed");
+  const size_t rows_t = (size_t)N + kSplitPad;
   const int nblk = (N + kNB - 1) / kNB;
   const size_t rows = (size_t)N + kSplitPad;
   if (!L.linv) {
@@ -1242,19 +1303,14 @@ int factor_mixed(wbem_context* h) {
     WB_CHK(dev_alloc(h, &L.uinv, (size_t)nblk * kNB * kNB));
     WB_CHK(dev_alloc(h, &L.linvT, (size_t)nblk * kNB * kNB));
     WB_CHK(dev_alloc(h, &L.uinvT, (size_t)nblk * kNB * kNB));
-    WB_CHK(dev_alloc(h, &L.split2[0], (size_t)4 * rows * kNB2));
-    WB_CHK(dev_alloc(h, &L.split2[1], (size_t)4 * rows * kNB2));
+    WB_CHK(dev_alloc(h, &L.u12t[0], rows * kNB2));
+    WB_CHK(dev_alloc(h, &L.u12t[1], rows * kNB2));
     WB_CHK(dev_alloc(h, &L.w, (size_t)2 * N));
     WB_CHK(dev_alloc(h, &L.flags, (size_t)4 * nblk));
     WB_CU(cudaMemsetAsync(L.flags, 0, sizeof(unsigned) * 4 * nblk, h->stream));
     L.epoch = 0;
-    for (int b = 0; b < 2; ++b) {
-      uint16_t* b2 = L.split2[b];
-      WB_CU(cudaMemsetAsync(b2, 0, sizeof(uint16_t) * 4 * rows * kNB2, h->stream));
-      GemmMaps& m2 = L.maps2[b];
-      if (!encode_split3(&m2, b2, rows, kNB2))
-        return fail(h, WBEM_ERR_CUDA, "cuTensorMapEncodeTiled failed");
-    }
+    for (int b = 0; b < 2; ++b)
+      WB_CU(cudaMemsetAsync(L.u12t[b], 0, sizeof(float) * rows * kNB2, h->stream));
     int lo = 0, hi = 0;
     WB_CU(cudaDeviceGetStreamPriorityRange(&lo, &hi));
     WB_CU(cudaStreamCreateWithPriority(&L.s_panel, cudaStreamNonBlocking, hi));
@@ -1265,6 +1321,15 @@ int factor_mixed(wbem_context* h) {
     for (cudaEvent_t* e : {&L.ev_fork, &L.ev_row, &L.ev_trail, &L.ev_join, &L.ev_next_rows, &L.ev_blk,
                            &L.ev_u12, &L.ev_inrow, &L.ev_col2[0], &L.ev_col2[1]})
       WB_CU(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  }
+  // the trailing update's operand maps: A = the LU buffer (L21 in place),
+  // B = the U12^T copies (256-row boxes)
+  for (int b = 0; b < 2; ++b) {
+    GemmMaps& m2 = L.maps2[b];
+    m2.Ahi = m2.Alo = L.cmap;
+    if (!encode_cmap(&m2.Bhi, L.u12t[b], (int)rows_t, kNB2, kNB2, G3N))
+      return fail(h, WBEM_ERR_CUDA, "cuTensorMapEncodeTiled (U12 copy) failed");
+    m2.Blo = m2.Bhi;
   }
   EvTimer tm(h->stream);
   float* A = h->d_lu;
@@ -1313,7 +1378,7 @@ int factor_mixed(wbem_context* h) {
   auto pe = [&](ProfTimer& t, cudaStream_t s, double w) {
     if (prof) t.end(s, w);
   };
-  auto gemm_flop = [](int M, int Nc, int K) { return 3.0 * 2.0 * M * (double)Nc * K; };
+  auto gemm_flop = [](int M, int Nc, int K) { return 2.0 * M * (double)Nc * K; };
   WB_CU(cudaEventRecord(L.ev_fork, h->stream));
   WB_CU(cudaStreamWaitEvent(sp, L.ev_fork, 0));
   WB_CU(cudaStreamWaitEvent(st, L.ev_fork, 0));
@@ -1325,7 +1390,7 @@ int factor_mixed(wbem_context* h) {
   for (int p0 = 0; p0 < N; p0 += kNB2) {
     const int p1 = std::min(N, p0 + kNB2);
     const int buf = (p0 / kNB2) & 1;
-    uint16_t* b2 = L.split2[buf];
+    float* u12 = L.u12t[buf];
     const int n = N - p1;
     for (int k0 = p0; k0 < p1; k0 += kNB) {
       const int k = k0 / kNB, nb = std::min(kNB, N - k0), k1 = k0 + nb;
@@ -1362,7 +1427,7 @@ int factor_mixed(wbem_context* h) {
           WB_CU((run_panel_small<128, 64, false>(pu, none, none, su)));
           h->launches++;
         }
-        const SplitOut U12{b2 + 2 * rows * kNB2, b2 + 3 * rows * kNB2, p1, kNB2, k0 - p0};
+        const SplitOut U12{nullptr, nullptr, p1, kNB2, k0 - p0, u12};
         const PanelArgs pr{L.linvT + bo, kNB, A + (size_t)k0 * ld + p1, ld, A + (size_t)k0 * ld + p1,
                            ld, kNB, n, kNB, k0, p1, 0, 1};
         WB_CU((run_panel_small<128, 64, true>(pr, U12, none, su)));
@@ -1372,11 +1437,10 @@ int factor_mixed(wbem_context* h) {
       if (k1 >= N) break;
       const int m = N - k1;
       const int sh = std::min(kNB, m);  // the strip: rows of block k + 1
-      const SplitOut L21{b2, b2 + rows * kNB2, p1, kNB2, k0 - p0};
-      const SplitOut l21 = p1 < N ? L21 : none;
-      // column panel L_ik = A_ik inv(U_kk), in place, with the outer L21
-      // split: the strip on s_panel (after the s_col2 work of block k - 1,
-      // which updated these rows), the rows below on s_col2
+      const SplitOut l21 = none;  // the trailing update reads L21 in place
+      // column panel L_ik = A_ik inv(U_kk), in place: the strip on s_panel
+      // (after the s_col2 work of block k - 1, which updated these rows),
+      // the rows below on s_col2
       WB_CU(cudaStreamWaitEvent(sp, L.ev_col2[(k + 1) & 1], 0));
       const PanelArgs pc{A + (size_t)k1 * ld + k0, ld, L.uinv + bo, kNB, A + (size_t)k1 * ld + k0,
                          ld, sh, kNB, kNB, k1, k0, 0, 0};
@@ -1430,7 +1494,7 @@ int factor_mixed(wbem_context* h) {
     WB_CU(cudaStreamWaitEvent(sp, L.ev_join, 0));
     if (trail_pending) WB_CU(cudaStreamWaitEvent(sp, L.ev_trail, 0));
     pb(h->prof_gemm, sp);
-    WB_CU(run_gemm(L.maps2[buf], L.cmap, p1, p1, 0, 0, n, p2 - p1, p1 - p0, h->d_err, sp));
+    WB_CU(run_gemm<true>(L.maps2[buf], L.cmap, p1, p1, p1, 0, p0, n, p2 - p1, p1 - p0, h->d_err, sp));
     pe(h->prof_gemm, sp, gemm_flop(n, p2 - p1, p1 - p0));
     h->launches++;
     if (p2 < N) {
@@ -1442,13 +1506,13 @@ int factor_mixed(wbem_context* h) {
       // so that its row panel can start while the rows below are updated.
       const int spare = prof ? 0 : kLookaheadSMs;
       pb(h->prof_gemm, st);
-      WB_CU(run_gemm(L.maps2[buf], L.cmap, p1, p2, 0, p2 - p1, p2 - p1, N - p2, p1 - p0, h->d_err, st,
-                     spare));
+      WB_CU(run_gemm<true>(L.maps2[buf], L.cmap, p1, p2, p1, p2 - p1, p0, p2 - p1, N - p2, p1 - p0,
+                           h->d_err, st, spare));
       pe(h->prof_gemm, st, gemm_flop(p2 - p1, N - p2, p1 - p0));
       WB_CU(cudaEventRecord(L.ev_next_rows, st));
       pb(h->prof_gemm, st);
-      WB_CU(run_gemm(L.maps2[buf], L.cmap, p2, p2, p2 - p1, p2 - p1, N - p2, N - p2, p1 - p0, h->d_err,
-                     st, spare));
+      WB_CU(run_gemm<true>(L.maps2[buf], L.cmap, p2, p2, p2, p2 - p1, p0, N - p2, N - p2, p1 - p0,
+                           h->d_err, st, spare));
       pe(h->prof_gemm, st, gemm_flop(N - p2, N - p2, p1 - p0));
       WB_CU(cudaEventRecord(L.ev_trail, st));
       trail_pending = true;
@@ -1538,7 +1602,7 @@ extern "C" int wbem_test_gemm_bf16x3(int M, int Nc, int K, const float* dA, cons
   if (st == WBEM_OK && cudaMalloc(&err, sizeof(DevErr)) != cudaSuccess) st = WBEM_ERR_NOMEM;
   if (st == WBEM_OK) {
     cudaMemset(err, 0, sizeof(DevErr));
-    if (run_gemm(mp, cmap, 0, 0, 0, 0, M, Nc, K, err, 0) != cudaSuccess) st = WBEM_ERR_CUDA;
+    if (run_gemm<false>(mp, cmap, 0, 0, 0, 0, 0, M, Nc, K, err, 0) != cudaSuccess) st = WBEM_ERR_CUDA;
     if (cudaDeviceSynchronize() != cudaSuccess) st = WBEM_ERR_CUDA;
     DevErr de{};
     cudaMemcpy(&de, err, sizeof de, cudaMemcpyDeviceToHost);
@@ -1550,6 +1614,44 @@ extern "C" int wbem_test_gemm_bf16x3(int M, int Nc, int K, const float* dA, cons
   if (err) cudaFree(err);
   if (Cp) cudaFree(Cp);
   cudaFree(buf);
+  return st;
+}
+
+// C (M x Nc, ld Nc) -= A (M x K) B^T (Nc x K), FP32 A and B row-major on the
+// device, one TF32 tensor-core product (the factorisation's trailing update).
+extern "C" int wbem_test_gemm_tf32(int M, int Nc, int K, const float* dA, const float* dB, float* dC) {
+  using namespace wbem;
+  if (M < 1 || Nc < 1 || K < G3K || K % G3K) return WBEM_ERR_ARG;
+  GemmMaps mp;
+  int st = WBEM_OK;
+  if (!encode_cmap(&mp.Ahi, dA, M, K, K, G3M) || !encode_cmap(&mp.Bhi, dB, Nc, K, K, G3N))
+    st = WBEM_ERR_CUDA;
+  mp.Alo = mp.Ahi;
+  mp.Blo = mp.Bhi;
+  const int ldc = (Nc + 31) / 32 * 32;
+  float* Cp = nullptr;
+  if (st == WBEM_OK && cudaMalloc(&Cp, sizeof(float) * (size_t)M * ldc) != cudaSuccess) st = WBEM_ERR_NOMEM;
+  CUtensorMap cmap;
+  if (st == WBEM_OK) {
+    cudaMemcpy2D(Cp, sizeof(float) * ldc, dC, sizeof(float) * Nc, sizeof(float) * Nc, M,
+                 cudaMemcpyDeviceToDevice);
+    if (!encode_cmap(&cmap, Cp, M, Nc, ldc)) st = WBEM_ERR_CUDA;
+  }
+  DevErr* err = nullptr;
+  if (st == WBEM_OK && cudaMalloc(&err, sizeof(DevErr)) != cudaSuccess) st = WBEM_ERR_NOMEM;
+  if (st == WBEM_OK) {
+    cudaMemset(err, 0, sizeof(DevErr));
+    if (run_gemm<true>(mp, cmap, 0, 0, 0, 0, 0, M, Nc, K, err, 0) != cudaSuccess) st = WBEM_ERR_CUDA;
+    if (cudaDeviceSynchronize() != cudaSuccess) st = WBEM_ERR_CUDA;
+    DevErr de{};
+    cudaMemcpy(&de, err, sizeof de, cudaMemcpyDeviceToHost);
+    if (st == WBEM_OK && de.code) st = de.code;
+    if (st == WBEM_OK)
+      cudaMemcpy2D(dC, sizeof(float) * Nc, Cp, sizeof(float) * ldc, sizeof(float) * Nc, M,
+                   cudaMemcpyDeviceToDevice);
+  }
+  if (err) cudaFree(err);
+  if (Cp) cudaFree(Cp);
   return st;
 }
 
