@@ -275,10 +275,10 @@ NCU_TRAFFIC = {
 NCU_TILE_INSTR = 2949815885.0
 
 # DRAM bytes of a trailing-update launch over its algorithmic C traffic
-# (8 bytes per element of C, read and written once): 2.114 GB against
-# 2.010 GB for the largest launch at N = 16,384 (15,872 x 15,360, K = 512),
-# from one ncu capture; the operands add the rest.
-NCU_GEMM_TRAFFIC_RATIO = (1.218723e9 + 0.895937e9) / (8.0 * 15872 * 15360)
+# (8 bytes per element of C, read and written once): 2.205 GB against
+# 1.887 GB for the largest launch at N = 16,384 (15,360 x 15,360, K = 512,
+# TF32), from one ncu capture; the operands add the rest.
+NCU_GEMM_TRAFFIC_RATIO = (1.309495e9 + 0.895142e9) / (8.0 * 15360 * 15360)
 
 
 def ncu_traffic(kernel, n):
