@@ -122,3 +122,39 @@ def test_fma_sphere_beyond_dense_size():
     e = rel2(dphi, dpdn)
     print(f"sphere N={m.n_dofs}: dphi vs exact {e:.2e}, {f.stats()['iterations']} iterations")
     assert e < 1e-3
+
+
+def test_fma_refuses_a_mesh_too_coarse_for_two_levels():
+    """The 866-node cube-sphere: its panels are too large for the leaf margin
+    of a two-level tree, so the FMA assembly reports an argument error."""
+    from helpers import sphere
+    m, ptr, idx, p, dpdn = sphere(12)
+    f = _fma(m, ptr, idx)
+    with pytest.raises(WBEMError):
+        f.assemble_system()
+
+
+def test_fma_sphere_and_moved_nodes():
+    """A 9,602-node cube-sphere against the dense FP64 operator, and the same
+    handle after its nodes move (update_nodes rebuilds the tree and the
+    close pairs) against a new handle on the moved mesh."""
+    from helpers import sphere
+    m, ptr, idx, p, dpdn = sphere(40)
+    v = np.random.default_rng(11).normal(size=m.n_dofs)
+    g = BEMProblem(m.X, m.cells, m.dirichlet, ptr, idx, precision=PREC_FP64)
+    g.assemble_system()
+    f = _fma(m, ptr, idx, 8)
+    f.assemble_system()
+    e1 = rel2(f.vmult(v), g.vmult(v))
+    # a smooth displacement of every node (double nodes move together)
+    X2 = m.X * (1.0 + 0.05 * np.sin(3.0 * m.X[:, :1]))
+    f.update_nodes(X2)
+    f.assemble_system()
+    fresh = BEMProblem(X2, m.cells, m.dirichlet, ptr, idx, method=METHOD_FMA, fma_order=8)
+    fresh.assemble_system()
+    assert np.array_equal(f.vmult(v), fresh.vmult(v))
+    g2 = BEMProblem(X2, m.cells, m.dirichlet, ptr, idx, precision=PREC_FP64)
+    g2.assemble_system()
+    e2 = rel2(f.vmult(v), g2.vmult(v))
+    print(f"sphere n=40 order 8: vmult {e1:.2e}, moved {e2:.2e}")
+    assert e1 <= 2e-5 and e2 <= 2e-5

@@ -609,18 +609,20 @@ __global__ void k_fma_l2l(const int* __restrict__ parent, const int* __restrict_
 }
 
 // The product's evaluation at the collocation points, one CTA per chunk of
-// up to kEvalTargets rows of one leaf, each thread holding two rows and
-// kEvalLanes threads sharing a pair: the far field (L2P of the leaf's local
-// expansion), the near field evaluated on the fly over the points of the
-// neighbour leaves (FP32 in leaf-local coordinates, two rows per packed
-// FP32x2 instruction, points staged in shared memory with each value
-// duplicated for the packed operands; FP64 sum of FP32 partials) and the
-// close-pair corrections (FP64). The lanes of a pair split every sum the same
+// up to kEvalTargets rows of one leaf, each thread holding four rows (two
+// packed pairs) and kEvalLanes threads sharing a quad: the far field (L2P of
+// the leaf's local expansion), the near field evaluated on the fly over the
+// points of the neighbour leaves (FP32 in coordinates local to this leaf's
+// centre, two rows per packed FP32x2 instruction, points staged in shared
+// memory with each value duplicated for the packed operands and the next
+// chunk loaded into registers meanwhile; FP64 sum of FP32 partials) and the
+// close-pair corrections (FP64). The lanes of a quad split every sum the same
 // way on every call and are combined by shuffles: the product is
 // deterministic.
-constexpr int kEvalTargets = 32;
+constexpr int kEvalTargets = 64;
 constexpr int kEvalLanes = 8;
-constexpr int kEvalThreads = kEvalTargets / 2 * kEvalLanes;
+constexpr int kEvalRows = 4;  // rows per thread
+constexpr int kEvalThreads = kEvalTargets / kEvalRows * kEvalLanes;
 constexpr int kEvalChunk = 256;
 // Packed FP32x2 arithmetic on 64-bit registers (two rows per instruction).
 __device__ __forceinline__ unsigned long long pk2(float lo, float hi) {
@@ -663,46 +665,46 @@ k_fma_eval(const int2* __restrict__ items, const int* __restrict__ tptr, const i
   __shared__ unsigned long long sD[kEvalChunk];
   __shared__ float sL[kFmaMaxOrder * kFmaMaxOrder * kFmaMaxOrder];
   __shared__ float sw[kEvalTargets][3][kFmaMaxOrder];
+  __shared__ int snp[28];
+  __shared__ float soff[27][3];
   const int2 it = items[blockIdx.x];
   const int leaf = it.x, t0 = it.y;
   const int nt = min(kEvalTargets, tptr[leaf + 1] - t0);
-  const int tid = threadIdx.x, pr = tid / kEvalLanes, lane = tid % kEvalLanes;
-  const int r0 = 2 * pr, r1 = 2 * pr + 1;
-  const bool v0 = r0 < nt, v1 = r1 < nt;
-  const int i0 = v0 ? tidx[t0 + r0] : -1, i1 = v1 ? tidx[t0 + r1] : -1;
-  const float4 x0 = v0 ? xloc[i0] : make_float4(0.f, 0.f, 0.f, 0.f);
-  const float4 x1 = v1 ? xloc[i1] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const int tid = threadIdx.x, qd = tid / kEvalLanes, lane = tid % kEvalLanes;
+  int ix[kEvalRows];
+  float4 xr[kEvalRows];
+#pragma unroll
+  for (int h = 0; h < kEvalRows; ++h) {
+    const int r = kEvalRows * qd + h;
+    ix[h] = r < nt ? tidx[t0 + r] : -1;
+    xr[h] = ix[h] >= 0 ? xloc[ix[h]] : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
   const int n = c_fma.n, n3 = c_fma.n3, nq = c_fma.nq;
-  double acc0 = 0.0, acc1 = 0.0;
+  double acc[kEvalRows] = {0.0, 0.0, 0.0, 0.0};
   if (Lx) {
     for (int k = tid; k < n3; k += kEvalThreads) sL[k] = Lx[(size_t)leaf * n3 + k];
-    if (lane < 6) {
-      const float4& xr = lane < 3 ? x0 : x1;
-      const int dir = lane % 3;
-      const float ih = (float)(1.0 / half);
-      cheb_weights(c_fma, (dir == 0 ? xr.x : dir == 1 ? xr.y : xr.z) * ih, sw[lane < 3 ? r0 : r1][dir],
-                   nullptr);
+    // the quad's 3 x kEvalRows (row, axis) weight sets over its kEvalLanes lanes
+    for (int x = lane; x < 3 * kEvalRows; x += kEvalLanes) {
+      const int hh = x / 3, dir = x % 3;
+      float u = 0.f;  // the coordinate by unrolled selection (no indexed register array)
+#pragma unroll
+      for (int h = 0; h < kEvalRows; ++h)
+        if (h == hh) u = dir == 0 ? xr[h].x : dir == 1 ? xr[h].y : xr[h].z;
+      cheb_weights(c_fma, u * (float)(1.0 / half), sw[kEvalRows * qd + hh][dir], nullptr);
     }
     __syncthreads();
-    float f0 = 0.f, f1 = 0.f;
-    for (int uv = lane; uv < n * n; uv += kEvalLanes) {
-      const float s0 = sw[r0][0][uv / n] * sw[r0][1][uv % n];
-      const float s1 = sw[r1][0][uv / n] * sw[r1][1][uv % n];
-      const float* Lr = sL + uv * n;
-      for (int w = 0; w < n; ++w) {
-        f0 = fmaf(s0 * sw[r0][2][w], Lr[w], f0);
-        f1 = fmaf(s1 * sw[r1][2][w], Lr[w], f1);
+#pragma unroll
+    for (int h = 0; h < kEvalRows; ++h) {
+      const int r = kEvalRows * qd + h;
+      float f = 0.f;
+      for (int uv = lane; uv < n * n; uv += kEvalLanes) {
+        const float sxy = sw[r][0][uv / n] * sw[r][1][uv % n];
+        const float* Lr = sL + uv * n;
+        for (int w = 0; w < n; ++w) f = fmaf(sxy * sw[r][2][w], Lr[w], f);
       }
+      acc[h] = (double)f;
     }
-    acc0 = (double)f0;
-    acc1 = (double)f1;
   }
-  // the neighbour leaves' points as one sequence (prefix counts and centre
-  // offsets in shared memory), staged relative to this leaf's centre in
-  // chunks of kEvalChunk, the next chunk loaded into registers while the
-  // current one is evaluated
-  __shared__ int snp[28];
-  __shared__ float soff[27][3];
   const int ne = nb_ptr[leaf + 1] - nb_ptr[leaf];
   if (tid == 0) {
     int c = 0;
@@ -716,7 +718,10 @@ k_fma_eval(const int2* __restrict__ items, const int* __restrict__ tptr, const i
   }
   __syncthreads();
   const int total = snp[ne];
-  const unsigned long long cx = pk2(-x0.x, -x1.x), cy = pk2(-x0.y, -x1.y), cz = pk2(-x0.z, -x1.z);
+  const unsigned long long cx0 = pk2(-xr[0].x, -xr[1].x), cy0 = pk2(-xr[0].y, -xr[1].y),
+                           cz0 = pk2(-xr[0].z, -xr[1].z);
+  const unsigned long long cx1 = pk2(-xr[2].x, -xr[3].x), cy1 = pk2(-xr[2].y, -xr[3].y),
+                           cz1 = pk2(-xr[2].z, -xr[3].z);
   // point g of the sequence: leaf-local position plus its leaf's offset
   auto fetch = [&](int g, float4& P, float4& Q) {
     int e = 0;
@@ -728,15 +733,18 @@ k_fma_eval(const int2* __restrict__ items, const int* __restrict__ tptr, const i
     P.y += soff[e][1];
     P.z += soff[e][2];
   };
-  float4 nP[2], nQ[2];
-  for (int u = 0; u < 2; ++u)
+  constexpr int kPer = kEvalChunk / kEvalThreads;  // staged points per thread
+  float4 nP[kPer], nQ[kPer];
+#pragma unroll
+  for (int u = 0; u < kPer; ++u)
     if (u * kEvalThreads + tid < total) fetch(u * kEvalThreads + tid, nP[u], nQ[u]);
-  unsigned long long pa = 0ull, pb = 0ull, pc = 0ull, pd = 0ull;
+  unsigned long long pa0 = 0ull, pa1 = 0ull;
   int nchunk = 0;
   for (int base = 0; base < total; base += kEvalChunk) {
     const int cnt = min(kEvalChunk, total - base);
     __syncthreads();
-    for (int u = 0; u < 2; ++u) {
+#pragma unroll
+    for (int u = 0; u < kPer; ++u) {
       const int j = u * kEvalThreads + tid;
       if (j < cnt) {
         const float4 P = nP[u], Q = nQ[u];
@@ -747,41 +755,50 @@ k_fma_eval(const int2* __restrict__ items, const int* __restrict__ tptr, const i
       }
     }
     __syncthreads();
-    for (int u = 0; u < 2; ++u) {
+#pragma unroll
+    for (int u = 0; u < kPer; ++u) {
       const int g = base + kEvalChunk + u * kEvalThreads + tid;
       if (g < total) fetch(g, nP[u], nQ[u]);
     }
-    // q / r - (R . m) / r^3 = (q - (R . m) / r^2) / r for two rows
-    auto term = [&](int k, unsigned long long& part) {
+    // q / r - (R . m) / r^3 = (q - (R . m) / r^2) / r for two row pairs
+    auto term = [&](int k, unsigned long long& p0, unsigned long long& p1) {
       const ulonglong2 A = sA[k], B = sB[k], C = sC[k];
       const unsigned long long D = sD[k];
-      const unsigned long long rx = add2(A.x, cx), ry = add2(A.y, cy), rz = add2(B.x, cz);
-      const unsigned long long r2 = fma2(rx, rx, fma2(ry, ry, mul2(rz, rz)));
-      float q0, q1;
-      upk2(r2, q0, q1);
-      const unsigned long long ri = pk2(rsqrt_approx(q0), rsqrt_approx(q1));
-      const unsigned long long dn = fma2(rx, C.x, fma2(ry, C.y, mul2(rz, D)));
-      part = fma2(fma2(dn, mul2(ri, ri), B.y), ri, part);
+      {
+        const unsigned long long rx = add2(A.x, cx0), ry = add2(A.y, cy0), rz = add2(B.x, cz0);
+        const unsigned long long r2 = fma2(rx, rx, fma2(ry, ry, mul2(rz, rz)));
+        float q0, q1;
+        upk2(r2, q0, q1);
+        const unsigned long long ri = pk2(rsqrt_approx(q0), rsqrt_approx(q1));
+        const unsigned long long dn = fma2(rx, C.x, fma2(ry, C.y, mul2(rz, D)));
+        p0 = fma2(fma2(dn, mul2(ri, ri), B.y), ri, p0);
+      }
+      {
+        const unsigned long long rx = add2(A.x, cx1), ry = add2(A.y, cy1), rz = add2(B.x, cz1);
+        const unsigned long long r2 = fma2(rx, rx, fma2(ry, ry, mul2(rz, rz)));
+        float q0, q1;
+        upk2(r2, q0, q1);
+        const unsigned long long ri = pk2(rsqrt_approx(q0), rsqrt_approx(q1));
+        const unsigned long long dn = fma2(rx, C.x, fma2(ry, C.y, mul2(rz, D)));
+        p1 = fma2(fma2(dn, mul2(ri, ri), B.y), ri, p1);
+      }
     };
-    int k = lane;
-    for (; k + 3 * kEvalLanes < cnt; k += 4 * kEvalLanes) {
-      term(k, pa);
-      term(k + kEvalLanes, pb);
-      term(k + 2 * kEvalLanes, pc);
-      term(k + 3 * kEvalLanes, pd);
-    }
-    for (; k < cnt; k += kEvalLanes) term(k, pa);
+    for (int k = lane; k < cnt; k += kEvalLanes) term(k, pa0, pa1);
     // FP64 sum of FP32 partials every eight chunks
     if ((++nchunk & 7) == 0 || base + kEvalChunk >= total) {
-      float pl, ph;
-      upk2(add2(add2(pa, pb), add2(pc, pd)), pl, ph);
-      acc0 += (double)pl;
-      acc1 += (double)ph;
-      pa = pb = pc = pd = 0ull;
+      float l0, h0, l1, h1;
+      upk2(pa0, l0, h0);
+      upk2(pa1, l1, h1);
+      acc[0] += (double)l0;
+      acc[1] += (double)h0;
+      acc[2] += (double)l1;
+      acc[3] += (double)h1;
+      pa0 = pa1 = 0ull;
     }
   }
-  for (int h = 0; h < 2; ++h) {
-    const int i = h ? i1 : i0;
+#pragma unroll
+  for (int h = 0; h < kEvalRows; ++h) {
+    const int i = ix[h];
     if (i < 0) continue;
     double c = 0.0;
     for (int k = close_ptr[i] + lane; k < close_ptr[i + 1]; k += kEvalLanes) {
@@ -790,17 +807,16 @@ k_fma_eval(const int2* __restrict__ items, const int* __restrict__ tptr, const i
       c += v[0] * a[d.x] + v[1] * a[d.y] + v[2] * a[d.z] + v[3] * a[d.w] + v[4] * b[d.x] +
            v[5] * b[d.y] + v[6] * b[d.z] + v[7] * b[d.w];
     }
-    if (h) acc1 += c; else acc0 += c;
+    acc[h] += c;
   }
 #pragma unroll
-  for (int o = 1; o < kEvalLanes; o <<= 1) {
-    acc0 += __shfl_xor_sync(0xffffffffu, acc0, o);
-    acc1 += __shfl_xor_sync(0xffffffffu, acc1, o);
-  }
-  if (lane == 0) {
-    if (v0) y[i0] = acc0;
-    if (v1) y[i1] = acc1;
-  }
+  for (int h = 0; h < kEvalRows; ++h)
+#pragma unroll
+    for (int o = 1; o < kEvalLanes; o <<= 1) acc[h] += __shfl_xor_sync(0xffffffffu, acc[h], o);
+  if (lane == 0)
+#pragma unroll
+    for (int h = 0; h < kEvalRows; ++h)
+      if (ix[h] >= 0) y[ix[h]] = acc[h];
 }
 
 // Inputs of one FMA product: mode 0 (vmult): a = x o, b = -x s;
