@@ -142,7 +142,8 @@ __global__ void k_fma_close(int N, const int* __restrict__ tgt_leaf, const int* 
                             const int* __restrict__ leaf_pan, const double* __restrict__ X,
                             const double* __restrict__ geo, const int* __restrict__ sptr,
                             const int* __restrict__ scell, const int* __restrict__ ptr,
-                            int* __restrict__ cnt, int* __restrict__ prow, int* __restrict__ ppan) {
+                            int* __restrict__ cnt, int* __restrict__ prow, int* __restrict__ ppan,
+                            uint8_t* __restrict__ psing) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
   const double xi = X[3 * (size_t)i], yi = X[3 * (size_t)i + 1], zi = X[3 * (size_t)i + 2];
@@ -155,12 +156,14 @@ __global__ void k_fma_close(int N, const int* __restrict__ tgt_leaf, const int* 
       const int cell = leaf_pan[k];
       const double* g = geo + 4 * (size_t)cell;
       const double dx = g[0] - xi, dy = g[1] - yi, dz = g[2] - zi;
-      bool close = dx * dx + dy * dy + dz * dz < 12.0 * g[3] * g[3];
-      for (int m = sptr[i]; m < sptr[i + 1] && !close; ++m) close = scell[m] == cell;
+      bool sing = false;  // a double-node partner of the row is a vertex of the panel
+      for (int m = sptr[i]; m < sptr[i + 1] && !sing; ++m) sing = scell[m] == cell;
+      const bool close = sing || dx * dx + dy * dy + dz * dz < 12.0 * g[3] * g[3];
       if (!close) continue;
       if (ptr) {
         prow[base + c] = i;
         ppan[base + c] = cell;
+        psing[base + c] = sing ? 1 : 0;
       }
       ++c;
     }
@@ -191,10 +194,13 @@ __device__ __forceinline__ void fma_pair_approx(const float4* __restrict__ P,
   }
 }
 
-// Corrections of the close pairs, one thread per pair: the dense assembly's
-// FP64 value (4 N and 4 D entries) minus the product's FP32 value, stored as
-// val[8 * pair + 0..3] = N, [4..7] = D.
-__global__ void k_fma_close_val(long long npairs, const int* __restrict__ pair_row,
+// Corrections of the close pairs, one thread per pair of a list (the
+// regular and the singular pairs are launched as separate lists, so that the
+// warps do not diverge between the 16-point and the vertex-singular rules):
+// the dense assembly's FP64 value (4 N and 4 D entries) minus the product's
+// FP32 value, stored as val[8 * pair + 0..3] = N, [4..7] = D.
+__global__ void k_fma_close_val(long long npairs, const int* __restrict__ plist,
+                                const int* __restrict__ pair_row,
                                 const int* __restrict__ pair_pan, const double* __restrict__ X,
                                 const int* __restrict__ dnset, const int4* __restrict__ cell_dofs,
                                 const double* __restrict__ rec, const int* __restrict__ tgt_leaf,
@@ -202,8 +208,9 @@ __global__ void k_fma_close_val(long long npairs, const int* __restrict__ pair_r
                                 const double* __restrict__ cen, const float4* __restrict__ xloc,
                                 const float4* __restrict__ ppos, double* __restrict__ val,
                                 const QuadTables* __restrict__ qt, const __grid_constant__ FmaConst c_fma) {
-  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= npairs) return;
+  const long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (li >= npairs) return;
+  const int k = plist[li];
   const int row = pair_row[k], cell = pair_pan[k];
   const double xi = X[3 * (size_t)row], yi = X[3 * (size_t)row + 1], zi = X[3 * (size_t)row + 2];
   int set[kMaxSet];
@@ -489,16 +496,15 @@ __global__ void k_fma_m2l_ops(int n, double e2, float* __restrict__ K) {
   const int oi = blockIdx.x, a = blockIdx.y, n3 = n * n * n;
   const int dx = oi / 49 - 3, dy = (oi / 7) % 7 - 3, dz = oi % 7 - 3;
   const bool used = max(abs(dx), max(abs(dy), abs(dz))) >= 2;
-  const double pi = 3.14159265358979323846;
-  const double ta0 = cos((2 * (a / (n * n)) + 1) * pi / (2.0 * n));
-  const double ta1 = cos((2 * ((a / n) % n) + 1) * pi / (2.0 * n));
-  const double ta2 = cos((2 * (a % n) + 1) * pi / (2.0 * n));
+  __shared__ double tn[kFmaMaxOrder];  // Chebyshev nodes, scaled by e / 2
+  if (threadIdx.x < n)
+    tn[threadIdx.x] = e2 * cos((2 * threadIdx.x + 1) * 3.14159265358979323846 / (2.0 * n));
+  __syncthreads();
+  const double ax = dx + tn[a / (n * n)], ay = dy + tn[(a / n) % n], az = dz + tn[a % n];
   for (int m = threadIdx.x; m < n3; m += blockDim.x) {
     float v = 0.f;
     if (used) {
-      const double rx = dx + e2 * (ta0 - cos((2 * (m / (n * n)) + 1) * pi / (2.0 * n)));
-      const double ry = dy + e2 * (ta1 - cos((2 * ((m / n) % n) + 1) * pi / (2.0 * n)));
-      const double rz = dz + e2 * (ta2 - cos((2 * (m % n) + 1) * pi / (2.0 * n)));
+      const double rx = ax - tn[m / (n * n)], ry = ay - tn[(m / n) % n], rz = az - tn[m % n];
       v = (float)(1.0 / sqrt(rx * rx + ry * ry + rz * rz));
     }
     K[((size_t)oi * n3 + a) * n3 + m] = v;
@@ -948,6 +954,8 @@ struct FmaState {
   int* d_pair_pan = nullptr;
   double* d_close_val = nullptr; // FP64 corrections, 8 per close pair
   size_t npairs = 0;
+  int* d_plist = nullptr;        // close pairs, the regular ones first, then the singular ones
+  size_t n_regular = 0;
   double* d_blocks = nullptr;    // near-field diagonal blocks of the system
   double* d_a = nullptr;         // product inputs (N each)
   double* d_b = nullptr;
@@ -1283,7 +1291,7 @@ static int fma_build(wbem_context* h, FmaState* F, const QuadTables& qt) {
     WB_CHK(dev_alloc(h, &d_cnt, (size_t)N));
     k_fma_close<<<(N + 127) / 128, 128, 0, h->stream>>>(
         N, F->d_tgt_leaf, F->d_nb_ptr, F->d_nb, F->d_leaf_pptr, F->d_leaf_pan, h->d_X, F->d_geo,
-        h->d_sptr, h->d_scell, nullptr, d_cnt, nullptr, nullptr);
+        h->d_sptr, h->d_scell, nullptr, d_cnt, nullptr, nullptr, nullptr);
     std::vector<int> cnt(N), cptr(N + 1, 0);
     WB_CU(cudaMemcpyAsync(cnt.data(), d_cnt, sizeof(int) * N, cudaMemcpyDeviceToHost, h->stream));
     WB_CU(cudaStreamSynchronize(h->stream));
@@ -1298,11 +1306,27 @@ static int fma_build(wbem_context* h, FmaState* F, const QuadTables& qt) {
     WB_CHK(fma_alloc(h, F, &F->d_pair_row, std::max<size_t>(1, F->npairs)));
     WB_CHK(fma_alloc(h, F, &F->d_pair_pan, std::max<size_t>(1, F->npairs)));
     WB_CHK(fma_alloc(h, F, &F->d_close_val, 8 * std::max<size_t>(1, F->npairs)));
+    uint8_t* d_sing = nullptr;
+    guard.slots.push_back((void**)&d_sing);
+    WB_CHK(dev_alloc(h, &d_sing, std::max<size_t>(1, F->npairs)));
     k_fma_close<<<(N + 127) / 128, 128, 0, h->stream>>>(
         N, F->d_tgt_leaf, F->d_nb_ptr, F->d_nb, F->d_leaf_pptr, F->d_leaf_pan, h->d_X, F->d_geo,
-        h->d_sptr, h->d_scell, F->d_close_ptr, nullptr, F->d_pair_row, F->d_pair_pan);
+        h->d_sptr, h->d_scell, F->d_close_ptr, nullptr, F->d_pair_row, F->d_pair_pan, d_sing);
     WB_CU(cudaGetLastError());
+    // the pair lists of the correction kernel: regular pairs, then singular
+    std::vector<uint8_t> sing(F->npairs);
+    if (F->npairs)
+      WB_CU(cudaMemcpyAsync(sing.data(), d_sing, F->npairs, cudaMemcpyDeviceToHost, h->stream));
     WB_CU(cudaStreamSynchronize(h->stream));
+    std::vector<int> plist;
+    plist.reserve(F->npairs);
+    for (size_t k = 0; k < F->npairs; ++k)
+      if (!sing[k]) plist.push_back((int)k);
+    F->n_regular = plist.size();
+    for (size_t k = 0; k < F->npairs; ++k)
+      if (sing[k]) plist.push_back((int)k);
+    if (plist.empty()) plist.push_back(0);
+    WB_CHK(fma_upload(h, F, &F->d_plist, plist));
   }
   const int n = F->n;
   std::vector<double> t(n);
@@ -1455,18 +1479,22 @@ int assemble_fma(wbem_context* h, const QuadTables& qt) {
   const int npts = C * nq;
   k_fma_points<<<(npts + 255) / 256, 256, 0, h->stream>>>(npts, nq, F->d_leaf_pan, F->d_pos_leaf,
                                                           h->d_rec, F->lev[F->L].d_cen, F->d_ppos);
-  if (F->npairs > 0) {
-    const unsigned grid = (unsigned)((F->npairs + 127) / 128);
-    k_fma_close_val<<<grid, 128, 0, h->stream>>>(
-        (long long)F->npairs, F->d_pair_row, F->d_pair_pan, h->d_X, h->d_dnset, h->d_cell_dofs,
-        h->d_rec, F->d_tgt_leaf, F->d_pan_pos, F->d_pos_leaf, F->lev[F->L].d_cen, F->d_xloc,
-        F->d_ppos, F->d_close_val, F->d_qt, F->cst);
+  // the regular pairs, then the singular ones (each list warp-uniform)
+  for (int part = 0; part < 2; ++part) {
+    const size_t off = part ? F->n_regular : 0;
+    const size_t cnt = part ? F->npairs - F->n_regular : F->n_regular;
+    if (cnt == 0) continue;
+    k_fma_close_val<<<(unsigned)((cnt + 127) / 128), 128, 0, h->stream>>>(
+        (long long)cnt, F->d_plist + off, F->d_pair_row, F->d_pair_pan, h->d_X, h->d_dnset,
+        h->d_cell_dofs, h->d_rec, F->d_tgt_leaf, F->d_pan_pos, F->d_pos_leaf, F->lev[F->L].d_cen,
+        F->d_xloc, F->d_ppos, F->d_close_val, F->d_qt, F->cst);
     WB_CU(cudaGetLastError());
+    h->launches++;
   }
   h->stats.t_singular_ms = tm.ms();
   WB_CHK(fma_apply(h, 2, nullptr, h->d_alpha));
   h->stats.t_alpha_ms = tm.ms();
-  h->launches += 3;
+  h->launches += 2;
   return check_device_error(h, "assemble (FMA)");
 }
 
