@@ -14,12 +14,14 @@
 //     panel diameters: the regular rule in FP64), so that those pairs carry
 //     the dense assembly's values;
 //   - the far field through Chebyshev-interpolation expansions of order n
-//     per direction (n^3 coefficients per box; the kernel-independent form of
-//     the multipole / local expansions): P2M at the leaves (charges
-//     JxW phi_j b_j and dipoles n JxW phi_j a_j of the quadrature points),
+//     per direction (the kernel-independent form of the multipole / local
+//     expansions): P2M at the leaves into four sets of n^3 coefficients per
+//     box (the charges JxW phi_j b_j and the three components of the dipoles
+//     n JxW phi_j a_j of the quadrature points, each interpolated by value),
 //     M2M up the tree and L2L down it as three 1-D passes, M2L over the
 //     interaction lists as FP32 GEMMs with the operators between Chebyshev
-//     nodes precomputed per box offset, and L2P at the collocation points.
+//     nodes (1/r and its gradient for the dipoles) precomputed per box
+//     offset, and L2P at the collocation points.
 //     Boxes are interpolated over their cube enlarged by kFmaExpand, so that a
 //     panel attached by its centre lies inside its leaf's box.
 // Every sum runs in a fixed order: the product is deterministic.
@@ -361,16 +363,21 @@ __global__ void k_fma_strengths(int npts, const int* __restrict__ leaf_pan,
 
 // P2M in work items of up to kP2MPanels panels of one leaf (so that large
 // leaves spread over several CTAs), kP2MGroups groups of kP2MGroupThreads
-// threads per item. Thread (i, j) < n^2 of a group holds the n coefficients
-// (i, j, 0..n-1) of the item's expansion over the group's chunks of
-// kP2MChunk points (chunks g, g + G, ...), whose 1-D interpolation weights
-// and derivatives the group computes first (one thread per point and axis).
-// The groups' sums are added in a fixed order into the item's partial
-// expansion; k_fma_p2m_sum adds a leaf's items in order.
+// threads per item. A box's multipole expansion has four sets of n^3
+// coefficients: the charges and the three dipole components, each
+// interpolated by value (the dipoles' kernel derivative is applied exactly
+// in the M2L, which keeps the double layer as accurate as the single
+// layer). Thread (i, j) < n^2 of a group holds coefficients (i, j, 0..n-1)
+// of the four sets over the group's chunks of kP2MChunk points (chunks g,
+// g + G, ...), whose 1-D interpolation weights the group computes first (one
+// thread per point and axis). The groups' sums are added in a fixed order
+// into the item's partial expansion; k_fma_p2m_sum adds a leaf's items in
+// order.
 constexpr int kP2MPanels = 32;
 constexpr int kP2MChunk = 32;
 constexpr int kP2MGroups = 4;
 constexpr int kP2MGroupThreads = 64;
+constexpr int kMpSets = 4;  // charge, dipole x, y, z
 template <int NO>
 __global__ void __launch_bounds__(kP2MGroups* kP2MGroupThreads)
 k_fma_p2m(const int4* __restrict__ items, const float4* __restrict__ ppos,
@@ -380,53 +387,56 @@ k_fma_p2m(const int4* __restrict__ items, const float4* __restrict__ ppos,
   const int nq = c_fma.nq, g = threadIdx.y, tid = threadIdx.x;
   __shared__ float4 sg[kP2MGroups][kP2MChunk];
   __shared__ __align__(16) float Sw[kP2MGroups][kP2MChunk][3][kFmaMaxOrder];
-  __shared__ __align__(16) float dSw[kP2MGroups][kP2MChunk][3][kFmaMaxOrder];
-  __shared__ float red[kP2MGroups][n3];
+  __shared__ float red[kP2MGroups][kMpSets * n3];
   const int4 it = items[blockIdx.x];
   const int p0 = it.y * nq, p1 = it.z * nq;
   const int nchunk = (p1 - p0 + kP2MChunk - 1) / kP2MChunk;
   const int rounds = (nchunk + kP2MGroups - 1) / kP2MGroups;
   const int mi = tid / NO, mj = tid % NO;
   const float ih = (float)(1.0 / half);
-  float acc[NO];
+  float acc[kMpSets][NO];
 #pragma unroll
-  for (int k = 0; k < NO; ++k) acc[k] = 0.f;
+  for (int q = 0; q < kMpSets; ++q)
+#pragma unroll
+    for (int k = 0; k < NO; ++k) acc[q][k] = 0.f;
   for (int r = 0; r < rounds; ++r) {
     const int base = p0 + (r * kP2MGroups + g) * kP2MChunk;
     const int cnt = max(0, min(kP2MChunk, p1 - base));
     for (int x = tid; x < 3 * cnt; x += kP2MGroupThreads) {
       const int pt = x / 3, dir = x % 3;
       const float4 y = ppos[base + pt];
-      cheb_weights(c_fma, (dir == 0 ? y.x : dir == 1 ? y.y : y.z) * ih, Sw[g][pt][dir], dSw[g][pt][dir]);
+      cheb_weights(c_fma, (dir == 0 ? y.x : dir == 1 ? y.y : y.z) * ih, Sw[g][pt][dir], nullptr);
       if (dir == 0) sg[g][pt] = pstr[base + pt];
     }
     __syncthreads();
     if (tid < NO * NO) {
       for (int p = 0; p < cnt; ++p) {
         const float4 q4 = sg[g][p];
-        const float sx = Sw[g][p][0][mi], dsx = dSw[g][p][0][mi];
-        const float sy = Sw[g][p][1][mj], dsy = dSw[g][p][1][mj];
-        const float sxy = sx * sy;
-        // charge and the x, y dipoles multiply S_z; the z dipole dS_z
-        const float A = fmaf(fmaf(q4.y, dsx * sy, q4.z * (sx * dsy)), ih, q4.x * sxy);
-        const float Bz = q4.w * sxy * ih;
+        const float sxy = Sw[g][p][0][mi] * Sw[g][p][1][mj];
+        const float c0 = q4.x * sxy, c1 = q4.y * sxy, c2 = q4.z * sxy, c3 = q4.w * sxy;
         const float* sz = Sw[g][p][2];
-        const float* dsz = dSw[g][p][2];
 #pragma unroll
-        for (int k = 0; k < NO; ++k) acc[k] = fmaf(A, sz[k], fmaf(Bz, dsz[k], acc[k]));
+        for (int k = 0; k < NO; ++k) {
+          acc[0][k] = fmaf(c0, sz[k], acc[0][k]);
+          acc[1][k] = fmaf(c1, sz[k], acc[1][k]);
+          acc[2][k] = fmaf(c2, sz[k], acc[2][k]);
+          acc[3][k] = fmaf(c3, sz[k], acc[3][k]);
+        }
       }
     }
     __syncthreads();
   }
   if (tid < NO * NO)
 #pragma unroll
-    for (int k = 0; k < NO; ++k) red[g][tid * NO + k] = acc[k];
+    for (int q = 0; q < kMpSets; ++q)
+#pragma unroll
+      for (int k = 0; k < NO; ++k) red[g][q * n3 + tid * NO + k] = acc[q][k];
   __syncthreads();
-  for (int m = g * kP2MGroupThreads + tid; m < n3; m += kP2MGroups * kP2MGroupThreads) {
+  for (int m = g * kP2MGroupThreads + tid; m < kMpSets * n3; m += kP2MGroups * kP2MGroupThreads) {
     float v = red[0][m];
 #pragma unroll
     for (int k = 1; k < kP2MGroups; ++k) v += red[k][m];
-    Wpart[(size_t)blockIdx.x * n3 + m] = v;
+    Wpart[(size_t)blockIdx.x * kMpSets * n3 + m] = v;
   }
 }
 
@@ -445,7 +455,8 @@ __global__ void k_fma_p2m_sum(const int* __restrict__ iptr, const float* __restr
 // S1[h][c][P] (the parent's weight of node P at child node c, h = the
 // child's half along the axis): the n^3 x n^3 translation is their tensor
 // product, applied as three passes of n^4 multiply-adds.
-// M2M: one CTA per parent box; W_P[P] = sum_children sum_c T[c][P] W_c[c].
+// M2M: one CTA per parent box; W_P[P] = sum_children sum_c T[c][P] W_c[c],
+// for each of the kMpSets coefficient sets (stride kMpSets n^3 per box).
 __global__ void k_fma_m2m(const int* __restrict__ child_ptr, const int* __restrict__ child,
                           const int* __restrict__ child_oct, const float* __restrict__ Wc,
                           float* __restrict__ Wp, const __grid_constant__ FmaConst c_fma) {
@@ -453,47 +464,52 @@ __global__ void k_fma_m2m(const int* __restrict__ child_ptr, const int* __restri
   __shared__ float w[kFmaMaxOrder * kFmaMaxOrder * kFmaMaxOrder];
   __shared__ float t1[kFmaMaxOrder * kFmaMaxOrder * kFmaMaxOrder];
   const int i0 = tid / (n * n), i1 = (tid / n) % n, i2 = tid % n;
-  float acc = 0.f;
-  for (int e = child_ptr[p]; e < child_ptr[p + 1]; ++e) {
-    const int o = child_oct[e];
-    const float(*Sx)[kFmaMaxOrder] = c_fma.S1[o >> 2];
-    const float(*Sy)[kFmaMaxOrder] = c_fma.S1[(o >> 1) & 1];
-    const float(*Sz)[kFmaMaxOrder] = c_fma.S1[o & 1];
-    __syncthreads();
-    if (tid < n3) w[tid] = Wc[(size_t)child[e] * n3 + tid];
-    __syncthreads();
-    if (tid < n3) {  // t1[cx][cy][Pz]
-      float v = 0.f;
-      for (int c = 0; c < n; ++c) v = fmaf(Sz[c][i2], w[(i0 * n + i1) * n + c], v);
-      t1[tid] = v;
+  for (int set = 0; set < kMpSets; ++set) {
+    float acc = 0.f;
+    for (int e = child_ptr[p]; e < child_ptr[p + 1]; ++e) {
+      const int o = child_oct[e];
+      const float(*Sx)[kFmaMaxOrder] = c_fma.S1[o >> 2];
+      const float(*Sy)[kFmaMaxOrder] = c_fma.S1[(o >> 1) & 1];
+      const float(*Sz)[kFmaMaxOrder] = c_fma.S1[o & 1];
+      __syncthreads();
+      if (tid < n3) w[tid] = Wc[((size_t)child[e] * kMpSets + set) * n3 + tid];
+      __syncthreads();
+      if (tid < n3) {  // t1[cx][cy][Pz]
+        float v = 0.f;
+        for (int c = 0; c < n; ++c) v = fmaf(Sz[c][i2], w[(i0 * n + i1) * n + c], v);
+        t1[tid] = v;
+      }
+      __syncthreads();
+      if (tid < n3) {  // w[cx][Py][Pz]
+        float v = 0.f;
+        for (int c = 0; c < n; ++c) v = fmaf(Sy[c][i1], t1[(i0 * n + c) * n + i2], v);
+        w[tid] = v;
+      }
+      __syncthreads();
+      if (tid < n3)  // W_P[Px][Py][Pz]
+        for (int c = 0; c < n; ++c) acc = fmaf(Sx[c][i0], w[(c * n + i1) * n + i2], acc);
     }
-    __syncthreads();
-    if (tid < n3) {  // w[cx][Py][Pz]
-      float v = 0.f;
-      for (int c = 0; c < n; ++c) v = fmaf(Sy[c][i1], t1[(i0 * n + c) * n + i2], v);
-      w[tid] = v;
-    }
-    __syncthreads();
-    if (tid < n3)  // W_P[Px][Py][Pz]
-      for (int c = 0; c < n; ++c) acc = fmaf(Sx[c][i0], w[(c * n + i1) * n + i2], acc);
+    if (tid < n3) Wp[((size_t)p * kMpSets + set) * n3 + tid] = acc;
   }
-  if (tid < n3) Wp[(size_t)p * n3 + tid] = acc;
 }
 
 // M2L. The kernel 1/r is homogeneous and the interpolation cubes scale with
 // the boxes, so the operator between the nodes of two boxes of one level
 // depends only on their offset d = key_target - key_source in [-3, 3]^3 (in
-// box units): K[d][a][m] = 1 / |d + (e / 2)(t_a - t_m)|, divided by the box
-// size of the level. The operators are computed once per order and the M2L of
-// a product runs as FP32 GEMMs, one per (level, offset) group of up to
-// kM2LPairs (target, source) pairs: C[a][p] = sum_m K[d][a][m] W_{s_p}[m],
-// written per pair; k_fma_m2l_sum adds a box's pairs in its list order.
+// box units). With R = d + (e / 2)(t_a - t_m) it has four blocks of n^3
+// columns, one per multipole set: 1 / |R| for the charges and R_k / |R|^3
+// (the gradient of 1/|x - y| in y) for the dipole components, divided by the
+// box size of the level and by its square. The operators are computed once
+// per order and the M2L of a product runs as FP32 GEMMs (K = 4 n^3), one per
+// (level, offset) group of up to kM2LPairs (target, source) pairs:
+// C[a][p] = sum_m' K[d][a][m'] W_{s_p}[m'], written per pair; k_fma_m2l_sum
+// adds a box's pairs in its list order.
 constexpr int kM2LOffsets = 343;  // ((dx + 3) 7 + dy + 3) 7 + dz + 3
 constexpr int kM2LPairs = 64;
 constexpr int kM2LRows = 128;
 constexpr int kM2LK = 32;
 __global__ void k_fma_m2l_ops(int n, double e2, float* __restrict__ K) {
-  const int oi = blockIdx.x, a = blockIdx.y, n3 = n * n * n;
+  const int oi = blockIdx.x, a = blockIdx.y, n3 = n * n * n, kd = kMpSets * n3;
   const int dx = oi / 49 - 3, dy = (oi / 7) % 7 - 3, dz = oi % 7 - 3;
   const bool used = max(abs(dx), max(abs(dy), abs(dz))) >= 2;
   __shared__ double tn[kFmaMaxOrder];  // Chebyshev nodes, scaled by e / 2
@@ -501,19 +517,28 @@ __global__ void k_fma_m2l_ops(int n, double e2, float* __restrict__ K) {
     tn[threadIdx.x] = e2 * cos((2 * threadIdx.x + 1) * 3.14159265358979323846 / (2.0 * n));
   __syncthreads();
   const double ax = dx + tn[a / (n * n)], ay = dy + tn[(a / n) % n], az = dz + tn[a % n];
+  float* row = K + ((size_t)oi * n3 + a) * kd;
   for (int m = threadIdx.x; m < n3; m += blockDim.x) {
-    float v = 0.f;
+    float k0 = 0.f, k1 = 0.f, k2 = 0.f, k3 = 0.f;
     if (used) {
       const double rx = ax - tn[m / (n * n)], ry = ay - tn[(m / n) % n], rz = az - tn[m % n];
-      v = (float)(1.0 / sqrt(rx * rx + ry * ry + rz * rz));
+      const double ri = 1.0 / sqrt(rx * rx + ry * ry + rz * rz), ri3 = ri * ri * ri;
+      k0 = (float)ri;
+      k1 = (float)(rx * ri3);
+      k2 = (float)(ry * ri3);
+      k3 = (float)(rz * ri3);
     }
-    K[((size_t)oi * n3 + a) * n3 + m] = v;
+    row[m] = k0;
+    row[n3 + m] = k1;
+    row[2 * n3 + m] = k2;
+    row[3 * n3 + m] = k3;
   }
 }
 
 // items: (offset, first entry, entries, level); entries: source box and
 // output row (global over the levels); one CTA of 256 threads per item, each
-// thread an 8 x 4 block of C per pass of kM2LRows target nodes.
+// thread an 8 x 4 block of C per pass of kM2LRows target nodes. The dipole
+// columns (m' >= n3) carry one more factor 1 / s, applied when staged.
 __global__ void __launch_bounds__(256)
 k_fma_m2l_gemm(const int4* __restrict__ items, const int* __restrict__ ent_src,
                const int* __restrict__ ent_out, const float* __restrict__ K,
@@ -521,10 +546,11 @@ k_fma_m2l_gemm(const int4* __restrict__ items, const int* __restrict__ ent_src,
                float* __restrict__ part, int n3) {
   __shared__ __align__(16) float Ks[kM2LK][kM2LRows + 4];
   __shared__ __align__(16) float Ws[kM2LK][kM2LPairs + 4];
+  const int kd = kMpSets * n3;
   const int4 it = items[blockIdx.x];
   const int begin = it.y, cnt = it.z;
   const float sc = lvl_scale[it.w];
-  const float* Ko = K + (size_t)it.x * n3 * n3;
+  const float* Ko = K + (size_t)it.x * n3 * kd;
   const int tid = threadIdx.x, ty = tid / 16, tx = tid % 16;
   for (int a0 = 0; a0 < n3; a0 += kM2LRows) {
     float acc[8][4];
@@ -532,15 +558,16 @@ k_fma_m2l_gemm(const int4* __restrict__ items, const int* __restrict__ ent_src,
     for (int i = 0; i < 8; ++i)
 #pragma unroll
       for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
-    for (int m0 = 0; m0 < n3; m0 += kM2LK) {
+    for (int m0 = 0; m0 < kd; m0 += kM2LK) {
       __syncthreads();
       for (int x = tid; x < kM2LRows * kM2LK; x += 256) {
         const int r = x / kM2LK, c = x % kM2LK, a = a0 + r, m = m0 + c;
-        Ks[c][r] = (a < n3 && m < n3) ? Ko[(size_t)a * n3 + m] : 0.f;
+        Ks[c][r] = (a < n3 && m < kd) ? Ko[(size_t)a * kd + m] : 0.f;
       }
       for (int x = tid; x < kM2LPairs * kM2LK; x += 256) {
         const int p = x / kM2LK, c = x % kM2LK, m = m0 + c;
-        Ws[c][p] = (p < cnt && m < n3) ? Wall[(size_t)ent_src[begin + p] * n3 + m] : 0.f;
+        float w = (p < cnt && m < kd) ? Wall[(size_t)ent_src[begin + p] * kd + m] : 0.f;
+        Ws[c][p] = m >= n3 ? w * sc : w;
       }
       __syncthreads();
 #pragma unroll 8
@@ -937,7 +964,7 @@ struct FmaState {
   int total_boxes = 0;
   float* d_Wall = nullptr;       // multipole / local coefficients of every box, levels
   float* d_Lall = nullptr;       // concatenated (the levels' d_W / d_L point into these)
-  float* d_K = nullptr;          // M2L operators per box offset (343 x n^3 x n^3)
+  float* d_K = nullptr;          // M2L operators per box offset (343 x n^3 x 4 n^3)
   int4* d_m2l_items = nullptr;   // (offset, first entry, entries, level)
   int n_m2l_items = 0;
   int* d_ent_src = nullptr;      // M2L entries: global source box
@@ -1086,7 +1113,7 @@ static int fma_build(wbem_context* h, FmaState* F, const QuadTables& qt) {
   std::vector<int> box_off(L + 2, 0);
   for (int l = 0; l <= L; ++l) box_off[l + 1] = box_off[l] + (int)keys[l].size();
   F->total_boxes = box_off[L + 1];
-  WB_CHK(fma_alloc(h, F, &F->d_Wall, (size_t)F->total_boxes * n3));
+  WB_CHK(fma_alloc(h, F, &F->d_Wall, (size_t)F->total_boxes * kMpSets * n3));
   WB_CHK(fma_alloc(h, F, &F->d_Lall, (size_t)F->total_boxes * n3));
   // M2L entries of all levels: (level, offset index, source box, list position)
   struct M2LEnt {
@@ -1108,7 +1135,7 @@ static int fma_build(wbem_context* h, FmaState* F, const QuadTables& qt) {
       cen[3 * (size_t)b + 2] = lo[2] + (keys[l][b].z + 0.5) * s;
     }
     WB_CHK(fma_upload(h, F, &V.d_cen, cen));
-    V.d_W = F->d_Wall + (size_t)box_off[l] * n3;
+    V.d_W = F->d_Wall + (size_t)box_off[l] * kMpSets * n3;
     V.d_L = F->d_Lall + (size_t)box_off[l] * n3;
     if (l > 0) {
       V.parent.resize(V.nbox);
@@ -1195,7 +1222,7 @@ static int fma_build(wbem_context* h, FmaState* F, const QuadTables& qt) {
     WB_CHK(fma_upload(h, F, &F->d_gptr, gptr));
     WB_CHK(fma_upload(h, F, &F->d_lvl_scale, lvl_scale));
     WB_CHK(fma_alloc(h, F, &F->d_part, (size_t)std::max(1, il_off) * n3));
-    WB_CHK(fma_alloc(h, F, &F->d_K, (size_t)kM2LOffsets * n3 * n3));
+    WB_CHK(fma_alloc(h, F, &F->d_K, (size_t)kM2LOffsets * n3 * kMpSets * n3));
     k_fma_m2l_ops<<<dim3(kM2LOffsets, n3), 128, 0, h->stream>>>(F->n, kFmaExpand / 2, F->d_K);
     WB_CU(cudaGetLastError());
   }
@@ -1258,7 +1285,8 @@ static int fma_build(wbem_context* h, FmaState* F, const QuadTables& qt) {
   if (p2m_items.empty()) p2m_items.push_back(make_int4(0, 0, 0, 0));
   WB_CHK(fma_upload(h, F, &F->d_p2m_items, p2m_items));
   WB_CHK(fma_upload(h, F, &F->d_p2m_iptr, p2m_iptr));
-  WB_CHK(fma_alloc(h, F, &F->d_Wpart, (size_t)std::max(1, F->n_p2m_items) * F->n * F->n * F->n));
+  WB_CHK(fma_alloc(h, F, &F->d_Wpart,
+                   (size_t)std::max(1, F->n_p2m_items) * kMpSets * F->n * F->n * F->n));
   std::vector<float4> xloc(N);
   for (int i = 0; i < N; ++i) {
     const Key3& k = keys[L][tl[i]];
@@ -1392,7 +1420,7 @@ static int fma_product(wbem_context* h, const double* a, const double* b, double
       default: k_fma_p2m<8><<<ni, pb, 0, s>>>(F->d_p2m_items, F->d_ppos, F->d_pstr, LV.half, F->d_Wpart, F->cst); break;
     }
   }
-  k_fma_p2m_sum<<<LV.nbox, nt, 0, s>>>(F->d_p2m_iptr, F->d_Wpart, LV.d_W, n3);
+  k_fma_p2m_sum<<<LV.nbox, 256, 0, s>>>(F->d_p2m_iptr, F->d_Wpart, LV.d_W, kMpSets * n3);
   for (int l = L; l > kFmaMinLevel; --l) {
     FmaLevel& P = F->lev[l - 1];
     k_fma_m2m<<<P.nbox, nt, 0, s>>>(P.d_child_ptr, P.d_child, P.d_child_oct, F->lev[l].d_W, P.d_W,
