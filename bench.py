@@ -540,9 +540,9 @@ def run_gpu(args, rank, world, local):
                             "traffic_per_launch": NCU_GEMM_TRAFFIC_RATIO * 8.0 * mn / kprof["gemm_launches"],
                             "traffic_source": "8 bytes per C element per launch (the average launch) times "
                                               "the DRAM / C-traffic ratio of one ncu capture at N = 16384"})
-        # the far-field assembly: bound by FP32 arithmetic (the survey's
-        # convention: 36 flop per regular kernel evaluation, 16 evaluations per
-        # (row, panel) pair); its HBM figure is reported beside it
+        # the far-field assembly: bound by FP32 arithmetic (work counted as 36
+        # flop per regular kernel evaluation, 16 evaluations per (row, panel)
+        # pair); its HBM figure is reported beside it
         tile_s = kprof["tile_ms"] / 1e3
         tile = {"kernel": "k_tile_mixed", "ms": kprof["tile_ms"], "launches": 1}
         t_flop = 36.0 * 16.0 * N * m.n_cells
