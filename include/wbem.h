@@ -84,11 +84,13 @@ typedef struct {
   int inner_digits;              /* GMRES_IR: inner relative tolerance 10^-inner_digits, 0 -> 4 */
   int method;                    /* WBEM_METHOD_* ("Solution method"), DIRECT by default */
   int fma_order;                 /* FMA: Chebyshev points per direction of the expansions, 3..8
-                                    (6 by default; the far field's error falls about 4x per step) */
+                                    (6 by default; the far field's error falls about 7x per step) */
   int reserved[4];
 } wbem_options;
 
 typedef struct {
+  /* FMA: t_assemble_ms is the octree and list build (host wall time), 0 when
+     the last build still holds; t_singular_ms the close-pair corrections */
   double t_geometry_ms, t_assemble_ms, t_singular_ms, t_alpha_ms, t_system_ms;
   double t_factor_ms, t_solve_ms, t_adjoint_ms;
   int iterations;           /* GMRES iterations of the last solve */

@@ -32,10 +32,11 @@
 // near-field matrix, source/bem_fma.cc:1099-1196).
 #include <cuda_runtime.h>
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <string>
-#include <unordered_map>
+#include <cstdint>
 #include <vector>
 #include "context.h"
 #include "host_util.h"
@@ -136,22 +137,29 @@ __global__ void k_fma_panel_geo(int C, const double* __restrict__ X,
   geo[4 * (size_t)c + 3] = dia;
 }
 
-// Close pairs of each row: count (ptr == nullptr) or list them from ptr[i]
-// on (row, panel), in the order of the row's neighbour leaves and their
-// panels. One thread per row.
-__global__ void k_fma_close(int N, const int* __restrict__ tgt_leaf, const int* __restrict__ nb_ptr,
+// Close pairs of each row, in the order of the row's neighbour leaves and
+// their panels; one thread per row, the rows taken in leaf order (tidx) so
+// that a warp walks the same neighbour panels. Count pass (ptr == nullptr):
+// cnt[i] = (pairs, singular pairs). List pass: the pairs as (row, panel) from ptr[i]
+// on, and their indices in the correction list, the regular pairs from
+// lptr[i].x on and the singular ones from lptr[i].y on.
+__global__ void k_fma_close(int N, const int* __restrict__ tidx, const int* __restrict__ tgt_leaf,
+                            const int* __restrict__ nb_ptr,
                             const int* __restrict__ nb, const int* __restrict__ leaf_pptr,
                             const int* __restrict__ leaf_pan, const double* __restrict__ X,
                             const double* __restrict__ geo, const int* __restrict__ sptr,
                             const int* __restrict__ scell, const int* __restrict__ ptr,
-                            int* __restrict__ cnt, int* __restrict__ prow, int* __restrict__ ppan,
-                            uint8_t* __restrict__ psing) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= N) return;
+                            const int2* __restrict__ lptr, int2* __restrict__ cnt,
+                            int* __restrict__ prow, int* __restrict__ ppan,
+                            int* __restrict__ plist) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= N) return;
+  const int i = tidx[j];
   const double xi = X[3 * (size_t)i], yi = X[3 * (size_t)i + 1], zi = X[3 * (size_t)i + 2];
   const int t = tgt_leaf[i];
   const int base = ptr ? ptr[i] : 0;
-  int c = 0;
+  const int2 lp = ptr ? lptr[i] : make_int2(0, 0);
+  int c = 0, ns = 0;
   for (int e = nb_ptr[t]; e < nb_ptr[t + 1]; ++e) {
     const int s = nb[e];
     for (int k = leaf_pptr[s]; k < leaf_pptr[s + 1]; ++k) {
@@ -165,12 +173,14 @@ __global__ void k_fma_close(int N, const int* __restrict__ tgt_leaf, const int* 
       if (ptr) {
         prow[base + c] = i;
         ppan[base + c] = cell;
-        psing[base + c] = sing ? 1 : 0;
+        if (sing) plist[lp.y + ns] = base + c;
+        else plist[lp.x + c - ns] = base + c;
       }
+      ns += sing ? 1 : 0;
       ++c;
     }
   }
-  if (!ptr) cnt[i] = c;
+  if (!ptr) cnt[i] = make_int2(c, ns);
 }
 
 // The FP32 value the product computes for one (row, panel) pair, as the 4 N
@@ -898,10 +908,85 @@ struct Key3 {
   int x, y, z;
   bool operator==(const Key3& o) const { return x == o.x && y == o.y && z == o.z; }
 };
-struct Key3Hash {
-  size_t operator()(const Key3& k) const {
-    return ((size_t)(unsigned)k.x * 73856093u) ^ ((size_t)(unsigned)k.y * 19349663u) ^
-           ((size_t)(unsigned)k.z * 83492791u);
+// Morton (Z-order) code of a box key with coordinates below 2^21: bit 3j+2
+// holds bit j of x, 3j+1 of y, 3j of z. A parent's code is its child's code
+// shifted right by 3, so one sort of the leaf codes orders every level, and
+// the children of a box are consecutive in that order, by octant 4x+2y+z.
+inline uint64_t spread3(uint32_t v) {
+  uint64_t x = v & 0x1fffffu;
+  x = (x | x << 32) & 0x001f00000000ffffull;
+  x = (x | x << 16) & 0x001f0000ff0000ffull;
+  x = (x | x << 8) & 0x100f00f00f00f00full;
+  x = (x | x << 4) & 0x10c30c30c30c30c3ull;
+  x = (x | x << 2) & 0x1249249249249249ull;
+  return x;
+}
+inline uint32_t compact3(uint64_t x) {
+  x &= 0x1249249249249249ull;
+  x = (x | x >> 2) & 0x10c30c30c30c30c3ull;
+  x = (x | x >> 4) & 0x100f00f00f00f00full;
+  x = (x | x >> 8) & 0x001f0000ff0000ffull;
+  x = (x | x >> 16) & 0x001f00000000ffffull;
+  x = (x | x >> 32) & 0x1fffffull;
+  return (uint32_t)x;
+}
+inline uint64_t morton(const Key3& k) {
+  return spread3((uint32_t)k.x) << 2 | spread3((uint32_t)k.y) << 1 | spread3((uint32_t)k.z);
+}
+inline Key3 unmorton(uint64_t m) {
+  return Key3{(int)compact3(m >> 2), (int)compact3(m >> 1), (int)compact3(m)};
+}
+
+// Stable LSD radix sort of (code, id) pairs on the low `bits` bits of the
+// code, 11 bits per pass.
+void radix_sort_pairs(std::vector<uint64_t>& key, std::vector<int>& id, int bits) {
+  const size_t n = key.size();
+  std::vector<uint64_t> k2(n);
+  std::vector<int> i2(n);
+  std::vector<size_t> cnt(2049);
+  for (int sh = 0; sh < bits; sh += 11) {
+    std::fill(cnt.begin(), cnt.end(), 0);
+    for (size_t e = 0; e < n; ++e) cnt[((key[e] >> sh) & 2047) + 1]++;
+    for (int d = 0; d < 2048; ++d) cnt[d + 1] += cnt[d];
+    for (size_t e = 0; e < n; ++e) {
+      const size_t p = cnt[(key[e] >> sh) & 2047]++;
+      k2[p] = key[e];
+      i2[p] = id[e];
+    }
+    key.swap(k2);
+    id.swap(i2);
+  }
+}
+
+// Box index of a Morton code at one level: an open-addressing table with
+// linear probing (codes are below 2^63, all ones marks an empty slot).
+struct BoxIndex {
+  std::vector<uint64_t> key;
+  std::vector<int> val;
+  size_t mask = 0;
+  static size_t slot(uint64_t c) { return (size_t)((c * 0x9e3779b97f4a7c15ull) >> 20); }
+  void build(const std::vector<uint64_t>& codes) {
+    size_t cap = 16;
+    while (cap < 2 * codes.size()) cap <<= 1;
+    key.assign(cap, ~0ull);
+    val.assign(cap, -1);
+    mask = cap - 1;
+    for (int b = 0; b < (int)codes.size(); ++b) {
+      size_t s = slot(codes[b]) & mask;
+      while (key[s] != ~0ull) s = (s + 1) & mask;
+      key[s] = codes[b];
+      val[s] = b;
+    }
+  }
+  // index of the box with key k at a level of side 2^l boxes, -1 if absent
+  int find(const Key3& k, int l) const {
+    const int m = 1 << l;
+    if (k.x < 0 || k.y < 0 || k.z < 0 || k.x >= m || k.y >= m || k.z >= m) return -1;
+    const uint64_t c = morton(k);
+    for (size_t s = slot(c) & mask;; s = (s + 1) & mask) {
+      if (key[s] == c) return val[s];
+      if (key[s] == ~0ull) return -1;
+    }
   }
 };
 
@@ -1059,51 +1144,73 @@ static int fma_build(wbem_context* h, FmaState* F, const QuadTables& qt) {
   // leaf level: the deepest level whose interpolation margin covers every
   // panel ((expand - 1) s / 2 >= panel radius) and whose leaves hold about
   // 16 or more collocation points on average
-  int L = kFmaMinLevel;
+  // (the margin only shrinks with depth: lm is the deepest level it allows)
+  int lm = kFmaMinLevel - 1;
   for (int l = kFmaMinLevel; l <= 20; ++l) {
-    const double s = S / (double)(1 << l);
-    if ((kFmaExpand - 1.0) * s / 2.0 < rho) break;
-    std::unordered_map<Key3, int, Key3Hash> cnt;
-    for (int i = 0; i < N; ++i)
-      cnt[{(int)std::floor((Xi[3 * (size_t)i] - lo[0]) / s), (int)std::floor((Xi[3 * (size_t)i + 1] - lo[1]) / s),
-           (int)std::floor((Xi[3 * (size_t)i + 2] - lo[2]) / s)}]++;
-    if ((double)N / cnt.size() < 16.0 && l > kFmaMinLevel) break;
-    L = l;
+    if ((kFmaExpand - 1.0) * (S / (double)(1 << l)) / 2.0 < rho) break;
+    lm = l;
   }
-  if ((kFmaExpand - 1.0) * (S / (double)(1 << L)) / 2.0 < rho)
+  if (lm < kFmaMinLevel)
     return fail(h, WBEM_ERR_ARG, "FMA: panels too large for an octree of at least two levels");
-  F->L = L;
-  const double sL = S / (double)(1 << L);
-  auto keyL = [&](const double* p) {
-    Key3 k{(int)std::floor((p[0] - lo[0]) / sL), (int)std::floor((p[1] - lo[1]) / sL),
-           (int)std::floor((p[2] - lo[2]) / sL)};
-    const int mx = (1 << L) - 1;
+  // Morton codes at level lm of the rows (ids 0..N-1) and panel centres
+  // (ids N + c); the key of a level l <= lm is the code shifted by 3 (lm - l)
+  // (floor(q 2^l) = floor(floor(q 2^lm) / 2^(lm - l)))
+  const double sm = S / (double)(1 << lm);
+  auto code_lm = [&](const double* p) {
+    const int mx = (1 << lm) - 1;
+    Key3 k{(int)std::floor((p[0] - lo[0]) / sm), (int)std::floor((p[1] - lo[1]) / sm),
+           (int)std::floor((p[2] - lo[2]) / sm)};
     k.x = std::min(std::max(k.x, 0), mx);
     k.y = std::min(std::max(k.y, 0), mx);
     k.z = std::min(std::max(k.z, 0), mx);
-    return k;
+    return morton(k);
   };
-  // boxes per level (sorted keys), leaf = level L
-  std::vector<std::vector<Key3>> keys(L + 1);
-  std::vector<std::unordered_map<Key3, int, Key3Hash>> index(L + 1);
-  std::vector<Key3> tk(N), pk(C);
-  for (int i = 0; i < N; ++i) tk[i] = keyL(&Xi[3 * (size_t)i]);
-  for (int c = 0; c < C; ++c) pk[c] = keyL(&pc[3 * (size_t)c]);
+  std::vector<uint64_t> code(N + (size_t)C);
+  std::vector<int> cid(N + (size_t)C);
+  for (int i = 0; i < N; ++i) {
+    code[i] = code_lm(&Xi[3 * (size_t)i]);
+    cid[i] = i;
+  }
+  for (int c = 0; c < C; ++c) {
+    code[N + (size_t)c] = code_lm(&pc[3 * (size_t)c]);
+    cid[N + (size_t)c] = N + c;
+  }
+  int L = kFmaMinLevel;
   {
-    std::vector<Key3> all(tk);
-    all.insert(all.end(), pk.begin(), pk.end());
-    auto less = [](const Key3& a, const Key3& b) {
-      return a.x != b.x ? a.x < b.x : a.y != b.y ? a.y < b.y : a.z < b.z;
-    };
-    for (int l = L; l >= 0; --l) {
-      std::vector<Key3> v;
-      v.reserve(all.size());
-      for (const Key3& k : all) v.push_back({k.x >> (L - l), k.y >> (L - l), k.z >> (L - l)});
-      std::sort(v.begin(), v.end(), less);
-      v.erase(std::unique(v.begin(), v.end()), v.end());
-      keys[l] = v;
-      for (int b = 0; b < (int)v.size(); ++b) index[l][v[b]] = b;
+    std::vector<uint64_t> tc(code.begin(), code.begin() + N);
+    std::vector<int> ti(cid.begin(), cid.begin() + N);
+    radix_sort_pairs(tc, ti, 3 * lm);
+    for (int l = kFmaMinLevel; l <= lm; ++l) {
+      const int sh = 3 * (lm - l);
+      size_t boxes = N > 0 ? 1 : 0;
+      for (int i = 1; i < N; ++i) boxes += (tc[i] >> sh) != (tc[i - 1] >> sh);
+      if ((double)N / (double)boxes < 16.0 && l > kFmaMinLevel) break;
+      L = l;
     }
+  }
+  F->L = L;
+  const double sL = S / (double)(1 << L);
+  // leaves: the distinct codes of rows and panels at level L, in code order;
+  // rows and panels of a leaf keep their index order (the sort is stable)
+  std::vector<int> tl(N), plf(C);
+  std::vector<std::vector<uint64_t>> codes(L + 1);
+  for (auto& c : code) c >>= 3 * (lm - L);
+  radix_sort_pairs(code, cid, 3 * L);
+  for (size_t e = 0; e < code.size(); ++e) {
+    if (e == 0 || code[e] != code[e - 1]) codes[L].push_back(code[e]);
+    const int b = (int)codes[L].size() - 1;
+    if (cid[e] < N) tl[cid[e]] = b;
+    else plf[cid[e] - N] = b;
+  }
+  for (int l = L - 1; l >= 0; --l)
+    for (const uint64_t c : codes[l + 1])
+      if (codes[l].empty() || codes[l].back() != c >> 3) codes[l].push_back(c >> 3);
+  std::vector<std::vector<Key3>> keys(L + 1);
+  std::vector<BoxIndex> index(L + 1);
+  for (int l = 0; l <= L; ++l) {
+    keys[l].resize(codes[l].size());
+    for (size_t b = 0; b < codes[l].size(); ++b) keys[l][b] = unmorton(codes[l][b]);
+    index[l].build(codes[l]);
   }
   auto adjacent = [](const Key3& a, const Key3& b) {
     return std::abs(a.x - b.x) <= 1 && std::abs(a.y - b.y) <= 1 && std::abs(a.z - b.z) <= 1;
@@ -1123,6 +1230,7 @@ static int fma_build(wbem_context* h, FmaState* F, const QuadTables& qt) {
   std::vector<int> gptr(F->total_boxes + 1, 0);
   std::vector<float> lvl_scale(L + 1);
   int il_off = 0;
+  std::vector<int> cptr, ch;  // children (CSR) of the previous level's boxes
   for (int l = 0; l <= L; ++l) {
     FmaLevel& V = F->lev[l];
     const double s = S / (double)(1 << l);
@@ -1140,20 +1248,22 @@ static int fma_build(wbem_context* h, FmaState* F, const QuadTables& qt) {
     if (l > 0) {
       V.parent.resize(V.nbox);
       V.oct.resize(V.nbox);
-      for (int b = 0; b < V.nbox; ++b) {
-        const Key3& k = keys[l][b];
-        V.parent[b] = index[l - 1].at({k.x >> 1, k.y >> 1, k.z >> 1});
-        V.oct[b] = (k.x & 1) * 4 + (k.y & 1) * 2 + (k.z & 1);
+      // both levels are in code order and a parent's code is the child's
+      // shifted by 3: one merge walk finds every parent
+      for (int b = 0, p = 0; b < V.nbox; ++b) {
+        while (codes[l - 1][p] != codes[l][b] >> 3) ++p;
+        V.parent[b] = p;
+        V.oct[b] = (int)(codes[l][b] & 7);
       }
       WB_CHK(fma_upload(h, F, &V.d_parent, V.parent));
       WB_CHK(fma_upload(h, F, &V.d_oct, V.oct));
       // children lists of the previous level
       FmaLevel& P = F->lev[l - 1];
-      std::vector<int> cptr(P.nbox + 1, 0), ch, coct;
+      cptr.assign(P.nbox + 1, 0);
+      ch.resize(V.nbox);
+      std::vector<int> coct(V.nbox);
       for (int b = 0; b < V.nbox; ++b) cptr[V.parent[b] + 1]++;
       for (int p = 0; p < P.nbox; ++p) cptr[p + 1] += cptr[p];
-      ch.resize(V.nbox);
-      coct.resize(V.nbox);
       std::vector<int> fill(cptr.begin(), cptr.end() - 1);
       for (int b = 0; b < V.nbox; ++b) {
         const int e = fill[V.parent[b]]++;
@@ -1175,13 +1285,11 @@ static int fma_build(wbem_context* h, FmaState* F, const QuadTables& qt) {
         for (int dx = -1; dx <= 1; ++dx)
           for (int dy = -1; dy <= 1; ++dy)
             for (int dz = -1; dz <= 1; ++dz) {
-              const Key3 pn{pk2.x + dx, pk2.y + dy, pk2.z + dz};
-              if (!index[l - 1].count(pn)) continue;
-              for (int o = 0; o < 8; ++o) {
-                const Key3 c2{2 * pn.x + (o >> 2), 2 * pn.y + ((o >> 1) & 1), 2 * pn.z + (o & 1)};
-                auto it = index[l].find(c2);
-                if (it != index[l].end() && !adjacent(c2, k)) il.push_back(it->second);
-              }
+              const int p = index[l - 1].find({pk2.x + dx, pk2.y + dy, pk2.z + dz}, l - 1);
+              if (p < 0) continue;
+              // the parent's children, in octant order
+              for (int e = cptr[p]; e < cptr[p + 1]; ++e)
+                if (!adjacent(keys[l][ch[e]], k)) il.push_back(ch[e]);
             }
         V.il_ptr[b + 1] = (int)il.size();
       }
@@ -1222,26 +1330,27 @@ static int fma_build(wbem_context* h, FmaState* F, const QuadTables& qt) {
     WB_CHK(fma_upload(h, F, &F->d_gptr, gptr));
     WB_CHK(fma_upload(h, F, &F->d_lvl_scale, lvl_scale));
     WB_CHK(fma_alloc(h, F, &F->d_part, (size_t)std::max(1, il_off) * n3));
-    WB_CHK(fma_alloc(h, F, &F->d_K, (size_t)kM2LOffsets * n3 * kMpSets * n3));
-    k_fma_m2l_ops<<<dim3(kM2LOffsets, n3), 128, 0, h->stream>>>(F->n, kFmaExpand / 2, F->d_K);
-    WB_CU(cudaGetLastError());
+    if (!F->d_K) {
+      WB_CHK(fma_alloc(h, F, &F->d_K, (size_t)kM2LOffsets * n3 * kMpSets * n3));
+      k_fma_m2l_ops<<<dim3(kM2LOffsets, n3), 128, 0, h->stream>>>(F->n, kFmaExpand / 2, F->d_K);
+      WB_CU(cudaGetLastError());
+    }
   }
   // leaves: panels per leaf, rows per leaf, neighbour leaves
   const FmaLevel& LV = F->lev[L];
   F->nleaf = LV.nbox;
-  std::vector<int> pptr(LV.nbox + 1, 0), pan(C), kleaf(C), ppos_of(C), tl(N);
-  for (int c = 0; c < C; ++c) pptr[index[L].at(pk[c]) + 1]++;
+  std::vector<int> pptr(LV.nbox + 1, 0), pan(C), kleaf(C), ppos_of(C);
+  for (int c = 0; c < C; ++c) pptr[plf[c] + 1]++;
   for (int b = 0; b < LV.nbox; ++b) pptr[b + 1] += pptr[b];
   {
     std::vector<int> fill(pptr.begin(), pptr.end() - 1);
     for (int c = 0; c < C; ++c) {
-      const int lf = index[L].at(pk[c]), k = fill[lf]++;
+      const int lf = plf[c], k = fill[lf]++;
       pan[k] = c;
       kleaf[k] = lf;
       ppos_of[c] = k;
     }
   }
-  for (int i = 0; i < N; ++i) tl[i] = index[L].at(tk[i]);
   std::vector<int> tptr(LV.nbox + 1, 0), tidx(N);
   for (int i = 0; i < N; ++i) tptr[tl[i] + 1]++;
   for (int b = 0; b < LV.nbox; ++b) tptr[b + 1] += tptr[b];
@@ -1255,8 +1364,8 @@ static int fma_build(wbem_context* h, FmaState* F, const QuadTables& qt) {
     for (int dx = -1; dx <= 1; ++dx)
       for (int dy = -1; dy <= 1; ++dy)
         for (int dz = -1; dz <= 1; ++dz) {
-          auto it = index[L].find({k.x + dx, k.y + dy, k.z + dz});
-          if (it != index[L].end()) nbl.push_back(it->second);
+          const int nbr = index[L].find({k.x + dx, k.y + dy, k.z + dz}, L);
+          if (nbr >= 0) nbl.push_back(nbr);
         }
     nbp[b + 1] = (int)nbl.size();
   }
@@ -1314,47 +1423,45 @@ static int fma_build(wbem_context* h, FmaState* F, const QuadTables& qt) {
   WB_CHK(fma_alloc(h, F, &F->d_geo, 4 * (size_t)C));
   k_fma_panel_geo<<<(C + 127) / 128, 128, 0, h->stream>>>(C, h->d_X, h->d_cell_dofs, F->d_geo);
   {
-    int* d_cnt = nullptr;
-    DeviceFreeGuard guard{{(void**)&d_cnt}};
+    int2 *d_cnt = nullptr, *d_lptr = nullptr;
+    DeviceFreeGuard guard{{(void**)&d_cnt, (void**)&d_lptr}};
     WB_CHK(dev_alloc(h, &d_cnt, (size_t)N));
     k_fma_close<<<(N + 127) / 128, 128, 0, h->stream>>>(
-        N, F->d_tgt_leaf, F->d_nb_ptr, F->d_nb, F->d_leaf_pptr, F->d_leaf_pan, h->d_X, F->d_geo,
-        h->d_sptr, h->d_scell, nullptr, d_cnt, nullptr, nullptr, nullptr);
-    std::vector<int> cnt(N), cptr(N + 1, 0);
-    WB_CU(cudaMemcpyAsync(cnt.data(), d_cnt, sizeof(int) * N, cudaMemcpyDeviceToHost, h->stream));
+        N, F->d_tidx, F->d_tgt_leaf, F->d_nb_ptr, F->d_nb, F->d_leaf_pptr, F->d_leaf_pan, h->d_X, F->d_geo,
+        h->d_sptr, h->d_scell, nullptr, nullptr, d_cnt, nullptr, nullptr, nullptr);
+    std::vector<int2> cnt(N), lptr(N);
+    std::vector<int> cptr(N + 1, 0);
+    WB_CU(cudaMemcpyAsync(cnt.data(), d_cnt, sizeof(int2) * N, cudaMemcpyDeviceToHost, h->stream));
     WB_CU(cudaStreamSynchronize(h->stream));
-    long long tot = 0;
+    // row offsets of the pairs, and of the correction list: the regular
+    // pairs (in pair order) first, then the singular ones (in pair order)
+    long long tot = 0, nreg = 0;
     for (int i = 0; i < N; ++i) {
-      tot += cnt[i];
+      tot += cnt[i].x;
       if (tot > 2000000000LL) return fail(h, WBEM_ERR_ARG, "FMA: more than 2e9 close pairs");
       cptr[i + 1] = (int)tot;
+      lptr[i].x = (int)nreg;
+      nreg += cnt[i].x - cnt[i].y;
+    }
+    for (int i = 0, ns = 0; i < N; ++i) {
+      lptr[i].y = (int)nreg + ns;
+      ns += cnt[i].y;
     }
     F->npairs = (size_t)tot;
+    F->n_regular = (size_t)nreg;
     WB_CHK(fma_upload(h, F, &F->d_close_ptr, cptr));
+    WB_CHK(upload(h, &d_lptr, lptr));
     WB_CHK(fma_alloc(h, F, &F->d_pair_row, std::max<size_t>(1, F->npairs)));
     WB_CHK(fma_alloc(h, F, &F->d_pair_pan, std::max<size_t>(1, F->npairs)));
     WB_CHK(fma_alloc(h, F, &F->d_close_val, 8 * std::max<size_t>(1, F->npairs)));
-    uint8_t* d_sing = nullptr;
-    guard.slots.push_back((void**)&d_sing);
-    WB_CHK(dev_alloc(h, &d_sing, std::max<size_t>(1, F->npairs)));
+    WB_CHK(fma_alloc(h, F, &F->d_plist, std::max<size_t>(1, F->npairs)));
     k_fma_close<<<(N + 127) / 128, 128, 0, h->stream>>>(
-        N, F->d_tgt_leaf, F->d_nb_ptr, F->d_nb, F->d_leaf_pptr, F->d_leaf_pan, h->d_X, F->d_geo,
-        h->d_sptr, h->d_scell, F->d_close_ptr, nullptr, F->d_pair_row, F->d_pair_pan, d_sing);
+        N, F->d_tidx, F->d_tgt_leaf, F->d_nb_ptr, F->d_nb, F->d_leaf_pptr, F->d_leaf_pan, h->d_X, F->d_geo,
+        h->d_sptr, h->d_scell, F->d_close_ptr, d_lptr, nullptr, F->d_pair_row, F->d_pair_pan,
+        F->d_plist);
     WB_CU(cudaGetLastError());
-    // the pair lists of the correction kernel: regular pairs, then singular
-    std::vector<uint8_t> sing(F->npairs);
-    if (F->npairs)
-      WB_CU(cudaMemcpyAsync(sing.data(), d_sing, F->npairs, cudaMemcpyDeviceToHost, h->stream));
+    // d_lptr is freed on return: the list pass must have read it
     WB_CU(cudaStreamSynchronize(h->stream));
-    std::vector<int> plist;
-    plist.reserve(F->npairs);
-    for (size_t k = 0; k < F->npairs; ++k)
-      if (!sing[k]) plist.push_back((int)k);
-    F->n_regular = plist.size();
-    for (size_t k = 0; k < F->npairs; ++k)
-      if (sing[k]) plist.push_back((int)k);
-    if (plist.empty()) plist.push_back(0);
-    WB_CHK(fma_upload(h, F, &F->d_plist, plist));
   }
   const int n = F->n;
   std::vector<double> t(n);
@@ -1484,17 +1591,33 @@ int assemble_fma(wbem_context* h, const QuadTables& qt) {
   const int nq = qt.q1 * qt.q1;
   FmaState* F = static_cast<FmaState*>(h->fma_state);
   if (!F || F->n != n || F->nq != nq || h->fma_geometry_stale) {
+    // the M2L operators depend on the order alone: a rebuild for moved
+    // nodes keeps them
+    float* keep_K = nullptr;
+    if (F && F->n == n && F->d_K) {
+      keep_K = F->d_K;
+      F->owned.erase(std::find(F->owned.begin(), F->owned.end(), (void*)keep_K));
+    }
     free_fma(h);
     F = new FmaState();
     F->n = n;
     F->nq = nq;
+    if (keep_K) {
+      F->d_K = keep_K;
+      F->owned.push_back(keep_K);
+    }
     h->fma_state = F;
+    const auto t0 = std::chrono::steady_clock::now();
     const int st = fma_build(h, F, qt);
     if (st != WBEM_OK) {
       free_fma(h);
       return st;
     }
+    h->stats.t_assemble_ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     h->fma_geometry_stale = false;
+  } else {
+    h->stats.t_assemble_ms = 0.0;  // the tree and lists of the last build still hold
   }
   if (h->rec_cells != (size_t)C * nq || !h->d_rec) {
     WB_CHK(dev_alloc(h, &h->d_rec, (size_t)C * nq * 8));
