@@ -592,14 +592,18 @@ __device__ __forceinline__ uint64_t smem_desc_sw64(uint32_t saddr) {
          ((uint64_t)1 << 46) | ((uint64_t)4 << 61);
 }
 
-// Barrier of one epilogue group (named barrier 1 + group, 128 threads).
+// Barrier of one epilogue group (named barrier 1 + group, 128 threads). The
+// barrier form is warp-aligned: the warp is reconverged first (one lane of
+// the group issues the C copies in branches of its own).
 __device__ __forceinline__ void named_bar_epi(int g) {
+  __syncwarp();
   asm volatile("bar.sync %0, 128;" ::"r"(1 + g) : "memory");
 }
 // The same barrier, also ORing a flag across the group, so every thread of
 // the group takes the same branch after it.
 __device__ __forceinline__ bool named_bar_epi_or(int g, bool v) {
   uint32_t r;
+  __syncwarp();
   asm volatile(
       "{\n .reg .pred p, q;\n setp.ne.u32 p, %2, 0;\n bar.red.or.pred q, %1, 128, p;\n selp.u32 %0, "
       "1, 0, q;\n}\n"
