@@ -145,11 +145,16 @@ def test_fma_sphere_and_moved_nodes():
     g.assemble_system()
     f = _fma(m, ptr, idx, 8)
     f.assemble_system()
+    # the octree and lists are built by the first assembly only
+    assert f.stats()["t_assemble_ms"] > 0
+    f.assemble_system()
+    assert f.stats()["t_assemble_ms"] == 0
     e1 = rel2(f.vmult(v), g.vmult(v))
     # a smooth displacement of every node (double nodes move together)
     X2 = m.X * (1.0 + 0.05 * np.sin(3.0 * m.X[:, :1]))
     f.update_nodes(X2)
     f.assemble_system()
+    assert f.stats()["t_assemble_ms"] > 0  # rebuilt for the moved nodes
     fresh = BEMProblem(X2, m.cells, m.dirichlet, ptr, idx, method=METHOD_FMA, fma_order=8)
     fresh.assemble_system()
     assert np.array_equal(f.vmult(v), fresh.vmult(v))
