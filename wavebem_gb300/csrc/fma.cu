@@ -159,6 +159,11 @@ __global__ void k_fma_close(int N, const int* __restrict__ tidx, const int* __re
   const int t = tgt_leaf[i];
   const int base = ptr ? ptr[i] : 0;
   const int2 lp = ptr ? lptr[i] : make_int2(0, 0);
+  // the row's singular cells, in registers when there are at most 16
+  const int s0 = sptr[i], nsr = sptr[i + 1] - s0;
+  int sc[16];
+#pragma unroll
+  for (int q = 0; q < 16; ++q) sc[q] = q < nsr ? scell[s0 + q] : -1;
   int c = 0, ns = 0;
   for (int e = nb_ptr[t]; e < nb_ptr[t + 1]; ++e) {
     const int s = nb[e];
@@ -167,7 +172,12 @@ __global__ void k_fma_close(int N, const int* __restrict__ tidx, const int* __re
       const double* g = geo + 4 * (size_t)cell;
       const double dx = g[0] - xi, dy = g[1] - yi, dz = g[2] - zi;
       bool sing = false;  // a double-node partner of the row is a vertex of the panel
-      for (int m = sptr[i]; m < sptr[i + 1] && !sing; ++m) sing = scell[m] == cell;
+      if (nsr <= 16) {
+#pragma unroll
+        for (int q = 0; q < 16; ++q) sing |= sc[q] == cell;
+      } else {
+        for (int m = s0; m < s0 + nsr && !sing; ++m) sing = scell[m] == cell;
+      }
       const bool close = sing || dx * dx + dy * dy + dz * dz < 12.0 * g[3] * g[3];
       if (!close) continue;
       if (ptr) {
