@@ -1522,8 +1522,11 @@ int assemble_fma(wbem_context* h, const QuadTables& qt) {
     // nodes keeps them
     float* keep_K = nullptr;
     if (F && F->n == n && F->d_K) {
-      keep_K = F->d_K;
-      F->owned.erase(std::find(F->owned.begin(), F->owned.end(), (void*)keep_K));
+      const auto it = std::find(F->owned.begin(), F->owned.end(), (void*)F->d_K);
+      if (it != F->owned.end()) {
+        keep_K = F->d_K;
+        F->owned.erase(it);
+      }
     }
     free_fma(h);
     F = new FmaState();
