@@ -15,6 +15,8 @@
 #include <vector>
 #include "context.h"
 #include "host_util.h"
+#include "fma_tree.h"
+#include "quadrature_rules.h"
 #include "../../include/wbem_kernels.h"
 
 using namespace wbem;
@@ -74,32 +76,6 @@ int check_device_error(wbem_context* h, const char* what) {
 }  // namespace wbem
 
 // ------------------------------------------------------------ quadrature
-// Gauss-Legendre points and weights on [0,1] (Newton on the Legendre
-// recurrence), ascending.
-static void gauss_legendre01(int n, std::vector<double>& x, std::vector<double>& w) {
-  x.resize(n);
-  w.resize(n);
-  const long double pi = 3.141592653589793238462643383279502884L;
-  for (int i = 0; i < n; ++i) {
-    long double z = cosl(pi * (i + 0.75L) / (n + 0.5L)), dp = 1;
-    for (int it = 0; it < 100; ++it) {
-      // P_n(z) and P_{n-1}(z) by the three-term recurrence
-      long double pn = (n == 0) ? 1 : z, pm = 1;
-      for (int k = 2; k <= n; ++k) {
-        long double pk = ((2 * k - 1) * z * pn - (k - 1) * pm) / k;
-        pm = pn;
-        pn = pk;
-      }
-      dp = n * (z * pn - pm) / (z * z - 1);
-      long double dz = pn / dp;
-      z -= dz;
-      if (fabsl(dz) < 1e-20L) break;
-    }
-    x[i] = (double)((1 - z) / 2);
-    w[i] = (double)(1 / ((1 - z * z) * dp * dp));
-  }
-}
-
 static int build_quadrature(wbem_context* h, int q1, int sorder) {
   if (q1 < 1 || q1 > kMaxQ1) return fail(h, WBEM_ERR_ARG, "quadrature_order must be in [1,8]");
   if (sorder < 1 || 2 * sorder * sorder > kMaxSingular)
@@ -107,7 +83,7 @@ static int build_quadrature(wbem_context* h, int q1, int sorder) {
   QuadTables t{};
   t.q1 = q1;
   std::vector<double> x, w;
-  gauss_legendre01(q1, x, w);
+  quad::gauss_legendre01(q1, x, w);
   h->gauss_n = q1;
   for (int a = 0; a < q1; ++a) {
     h->gauss_x[a] = x[a];
@@ -129,29 +105,16 @@ static int build_quadrature(wbem_context* h, int q1, int sorder) {
     }
   // vertex-singular rules (polar map of the two triangles at the vertex, with
   // the 1/R weight folded into the weights), see the oracle for the derivation
-  std::vector<double> sx, sw;
-  gauss_legendre01(sorder, sx, sw);
   const int m = sorder * sorder;
   t.nsp = 2 * m;
-  const double pi4 = 0.78539816339744830962;
   for (int v = 0; v < 4; ++v) {
-    for (int b = 0; b < sorder; ++b)
-      for (int a = 0; a < sorder; ++a) {
-        const int q = a + sorder * b;
-        const double u = sx[a], th = pi4 * sx[b];
-        const double px = u, py = u * std::tan(th);
-        double wq = sw[a] * sw[b] * pi4 / std::cos(th) * std::sqrt(px * px + py * py);
-        double pts[2][2] = {{px, py}, {py, px}};
-        for (int half = 0; half < 2; ++half) {
-          double X0 = pts[half][0], Y0 = pts[half][1], Xr = X0, Yr = Y0;
-          if (v == 1) { Xr = 1 - Y0; Yr = X0; }
-          if (v == 2) { Xr = Y0; Yr = 1 - X0; }
-          if (v == 3) { Xr = 1 - X0; Yr = 1 - Y0; }
-          t.sp[v][half * m + q][0] = Xr;
-          t.sp[v][half * m + q][1] = Yr;
-          t.sp[v][half * m + q][2] = wq;
-        }
-      }
+    std::vector<double> px, py, pw;
+    quad::vertex_singular_points(sorder, v, px, py, pw);
+    for (int k = 0; k < 2 * m; ++k) {
+      t.sp[v][k][0] = px[k];
+      t.sp[v][k][1] = py[k];
+      t.sp[v][k][2] = pw[k];
+    }
   }
   CU(upload_quadrature_fp64(t));
   CU(upload_quadrature_mixed(t));
@@ -216,16 +179,6 @@ static void find_double_nodes(int N, const double* X, int C, const int* cells,
   }
 }
 
-static uint64_t spread21(uint64_t v) {
-  v &= 0x1fffffULL;
-  v = (v | (v << 32)) & 0x1f00000000ffffULL;
-  v = (v | (v << 16)) & 0x1f0000ff0000ffULL;
-  v = (v | (v << 8)) & 0x100f00f00f00f00fULL;
-  v = (v | (v << 4)) & 0x10c30c30c30c30c3ULL;
-  v = (v | (v << 2)) & 0x1249249249249249ULL;
-  return v;
-}
-
 // Morton (Z-order) of the support points: the seed order of the patches
 // below.
 static void morton_order(int N, const double* X, std::vector<int>& perm, std::vector<int>& iperm) {
@@ -245,7 +198,8 @@ static void morton_order(int N, const double* X, std::vector<int>& perm, std::ve
       t = std::min(std::max(t, 0.0), 1.0);
       q[d] = (uint64_t)(t * 2097151.0);
     }
-    k[i] = {spread21(q[0]) | (spread21(q[1]) << 1) | (spread21(q[2]) << 2), i};
+    k[i] = {fma_tree::spread3((uint32_t)q[0]) | (fma_tree::spread3((uint32_t)q[1]) << 1) |
+                (fma_tree::spread3((uint32_t)q[2]) << 2), i};
   }
   std::sort(k.begin(), k.end());
   perm.resize(N);
