@@ -1,6 +1,7 @@
 // CPU checks of the FMA octree's host helpers (wavebem_gb300/csrc/fma_tree.h),
 // compiled and run by tests/test_fma_tree.py. Prints "ok" and exits 0 when
 // every check holds.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <map>
@@ -108,6 +109,70 @@ int main() {
       bad += (km >> (lm - l)) != kl;
     }
     CHECK(bad == 0, "key shift identity");
+  }
+  // tree links and interaction lists over leaves on a sphere shell (a
+  // surface, as a BEM mesh): every pair of leaves is either adjacent at the
+  // leaf level (the near field) or covered by exactly one M2L entry between
+  // their ancestors, never both
+  for (int L = 3; L <= 5; ++L) {
+    const int mn = 2;
+    std::normal_distribution<double> nd;
+    std::vector<uint64_t> leaf;
+    for (int t = 0; t < 20000; ++t) {
+      double d[3] = {nd(g), nd(g), nd(g)};
+      const double r = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+      int k[3];
+      for (int e = 0; e < 3; ++e)
+        k[e] = std::min((1 << L) - 1, std::max(0, (int)std::floor((0.5 + 0.4 * d[e] / r) * (1 << L))));
+      leaf.push_back(morton(Key3{k[0], k[1], k[2]}));
+    }
+    std::sort(leaf.begin(), leaf.end());
+    leaf.erase(std::unique(leaf.begin(), leaf.end()), leaf.end());
+    std::vector<std::vector<uint64_t>> codes(L + 1);
+    codes[L] = leaf;
+    for (int l = L - 1; l >= 0; --l) codes[l] = coarser_codes(codes[l + 1]);
+    std::vector<std::vector<Key3>> keys(L + 1);
+    std::vector<BoxIndex> index(L + 1);
+    for (int l = 0; l <= L; ++l) {
+      for (const uint64_t c : codes[l]) keys[l].push_back(unmorton(c));
+      index[l].build(codes[l]);
+    }
+    std::vector<LevelLinks> lk(L + 1);
+    for (int l = 0; l <= L; ++l)
+      link_level(l, mn, codes[l], keys[l], l > 0 ? codes[l - 1] : codes[l], l > 0 ? &index[l - 1] : nullptr,
+                 lk[l]);
+    bool links_ok = codes[0].size() == 1;
+    for (int l = 1; l <= L; ++l) {
+      for (size_t b = 0; b < codes[l].size(); ++b)
+        links_ok &= codes[l - 1][lk[l].parent[b]] == codes[l][b] >> 3 &&
+                    lk[l].oct[b] == (int)(codes[l][b] & 7);
+      for (size_t p = 0; p + 1 < lk[l].cptr.size(); ++p)
+        for (int e = lk[l].cptr[p]; e < lk[l].cptr[p + 1]; ++e)
+          links_ok &= lk[l].parent[lk[l].ch[e]] == (int)p && lk[l].coct[e] == lk[l].oct[lk[l].ch[e]] &&
+                      (e == lk[l].cptr[p] || lk[l].ch[e] > lk[l].ch[e - 1]);
+    }
+    CHECK(links_ok, "parents, octants and children");
+    const int nl = (int)leaf.size();
+    std::vector<std::vector<int>> anc(L + 1, std::vector<int>(nl));
+    for (int b = 0; b < nl; ++b) anc[L][b] = b;
+    for (int l = L - 1; l >= 0; --l)
+      for (int b = 0; b < nl; ++b) anc[l][b] = lk[l + 1].parent[anc[l + 1][b]];
+    std::vector<std::vector<char>> m2l(L + 1);
+    for (int l = mn; l <= L; ++l) {
+      const size_t nb = codes[l].size();
+      m2l[l].assign(nb * nb, 0);
+      for (size_t t = 0; t < nb; ++t)
+        for (int e = lk[l].il_ptr[t]; e < lk[l].il_ptr[t + 1]; ++e) m2l[l][t * nb + lk[l].il[e]]++;
+    }
+    long bad = 0;
+    for (int t = 0; t < nl; ++t)
+      for (int s2 = 0; s2 < nl; ++s2) {
+        int cover = 0;
+        for (int l = mn; l <= L; ++l) cover += m2l[l][(size_t)anc[l][t] * codes[l].size() + anc[l][s2]];
+        const bool near = adjacent(keys[L][t], keys[L][s2]);
+        bad += near ? cover != 0 : cover != 1;
+      }
+    CHECK(bad == 0, "near field and interaction lists cover every pair of leaves once");
   }
   if (fails) return 1;
   std::printf("ok\n");

@@ -1129,9 +1129,7 @@ static int fma_build(wbem_context* h, FmaState* F, const QuadTables& qt) {
     if (cid[e] < N) tl[cid[e]] = b;
     else plf[cid[e] - N] = b;
   }
-  for (int l = L - 1; l >= 0; --l)
-    for (const uint64_t c : codes[l + 1])
-      if (codes[l].empty() || codes[l].back() != c >> 3) codes[l].push_back(c >> 3);
+  for (int l = L - 1; l >= 0; --l) codes[l] = coarser_codes(codes[l + 1]);
   std::vector<std::vector<Key3>> keys(L + 1);
   std::vector<BoxIndex> index(L + 1);
   for (int l = 0; l <= L; ++l) {
@@ -1139,9 +1137,6 @@ static int fma_build(wbem_context* h, FmaState* F, const QuadTables& qt) {
     for (size_t b = 0; b < codes[l].size(); ++b) keys[l][b] = unmorton(codes[l][b]);
     index[l].build(codes[l]);
   }
-  auto adjacent = [](const Key3& a, const Key3& b) {
-    return std::abs(a.x - b.x) <= 1 && std::abs(a.y - b.y) <= 1 && std::abs(a.z - b.z) <= 1;
-  };
   F->lev.assign(L + 1, FmaLevel{});
   const int n3 = F->n * F->n * F->n;
   std::vector<int> box_off(L + 2, 0);
@@ -1157,7 +1152,6 @@ static int fma_build(wbem_context* h, FmaState* F, const QuadTables& qt) {
   std::vector<int> gptr(F->total_boxes + 1, 0);
   std::vector<float> lvl_scale(L + 1);
   int il_off = 0;
-  std::vector<int> cptr, ch;  // children (CSR) of the previous level's boxes
   for (int l = 0; l <= L; ++l) {
     FmaLevel& V = F->lev[l];
     const double s = S / (double)(1 << l);
@@ -1172,55 +1166,21 @@ static int fma_build(wbem_context* h, FmaState* F, const QuadTables& qt) {
     WB_CHK(fma_upload(h, F, &V.d_cen, cen));
     V.d_W = F->d_Wall + (size_t)box_off[l] * kMpSets * n3;
     V.d_L = F->d_Lall + (size_t)box_off[l] * n3;
+    LevelLinks lk;
+    link_level(l, kFmaMinLevel, codes[l], keys[l], l > 0 ? codes[l - 1] : codes[l],
+               l > 0 ? &index[l - 1] : nullptr, lk);
     if (l > 0) {
-      V.parent.resize(V.nbox);
-      V.oct.resize(V.nbox);
-      // both levels are in code order and a parent's code is the child's
-      // shifted by 3: one merge walk finds every parent
-      for (int b = 0, p = 0; b < V.nbox; ++b) {
-        while (codes[l - 1][p] != codes[l][b] >> 3) ++p;
-        V.parent[b] = p;
-        V.oct[b] = (int)(codes[l][b] & 7);
-      }
+      V.parent = lk.parent;
+      V.oct = lk.oct;
       WB_CHK(fma_upload(h, F, &V.d_parent, V.parent));
       WB_CHK(fma_upload(h, F, &V.d_oct, V.oct));
-      // children lists of the previous level
       FmaLevel& P = F->lev[l - 1];
-      cptr.assign(P.nbox + 1, 0);
-      ch.resize(V.nbox);
-      std::vector<int> coct(V.nbox);
-      for (int b = 0; b < V.nbox; ++b) cptr[V.parent[b] + 1]++;
-      for (int p = 0; p < P.nbox; ++p) cptr[p + 1] += cptr[p];
-      std::vector<int> fill(cptr.begin(), cptr.end() - 1);
-      for (int b = 0; b < V.nbox; ++b) {
-        const int e = fill[V.parent[b]]++;
-        ch[e] = b;
-        coct[e] = V.oct[b];
-      }
-      WB_CHK(fma_upload(h, F, &P.d_child_ptr, cptr));
-      WB_CHK(fma_upload(h, F, &P.d_child, ch));
-      WB_CHK(fma_upload(h, F, &P.d_child_oct, coct));
+      WB_CHK(fma_upload(h, F, &P.d_child_ptr, lk.cptr));
+      WB_CHK(fma_upload(h, F, &P.d_child, lk.ch));
+      WB_CHK(fma_upload(h, F, &P.d_child_oct, lk.coct));
     }
-    // interaction lists: children of the parent's neighbours (the parent
-    // included) that are not adjacent to the box
-    V.il_ptr.assign(V.nbox + 1, 0);
-    std::vector<int> il;
-    if (l >= kFmaMinLevel) {
-      for (int b = 0; b < V.nbox; ++b) {
-        const Key3& k = keys[l][b];
-        const Key3 pk2{k.x >> 1, k.y >> 1, k.z >> 1};
-        for (int dx = -1; dx <= 1; ++dx)
-          for (int dy = -1; dy <= 1; ++dy)
-            for (int dz = -1; dz <= 1; ++dz) {
-              const int p = index[l - 1].find({pk2.x + dx, pk2.y + dy, pk2.z + dz}, l - 1);
-              if (p < 0) continue;
-              // the parent's children, in octant order
-              for (int e = cptr[p]; e < cptr[p + 1]; ++e)
-                if (!adjacent(keys[l][ch[e]], k)) il.push_back(ch[e]);
-            }
-        V.il_ptr[b + 1] = (int)il.size();
-      }
-    }
+    V.il_ptr = lk.il_ptr;
+    const std::vector<int>& il = lk.il;
     lvl_scale[l] = (float)(1.0 / s);
     for (int b = 0; b < V.nbox; ++b) {
       const Key3& kt = keys[l][b];

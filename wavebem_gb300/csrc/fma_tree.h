@@ -5,6 +5,7 @@
 #pragma once
 #include <stdint.h>
 #include <algorithm>
+#include <cstdlib>
 #include <cstddef>
 #include <vector>
 
@@ -96,6 +97,76 @@ struct BoxIndex {
     }
   }
 };
+
+// Boxes of the next coarser level: the distinct codes of `finer` shifted
+// right by 3, in code order (finer is in code order, so equal parents are
+// consecutive).
+inline std::vector<uint64_t> coarser_codes(const std::vector<uint64_t>& finer) {
+  std::vector<uint64_t> c;
+  for (const uint64_t f : finer)
+    if (c.empty() || c.back() != f >> 3) c.push_back(f >> 3);
+  return c;
+}
+
+inline bool adjacent(const Key3& a, const Key3& b) {
+  return std::abs(a.x - b.x) <= 1 && std::abs(a.y - b.y) <= 1 && std::abs(a.z - b.z) <= 1;
+}
+
+// Links of level l (boxes `codes` / `keys` in code order) to level l - 1
+// (boxes `prev`, looked up through `prev_index`):
+//   parent, oct  the parent box and octant of each box (l > 0);
+//   cptr, ch, coct  the children of each box of level l - 1 (CSR; in code
+//                 order, which is octant order), with their octants;
+//   il_ptr, il   the interaction list of each box (CSR), for l >= min_level:
+//                the children of the parent's neighbours (the parent
+//                included) that are not adjacent to the box, neighbours in
+//                (dx, dy, dz) order and children in octant order.
+struct LevelLinks {
+  std::vector<int> parent, oct, cptr, ch, coct, il_ptr, il;
+};
+inline void link_level(int l, int min_level, const std::vector<uint64_t>& codes,
+                       const std::vector<Key3>& keys, const std::vector<uint64_t>& prev,
+                       const BoxIndex* prev_index, LevelLinks& k) {
+  const int nbox = (int)codes.size();
+  k = LevelLinks{};
+  k.il_ptr.assign(nbox + 1, 0);
+  if (l == 0) return;
+  k.parent.resize(nbox);
+  k.oct.resize(nbox);
+  // both levels are in code order and a parent's code is the child's
+  // shifted by 3: one merge walk finds every parent
+  for (int b = 0, p = 0; b < nbox; ++b) {
+    while (prev[p] != codes[b] >> 3) ++p;
+    k.parent[b] = p;
+    k.oct[b] = (int)(codes[b] & 7);
+  }
+  const int np = (int)prev.size();
+  k.cptr.assign(np + 1, 0);
+  k.ch.resize(nbox);
+  k.coct.resize(nbox);
+  for (int b = 0; b < nbox; ++b) k.cptr[k.parent[b] + 1]++;
+  for (int p = 0; p < np; ++p) k.cptr[p + 1] += k.cptr[p];
+  std::vector<int> fill(k.cptr.begin(), k.cptr.end() - 1);
+  for (int b = 0; b < nbox; ++b) {
+    const int e = fill[k.parent[b]]++;
+    k.ch[e] = b;
+    k.coct[e] = k.oct[b];
+  }
+  if (l < min_level) return;
+  for (int b = 0; b < nbox; ++b) {
+    const Key3& kb = keys[b];
+    const Key3 pk{kb.x >> 1, kb.y >> 1, kb.z >> 1};
+    for (int dx = -1; dx <= 1; ++dx)
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dz = -1; dz <= 1; ++dz) {
+          const int p = prev_index->find({pk.x + dx, pk.y + dy, pk.z + dz}, l - 1);
+          if (p < 0) continue;
+          for (int e = k.cptr[p]; e < k.cptr[p + 1]; ++e)
+            if (!adjacent(keys[k.ch[e]], kb)) k.il.push_back(k.ch[e]);
+        }
+    k.il_ptr[b + 1] = (int)k.il.size();
+  }
+}
 
 }  // namespace fma_tree
 }  // namespace wbem
